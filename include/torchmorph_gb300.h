@@ -1,0 +1,162 @@
+/*
+ * torchmorph_gb300 -- C ABI of the GB300 (sm_103a) morphology, distance
+ * transform and Sinkhorn kernels.
+ *
+ * The library (libtmcore.so) is the drop-in replacement for the reference's
+ * pybind11 module `torchmorph._C` (torchmorph/csrc/torchmorph.cpp:79-155).
+ * Every entry point takes plain device pointers, sizes and a CUDA stream; no
+ * torch types cross this boundary.  Each declaration names the reference
+ * function it replaces.
+ *
+ * Conventions
+ *   - An "item" is one (b, c) slice of the reference's (B, C, *spatial)
+ *     tensors; `batch` = B*C items are laid out back to back, each a
+ *     C-contiguous array of `ndim` (1..8) spatial dimensions `shape`.
+ *   - Index outputs are int32 planes laid out (ndim, batch, *shape), the
+ *     layout of the reference's `indices` tensors.
+ *   - Structuring elements, footprints, origins and sampling are HOST
+ *     arrays (the reference passes them as CPU tensors / Python lists).
+ *   - Work is enqueued on `stream` of the CURRENT device; calls are
+ *     asynchronous unless stated otherwise.  The caller selects the device.
+ *   - Every function returns a tm_status; on failure tm_last_error() holds
+ *     a message for the calling thread.
+ *   - Functions that need temporary device memory take a caller-owned
+ *     `workspace` of at least the size its *_workspace_size() companion
+ *     returns; the library itself never allocates device memory.
+ */
+#ifndef TORCHMORPH_GB300_H
+#define TORCHMORPH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *tm_stream_t; /* same type as cudaStream_t */
+
+typedef enum tm_status {
+    TM_OK = 0,
+    TM_ERR_INVALID_ARGUMENT = 1, /* bad shape, pointer, origin, mode, ...   */
+    TM_ERR_UNSUPPORTED = 2,      /* valid request this build does not serve */
+    TM_ERR_CUDA = 3,             /* a CUDA runtime call or launch failed    */
+    TM_ERR_TOO_LARGE = 4,        /* sizes overflow the kernel's index types */
+    TM_ERR_WORKSPACE = 5,        /* workspace missing or too small          */
+    TM_ERR_TIMEOUT = 6           /* a bounded device-side wait gave up       */
+} tm_status;
+
+/* Border modes of the grey operators (torchmorph/morphology/grey.py:8-14). */
+typedef enum tm_border_mode {
+    TM_MODE_CONSTANT = 0,
+    TM_MODE_REFLECT = 1,
+    TM_MODE_NEAREST = 2,
+    TM_MODE_MIRROR = 3,
+    TM_MODE_WRAP = 4
+} tm_border_mode;
+
+/* Element types accepted by the distance transforms' foreground input. */
+typedef enum tm_dtype { TM_F32 = 0, TM_U8 = 1 } tm_dtype;
+
+/* Chamfer metrics (torchmorph/distance_transform.py:121-123) plus the
+ * weighted 3-4-5 chamfer, which the reference does not have. */
+typedef enum tm_cdt_metric {
+    TM_CDT_CHESSBOARD = 0,
+    TM_CDT_TAXICAB = 1,
+    TM_CDT_CHAMFER345 = 2
+} tm_cdt_metric;
+
+/* Brute-force metrics (torchmorph/csrc/bfdt_kernel.cu:167-171). */
+typedef enum tm_bf_metric { TM_BF_EUCLIDEAN = 0, TM_BF_TAXICAB = 1, TM_BF_CHESSBOARD = 2 } tm_bf_metric;
+
+const char *tm_status_string(int status);
+const char *tm_last_error(void);
+int tm_version(void);
+
+/* ------------------------------------------------------------------ grey --
+ * Replaces grey_erosion_cuda / grey_dilation_cuda
+ * (torchmorph/csrc/torchmorph.cpp:3-19, torchmorph/csrc/grey_kernel.cu:332-356).
+ * structure: float32[prod(sshape)] host; footprint: uint8[prod(sshape)]
+ * host or NULL (all active); origin: int64[ndim] host.
+ * in/out: float32 device, batch*prod(shape) elements; out must not alias in.
+ */
+int tm_grey_erosion(const float *in, float *out, int64_t batch, int ndim,
+                    const int64_t *shape, const float *structure, const uint8_t *footprint,
+                    const int64_t *sshape, const int64_t *origin, int mode, float cval,
+                    tm_stream_t stream);
+int tm_grey_dilation(const float *in, float *out, int64_t batch, int ndim,
+                     const int64_t *shape, const float *structure, const uint8_t *footprint,
+                     const int64_t *sshape, const int64_t *origin, int mode, float cval,
+                     tm_stream_t stream);
+
+/* ---------------------------------------------------------------- binary --
+ * Replaces binary_erosion_cuda / binary_dilation_cuda
+ * (torchmorph/csrc/torchmorph.cpp:21-33, torchmorph/csrc/binary_kernel.cu:252-272).
+ * in/out: uint8 (torch.bool) device arrays holding 0/1; structure: uint8 host.
+ */
+int tm_binary_erosion(const uint8_t *in, uint8_t *out, int64_t batch, int ndim,
+                      const int64_t *shape, const uint8_t *structure, const int64_t *sshape,
+                      const int64_t *origin, int border_value, tm_stream_t stream);
+int tm_binary_dilation(const uint8_t *in, uint8_t *out, int64_t batch, int ndim,
+                       const int64_t *shape, const uint8_t *structure, const int64_t *sshape,
+                       const int64_t *origin, int border_value, tm_stream_t stream);
+
+/* ------------------------------------------------------------------- edt --
+ * Replaces edt_cuda (torchmorph/csrc/torchmorph.cpp:35-40,
+ * torchmorph/csrc/edt_kernel.cu:904-958).
+ * input: device array of `in_dtype`, nonzero = foreground.
+ * sampling: float32[ndim] host or NULL (unit spacing).
+ * dist: float32 device or NULL; indices: int32 (ndim, batch, *shape) or NULL;
+ * sqdist: int32 squared distances (unit spacing only) or NULL -- an output
+ * the reference does not have.  At least one output must be given.
+ * Feature indices follow scipy.ndimage: nearest background voxel, ties to
+ * the smallest last-axis coordinate, then the previous axis, and so on.
+ */
+size_t tm_edt_workspace_size(int64_t batch, int ndim, const int64_t *shape);
+int tm_edt(const void *input, int in_dtype, int64_t batch, int ndim, const int64_t *shape,
+           const float *sampling, float *dist, int32_t *indices, int32_t *sqdist,
+           void *workspace, size_t workspace_bytes, tm_stream_t stream);
+
+/* ------------------------------------------------------------------- cdt --
+ * Replaces cdt_cuda (torchmorph/csrc/torchmorph.cpp:42-47,
+ * torchmorph/csrc/cdt_kernel.cu:269-463).
+ * dist: float32 (path cost; -1 where an item has no background) or NULL;
+ * for TM_CDT_CHAMFER345 the cost is divided by 3.  indices as for tm_edt.
+ */
+size_t tm_cdt_workspace_size(int64_t batch, int ndim, const int64_t *shape);
+int tm_cdt(const void *input, int in_dtype, int64_t batch, int ndim, const int64_t *shape,
+           int metric, float *dist, int32_t *indices, void *workspace, size_t workspace_bytes,
+           tm_stream_t stream);
+
+/* ------------------------------------------------------------------ bfdt --
+ * Replaces bfdt_cuda (torchmorph/csrc/torchmorph.cpp:49-55,
+ * torchmorph/csrc/bfdt_kernel.cu:154-297).
+ */
+size_t tm_bfdt_workspace_size(int64_t batch, int ndim, const int64_t *shape);
+int tm_bfdt(const void *input, int in_dtype, int64_t batch, int ndim, const int64_t *shape,
+            int metric, const float *sampling, float *dist, int32_t *indices,
+            void *workspace, size_t workspace_bytes, tm_stream_t stream);
+
+/* -------------------------------------------------------------- sinkhorn --
+ * Replaces sinkhorn_fastiter (torchmorph/csrc/torchmorph.cpp:58-66,
+ * torchmorph/csrc/ot_kernel.cu:188-233): n_iter scaling iterations
+ * u = a / (K v + 1e-12), v = b / (K^T u + 1e-12) on (n, d) batches sharing
+ * K (d, d).  u and v are updated in place.
+ */
+int tm_sinkhorn_fastiter(const float *a, const float *b, const float *K, const float *K_T,
+                         float *u, float *v, int64_t n, int64_t d, int64_t n_iter,
+                         tm_stream_t stream);
+
+/* Replaces sinkhorn_logiter (torchmorph/csrc/torchmorph.cpp:68-77,
+ * torchmorph/csrc/ot_kernel.cu:235-283): n_iter log-domain iterations
+ * log_u = log_a - LSE_j(-M_ij/eps + log_v_j), then the same for log_v with M_T.
+ */
+int tm_sinkhorn_logiter(const float *log_a, const float *log_b, const float *M,
+                        const float *M_T, float *log_u, float *log_v, int64_t n, int64_t d,
+                        int64_t n_iter, double epsilon, tm_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TORCHMORPH_GB300_H */

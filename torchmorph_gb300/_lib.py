@@ -1,0 +1,123 @@
+"""ctypes binding of libtmcore.so, the C-ABI CUDA library (include/torchmorph_gb300.h).
+
+The library is loaded once per process.  There is no fallback: if the shared
+object is missing or fails to load, every operator raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import torch
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libtmcore.so")
+
+_lib = None
+_lock = threading.Lock()
+
+c_i64 = ctypes.c_int64
+c_int = ctypes.c_int
+c_void = ctypes.c_void_p
+c_size = ctypes.c_size_t
+c_float = ctypes.c_float
+c_double = ctypes.c_double
+I64P = ctypes.POINTER(ctypes.c_int64)
+F32P = ctypes.POINTER(ctypes.c_float)
+U8P = ctypes.POINTER(ctypes.c_uint8)
+
+# name -> (restype, argtypes); mirrors include/torchmorph_gb300.h
+SIGNATURES = {
+    "tm_status_string": (ctypes.c_char_p, [c_int]),
+    "tm_last_error": (ctypes.c_char_p, []),
+    "tm_version": (c_int, []),
+    "tm_grey_erosion": (c_int, [c_void, c_void, c_i64, c_int, I64P, F32P, U8P, I64P, I64P, c_int,
+                                c_float, c_void]),
+    "tm_grey_dilation": (c_int, [c_void, c_void, c_i64, c_int, I64P, F32P, U8P, I64P, I64P, c_int,
+                                 c_float, c_void]),
+    "tm_binary_erosion": (c_int, [c_void, c_void, c_i64, c_int, I64P, U8P, I64P, I64P, c_int,
+                                  c_void]),
+    "tm_binary_dilation": (c_int, [c_void, c_void, c_i64, c_int, I64P, U8P, I64P, I64P, c_int,
+                                   c_void]),
+    "tm_edt_workspace_size": (c_size, [c_i64, c_int, I64P]),
+    "tm_edt": (c_int, [c_void, c_int, c_i64, c_int, I64P, F32P, c_void, c_void, c_void, c_void,
+                       c_size, c_void]),
+    "tm_cdt_workspace_size": (c_size, [c_i64, c_int, I64P]),
+    "tm_cdt": (c_int, [c_void, c_int, c_i64, c_int, I64P, c_int, c_void, c_void, c_void, c_size,
+                       c_void]),
+    "tm_bfdt_workspace_size": (c_size, [c_i64, c_int, I64P]),
+    "tm_bfdt": (c_int, [c_void, c_int, c_i64, c_int, I64P, c_int, F32P, c_void, c_void, c_void,
+                        c_size, c_void]),
+    "tm_sinkhorn_fastiter": (c_int, [c_void, c_void, c_void, c_void, c_void, c_void, c_i64, c_i64,
+                                     c_i64, c_void]),
+    "tm_sinkhorn_logiter": (c_int, [c_void, c_void, c_void, c_void, c_void, c_void, c_i64, c_i64,
+                                    c_i64, c_double, c_void]),
+}
+
+TM_F32 = 0
+TM_U8 = 1
+
+
+class TorchmorphError(RuntimeError):
+    """A libtmcore call returned a non-zero tm_status."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(message)
+        self.status = status
+
+
+def load():
+    """Load libtmcore.so (building nothing) and bind every declared symbol."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"torchmorph_gb300: CUDA library {LIB_PATH} is missing; build it with "
+                "`python -c 'import __graft_entry__ as g; g.build()'` (no CPU fallback exists)"
+            )
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name, None)
+            if fn is None:
+                continue
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def available_symbols():
+    lib = load()
+    return [name for name in SIGNATURES if hasattr(lib, name)]
+
+
+def check(status: int, what: str) -> None:
+    if status != 0:
+        lib = load()
+        msg = lib.tm_last_error().decode(errors="replace")
+        kind = lib.tm_status_string(status).decode(errors="replace")
+        raise TorchmorphError(status, f"{what}: {kind}: {msg}")
+
+
+def i64_array(values):
+    values = [int(v) for v in values]
+    return (ctypes.c_int64 * max(1, len(values)))(*values)
+
+
+def f32_array(values):
+    values = [float(v) for v in values]
+    return (ctypes.c_float * max(1, len(values)))(*values)
+
+
+def ptr(t: torch.Tensor | None):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def stream_of(device: torch.device):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)

@@ -1,0 +1,91 @@
+// Shared host/device helpers of libtmcore (GB300, sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+
+#include "../../include/torchmorph_gb300.h"
+
+#define TM_MAX_NDIM 8
+
+namespace tmc {
+
+// Per-thread last-error message (reported through tm_last_error()).
+void set_error(const char *fmt, ...);
+int fail(int status, const char *fmt, ...);
+
+// Checks a CUDA call made by the library; records the message on failure.
+int cuda_check(cudaError_t err, const char *what);
+
+// Launch check after every kernel launch.
+inline int launch_check(const char *kernel) { return cuda_check(cudaGetLastError(), kernel); }
+
+// Number of SMs of the current device (cached per device).
+int sm_count();
+
+// Host-side geometry of a batch of items.
+struct Geometry {
+    int ndim;
+    int64_t batch;
+    int64_t shape[TM_MAX_NDIM];
+    int64_t stride[TM_MAX_NDIM];
+    int64_t numel_item;
+    int64_t numel;
+};
+
+int make_geometry(int64_t batch, int ndim, const int64_t *shape, Geometry *g);
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Fast unsigned division by a runtime constant (Granlund-Montgomery magic
+// numbers; valid for 32-bit dividends).  Used in kernels to unravel flat
+// indices without hardware integer division.
+struct FastDiv {
+    uint32_t d;
+    uint32_t mul;
+    uint32_t shift;
+};
+
+inline FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f;
+    f.d = d;
+    if (d <= 1) {
+        f.mul = 0;
+        f.shift = 0;
+        return f;
+    }
+    uint32_t l = 0;
+    while ((1ull << l) < d) l++;
+    // mul = floor(2^32 * (2^l - d) / d) + 1, q = (hi(n*mul) + n) >> l
+    uint64_t m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
+    f.mul = (uint32_t)m;
+    f.shift = l;
+    return f;
+}
+
+__host__ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
+    if (f.d == 1) return n;
+#ifdef __CUDA_ARCH__
+    uint32_t hi = __umulhi(n, f.mul);
+#else
+    uint32_t hi = (uint32_t)(((uint64_t)n * f.mul) >> 32);
+#endif
+    return (hi + ((n - hi) >> 1)) >> (f.shift - 1);
+}
+
+}  // namespace tmc
+
+#define TM_CHECK_CUDA(call)                                    \
+    do {                                                       \
+        int _st = tmc::cuda_check((call), #call);               \
+        if (_st != TM_OK) return _st;                          \
+    } while (0)
+
+#define TM_LAUNCH_CHECK(name)                                  \
+    do {                                                       \
+        int _st = tmc::launch_check(name);                      \
+        if (_st != TM_OK) return _st;                          \
+    } while (0)

@@ -1,0 +1,148 @@
+"""Binary morphology front end (reference torchmorph/morphology/binary.py).
+
+Argument handling and error messages follow the reference; each erosion or
+dilation step is one libtmcore launch through ``_C``.
+"""
+
+from __future__ import annotations
+
+import torch
+from torch import Tensor
+
+from .. import _C
+from .._validation import validate_bcs_input, validate_output
+from .structure import _normalize_origin, _validate_origin, generate_binary_structure
+
+
+def _normalize_structure(structure: Tensor, spatial_ndim: int, name: str = "structure") -> Tensor:
+    if structure.ndim != spatial_ndim:
+        raise ValueError(f"{name} dimension is not {spatial_ndim}, got {structure.ndim}")
+    return (structure != 0).detach().to(device="cpu", dtype=torch.bool).contiguous()
+
+
+def _binary_morphology_cuda_step(input, structure, border_value, origin, *, mode):
+    """One erosion/dilation launch; `structure` is a CPU bool tensor."""
+    x = input if input.dtype == torch.bool and input.is_contiguous() else (input != 0).contiguous()
+    kernel = _C.binary_erosion_cuda if mode == "erosion" else _C.binary_dilation_cuda
+    return kernel(x, structure, list(origin), bool(border_value))
+
+
+def _binary_morphology(input, structure, iterations, mask, output, border_value, origin, *, mode):
+    until_stable = iterations < 1
+    nd = validate_bcs_input(input)
+    validate_output(input, output)
+    if structure is None:
+        structure = generate_binary_structure(nd, 1)
+    structure = _normalize_structure(structure, nd)
+    origin = _normalize_origin(origin, nd)
+    _validate_origin(origin, structure)
+    x = input != 0
+    original = x
+    if mask is not None and mask.shape != input.shape:
+        raise ValueError(f"mask shape {mask.shape} must match input shape {input.shape}")
+    mask_b = mask.to(device=input.device, dtype=torch.bool) if mask is not None else None
+    empty = not bool(structure.any())  # CPU tensor: no device sync
+
+    def step(v):
+        if empty:
+            return torch.full_like(v, mode == "erosion", dtype=torch.bool)
+        return _binary_morphology_cuda_step(v, structure, border_value, origin, mode=mode)
+
+    if until_stable:
+        prev = None
+        while True:
+            x = step(x)
+            if mask_b is not None:
+                x = torch.where(mask_b, x, original)
+            if prev is not None and torch.equal(x, prev):
+                break
+            prev = x
+    else:
+        for _ in range(iterations):
+            x = step(x)
+            if mask_b is not None:
+                x = torch.where(mask_b, x, original)
+    result = x.to(dtype=torch.bool)
+    if output is not None:
+        output.copy_(result)
+        return output
+    return result
+
+
+def binary_erosion(input, structure=None, iterations=1, mask=None, output=None, border_value=False,
+                   origin=0) -> Tensor:
+    """N-dimensional binary erosion of a (B, C, *spatial) CUDA tensor."""
+    return _binary_morphology(input, structure, iterations, mask, output, border_value, origin,
+                              mode="erosion")
+
+
+def binary_dilation(input, structure=None, iterations=1, mask=None, output=None, border_value=False,
+                    origin=0) -> Tensor:
+    """N-dimensional binary dilation of a (B, C, *spatial) CUDA tensor."""
+    return _binary_morphology(input, structure, iterations, mask, output, border_value, origin,
+                              mode="dilation")
+
+
+def binary_propagation(input, structure=None, mask=None, output=None, border_value=False,
+                       origin=0) -> Tensor:
+    """Dilation repeated until stable inside `mask`."""
+    return _binary_morphology(input, structure, -1, mask, output, border_value, origin,
+                              mode="dilation")
+
+
+def binary_fill_holes(input, structure=None, output=None, origin=0) -> Tensor:
+    """Fill the background regions not connected to the border."""
+    validate_bcs_input(input)
+    validate_output(input, output)
+    outside = binary_propagation(torch.zeros_like(input, dtype=torch.bool), structure=structure,
+                                 mask=input == 0, output=None, border_value=True, origin=origin)
+    result = torch.logical_not(outside)
+    if output is not None:
+        output.copy_(result)
+        return output
+    return result
+
+
+def binary_hit_or_miss(input, structure1=None, structure2=None, output=None, origin1=0,
+                       origin2=None) -> Tensor:
+    """Voxels where structure1 fits the foreground and structure2 fits the background."""
+    nd = validate_bcs_input(input)
+    validate_output(input, output)
+    origin1 = _normalize_origin(origin1, nd)
+    origin2 = origin1 if origin2 is None else _normalize_origin(origin2, nd)
+    if structure1 is None:
+        structure1 = generate_binary_structure(nd, 1)
+    structure1 = _normalize_structure(structure1, nd, "structure1")
+    _validate_origin(origin1, structure1, "origin1")
+    if structure2 is None:
+        structure2 = torch.logical_not(structure1).contiguous()
+    else:
+        structure2 = _normalize_structure(structure2, nd, "structure2")
+    _validate_origin(origin2, structure2, "origin2")
+    fg = input != 0
+    if bool(structure1.any()):
+        hit = binary_erosion(fg, structure=structure1, origin=origin1)
+    else:
+        hit = torch.ones_like(fg, dtype=torch.bool)
+    if bool(structure2.any()):
+        result = torch.logical_and(hit, binary_erosion(fg == 0, structure=structure2, origin=origin2))
+    else:
+        result = hit
+    if output is not None:
+        output.copy_(result)
+        return output
+    return result
+
+
+def binary_opening(input, structure=None, iterations=1, mask=None, output=None, border_value=False,
+                   origin=0) -> Tensor:
+    """Erosion followed by dilation."""
+    x = binary_erosion(input, structure, iterations, mask, None, border_value, origin)
+    return binary_dilation(x, structure, iterations, mask, output, border_value, origin)
+
+
+def binary_closing(input, structure=None, iterations=1, mask=None, output=None, border_value=False,
+                   origin=0) -> Tensor:
+    """Dilation followed by erosion."""
+    x = binary_dilation(input, structure, iterations, mask, None, border_value, origin)
+    return binary_erosion(x, structure, iterations, mask, output, border_value, origin)

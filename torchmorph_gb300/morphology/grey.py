@@ -1,0 +1,168 @@
+"""Grey morphology front end (reference torchmorph/morphology/grey.py).
+
+Argument resolution, validation and error messages follow the reference
+operator for operator; the arithmetic runs in libtmcore through ``_C``.
+"""
+
+from __future__ import annotations
+
+import torch
+from torch import Tensor
+
+from .. import _C
+from .._validation import validate_bcs_input, validate_output
+from .structure import _normalize_origin, _validate_origin
+
+_MODE_MAP = {
+    "constant": 0,
+    "reflect": 1,
+    "nearest": 2,
+    "mirror": 3,
+    "wrap": 4,
+}
+
+
+def _element_kwargs(size, footprint, structure, mode, cval, origin) -> dict:
+    return dict(size=size, footprint=footprint, structure=structure, mode=mode, cval=cval,
+                origin=origin)
+
+
+def _resolve_element(spatial_ndim, size, footprint, structure):
+    """(structure float32 CPU, footprint bool CPU or empty) with priority structure > footprint > size."""
+    fp_cpu = torch.empty(0, dtype=torch.bool)
+    if structure is not None:
+        struct = structure.to(torch.float32)
+        if footprint is not None:
+            mask = footprint.to(torch.bool)
+            if tuple(mask.shape) != tuple(struct.shape):
+                raise ValueError(
+                    f"Footprint shape {tuple(mask.shape)} must match structure "
+                    f"shape {tuple(struct.shape)}."
+                )
+            if not mask.any():
+                raise ValueError("All-zero footprint is not supported.")
+            fp_cpu = mask.detach().to(device="cpu", dtype=torch.bool).contiguous()
+    elif footprint is not None:
+        mask = footprint.to(torch.bool)
+        if not mask.any():
+            raise ValueError("All-zero footprint is not supported.")
+        struct = torch.zeros(tuple(mask.shape), dtype=torch.float32)
+        fp_cpu = mask.detach().to(device="cpu", dtype=torch.bool).contiguous()
+    elif size is not None:
+        if isinstance(size, int):
+            size = (size,) * spatial_ndim
+        if any(v <= 0 for v in size):
+            raise ValueError("size values must be greater than zero")
+        struct = torch.zeros(tuple(size), dtype=torch.float32)
+    else:
+        raise ValueError("At least one of size, footprint, or structure must be specified.")
+    if struct.ndim != spatial_ndim:
+        raise ValueError(
+            f"Structure dimension {struct.ndim} must match spatial dimension {spatial_ndim}."
+        )
+    return struct.detach().to(device="cpu", dtype=torch.float32).contiguous(), fp_cpu
+
+
+def _prepare(input, size, footprint, structure, mode, origin):
+    nd = validate_bcs_input(input)
+    struct, fp = _resolve_element(nd, size, footprint, structure)
+    o = _normalize_origin(origin, nd)
+    _validate_origin(o, struct)
+    if mode not in _MODE_MAP:
+        raise ValueError(f"Unknown mode '{mode}'. Must be one of {list(_MODE_MAP.keys())}.")
+    return struct, fp, list(o), _MODE_MAP[mode]
+
+
+def _grey_morphology(
+    input: Tensor,
+    size=None,
+    footprint=None,
+    structure=None,
+    output=None,
+    mode: str = "reflect",
+    cval: float = 0.0,
+    origin=0,
+    *,
+    operation: str,
+) -> Tensor:
+    validate_bcs_input(input)
+    validate_output(input, output)
+    struct, fp, o, m = _prepare(input, size, footprint, structure, mode, origin)
+    kernel = _C.grey_erosion_cuda if operation == "erosion" else _C.grey_dilation_cuda
+    result = kernel(input.detach().contiguous().float(), struct, fp, o, m, cval)
+    if output is not None:
+        output.copy_(result)
+        return output
+    return result
+
+
+def grey_erosion(input, size=None, footprint=None, structure=None, output=None, mode="reflect",
+                 cval=0.0, origin=0) -> Tensor:
+    """N-dimensional grey erosion of a (B, C, *spatial) CUDA tensor, computed in float32."""
+    return _grey_morphology(input, size, footprint, structure, output, mode, cval, origin,
+                            operation="erosion")
+
+
+def grey_dilation(input, size=None, footprint=None, structure=None, output=None, mode="reflect",
+                  cval=0.0, origin=0) -> Tensor:
+    """N-dimensional grey dilation of a (B, C, *spatial) CUDA tensor, computed in float32."""
+    return _grey_morphology(input, size, footprint, structure, output, mode, cval, origin,
+                            operation="dilation")
+
+
+def grey_opening(input, size=None, footprint=None, structure=None, output=None, mode="reflect",
+                 cval=0.0, origin=0) -> Tensor:
+    """Grey opening: dilation of the erosion."""
+    kw = _element_kwargs(size, footprint, structure, mode, cval, origin)
+    return grey_dilation(grey_erosion(input, **kw), output=output, **kw)
+
+
+def grey_closing(input, size=None, footprint=None, structure=None, output=None, mode="reflect",
+                 cval=0.0, origin=0) -> Tensor:
+    """Grey closing: erosion of the dilation."""
+    kw = _element_kwargs(size, footprint, structure, mode, cval, origin)
+    return grey_erosion(grey_dilation(input, **kw), output=output, **kw)
+
+
+def _finish(result, output):
+    if output is not None:
+        output.copy_(result)
+        return output
+    return result
+
+
+def morphological_gradient(input, size=None, footprint=None, structure=None, output=None,
+                           mode="reflect", cval=0.0, origin=0) -> Tensor:
+    """Dilation minus erosion."""
+    validate_bcs_input(input)
+    validate_output(input, output)
+    kw = _element_kwargs(size, footprint, structure, mode, cval, origin)
+    return _finish(grey_dilation(input, **kw) - grey_erosion(input, **kw), output)
+
+
+def white_tophat(input, size=None, footprint=None, structure=None, output=None, mode="reflect",
+                 cval=0.0, origin=0) -> Tensor:
+    """Input minus its grey opening."""
+    validate_bcs_input(input)
+    validate_output(input, output)
+    opened = grey_opening(input, **_element_kwargs(size, footprint, structure, mode, cval, origin))
+    return _finish(input.detach().float() - opened, output)
+
+
+def black_tophat(input, size=None, footprint=None, structure=None, output=None, mode="reflect",
+                 cval=0.0, origin=0) -> Tensor:
+    """Grey closing minus the input."""
+    validate_bcs_input(input)
+    validate_output(input, output)
+    closed = grey_closing(input, **_element_kwargs(size, footprint, structure, mode, cval, origin))
+    return _finish(closed - input.detach().float(), output)
+
+
+def morphological_laplace(input, size=None, footprint=None, structure=None, output=None,
+                          mode="reflect", cval=0.0, origin=0) -> Tensor:
+    """Dilation plus erosion minus twice the input."""
+    validate_bcs_input(input)
+    validate_output(input, output)
+    kw = _element_kwargs(size, footprint, structure, mode, cval, origin)
+    res = grey_dilation(input, **kw) + grey_erosion(input, **kw) - 2 * input.detach().float()
+    return _finish(res, output)

@@ -1,0 +1,197 @@
+"""Entropic optimal transport (reference torchmorph/optimal_transport.py).
+
+``SinkhornSolver`` keeps the reference's constructor, forward/plan/potentials
+API, preprocessing and autograd contract.  CUDA float32 inputs run the fused
+libtmcore iterations (``_C.sinkhorn_logiter`` / ``_C.sinkhorn_fastiter``);
+other dtypes/devices run the same iterations in plain torch, exactly as the
+reference does.
+"""
+
+from __future__ import annotations
+
+from typing import Optional
+
+import torch
+from torch import Tensor, nn
+
+
+def build_cost_matrix(shape, p=2, device=None) -> Tensor:
+    """(d, d) pairwise L^p distances between the d points of a grid of `shape`."""
+    grids = torch.meshgrid([torch.arange(s, device=device) for s in shape], indexing="ij")
+    pts = torch.stack(grids, dim=-1).reshape(-1, len(shape)).float()
+    return torch.cdist(pts, pts, p=p)
+
+
+def _use_fused_kernels(t: Tensor) -> bool:
+    return t.is_cuda and t.dtype == torch.float32
+
+
+def _transpose_or_self(matrix: Tensor) -> Tensor:
+    return matrix if torch.equal(matrix, matrix.mT) else matrix.mT.contiguous()
+
+
+_GRAPH_MIN_ITER = 100
+_GRAPH_CHUNK = 25
+
+
+def _run_fused(launch, max_iter, device):
+    """Enqueue `max_iter` in-place iterations via launch(k); long runs replay a captured chunk."""
+    if max_iter < _GRAPH_MIN_ITER or torch.cuda.is_current_stream_capturing():
+        launch(max_iter)
+        return
+    try:
+        with torch.cuda.device(device):
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                launch(_GRAPH_CHUNK)
+            torch.cuda.current_stream().wait_stream(side)
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph):
+                launch(_GRAPH_CHUNK)
+            for _ in range(max_iter // _GRAPH_CHUNK - 1):
+                graph.replay()
+            rest = max_iter % _GRAPH_CHUNK
+            if rest:
+                launch(rest)
+    except RuntimeError:
+        launch(max_iter)  # fixed-point steps: extra iterations are harmless
+
+
+def _scaling_iterations(a, b, cost_matrix, epsilon, max_iter, threshold):
+    K = torch.exp(-cost_matrix / epsilon)
+    if _use_fused_kernels(a):
+        from . import _C
+
+        a, b = a.contiguous(), b.contiguous()
+        K_T = _transpose_or_self(K)
+        u = torch.ones_like(a)
+        v = torch.ones_like(b)
+        _run_fused(lambda k: _C.sinkhorn_fastiter(a, b, K, K_T, u, v, k), max_iter, a.device)
+        return u.log(), v.log()
+    u = torch.ones_like(a)
+    v = torch.ones_like(b)
+    for i in range(max_iter):
+        u_prev = u
+        u = a / (v @ K.mT + 1e-12)
+        v = b / (u @ K + 1e-12)
+        if threshold > 0 and i % 10 == 0:
+            if (u - u_prev).abs().sum(dim=-1).max() <= threshold:
+                break
+    return u.log(), v.log()
+
+
+def _log_iterations(a, b, cost_matrix, epsilon, max_iter, threshold):
+    log_a, log_b = a.log(), b.log()
+    if _use_fused_kernels(a):
+        from . import _C
+
+        log_a, log_b = log_a.contiguous(), log_b.contiguous()
+        cost_T = _transpose_or_self(cost_matrix)
+        log_u = torch.zeros_like(a)
+        log_v = torch.zeros_like(b)
+        _run_fused(lambda k: _C.sinkhorn_logiter(log_a, log_b, cost_matrix, cost_T, log_u, log_v,
+                                                 k, epsilon), max_iter, a.device)
+        return log_u, log_v
+    log_K = -cost_matrix / epsilon
+    log_u = torch.zeros_like(a)
+    log_v = torch.zeros_like(b)
+    for i in range(max_iter):
+        prev = log_u
+        log_u = log_a - torch.logsumexp(log_K + log_v.unsqueeze(-2), dim=-1)
+        log_v = log_b - torch.logsumexp(log_K.mT + log_u.unsqueeze(-2), dim=-1)
+        if threshold > 0 and i % 10 == 0:
+            if (log_u - prev).abs().sum(dim=-1).max() <= threshold:
+                break
+    return log_u, log_v
+
+
+class _SinkhornDistance(torch.autograd.Function):
+    """<P, C> with envelope-theorem gradients (centred dual potentials) for a and b."""
+
+    @staticmethod
+    def forward(ctx, a, b, cost_matrix, epsilon, max_iter, threshold, log_space):
+        iterate = _log_iterations if log_space else _scaling_iterations
+        log_u, log_v = iterate(a, b, cost_matrix, epsilon, max_iter, threshold)
+        plan = torch.exp(log_u.unsqueeze(-1) - cost_matrix / epsilon + log_v.unsqueeze(-2))
+        distance = (plan * cost_matrix).sum(dim=(-2, -1))
+        f = epsilon * log_u
+        g = epsilon * log_v
+        ctx.save_for_backward(f - f.mean(dim=-1, keepdim=True), g - g.mean(dim=-1, keepdim=True))
+        return distance
+
+    @staticmethod
+    def backward(ctx, grad_output):
+        f, g = ctx.saved_tensors
+        grad = grad_output.unsqueeze(-1)
+        return grad * f, grad * g, None, None, None, None, None
+
+
+class SinkhornSolver(nn.Module):
+    """Entropy-regularised balanced OT between (n, d) histogram batches sharing a (d, d) cost."""
+
+    def __init__(self, epsilon=1.0, max_iter=100, threshold=0.0, p=2, log_space=False):
+        super().__init__()
+        if epsilon <= 0:
+            raise ValueError("epsilon must be positive.")
+        if max_iter <= 0:
+            raise ValueError("max_iter must be positive.")
+        if threshold < 0:
+            raise ValueError("threshold must be non-negative.")
+        self.epsilon = epsilon
+        self.max_iter = max_iter
+        self.threshold = threshold
+        self.p = p
+        self.log_space = log_space
+
+    def extra_repr(self):
+        return (
+            f"epsilon={self.epsilon}, max_iter={self.max_iter}, "
+            f"threshold={self.threshold}, log_space={self.log_space}"
+        )
+
+    def data_preprocess(self, source, target, cost_matrix: Optional[Tensor] = None):
+        """Validate (n, d) inputs, clamp negatives and normalise each row to unit mass."""
+        if source.ndim != 2 or source.shape != target.shape:
+            raise ValueError("source and target must be (n, d) tensors of the same shape.")
+        if not source.is_floating_point():
+            raise ValueError("source and target must be floating-point tensors.")
+        d = source.shape[1]
+        if cost_matrix is None:
+            cost_matrix = build_cost_matrix((d,), self.p, source.device)
+        elif cost_matrix.shape != (d, d):
+            raise ValueError(
+                f"cost_matrix must have shape ({d}, {d}), got {tuple(cost_matrix.shape)}."
+            )
+        cost_matrix = cost_matrix.to(device=source.device, dtype=source.dtype).contiguous()
+        source = source.clamp(min=0)
+        target = target.clamp(min=0)
+        source = source / source.sum(dim=-1, keepdim=True).clamp(min=1e-12)
+        target = target / target.sum(dim=-1, keepdim=True).clamp(min=1e-12)
+        return source, target, cost_matrix
+
+    def forward(self, source: Tensor, target: Tensor, cost_matrix: Optional[Tensor] = None):
+        """(n,) transport distances <P, C> between the rows of source and target."""
+        source, target, cost_matrix = self.data_preprocess(source, target, cost_matrix)
+        return _SinkhornDistance.apply(source, target, cost_matrix, self.epsilon, self.max_iter,
+                                       self.threshold, self.log_space)
+
+    @torch.no_grad()
+    def plan(self, source: Tensor, target: Tensor, cost_matrix: Optional[Tensor] = None):
+        """(n, d, d) transport plans."""
+        source, target, cost_matrix = self.data_preprocess(source, target, cost_matrix)
+        log_u, log_v = self._iterate(source, target, cost_matrix)
+        return torch.exp(log_u.unsqueeze(-1) - cost_matrix / self.epsilon + log_v.unsqueeze(-2))
+
+    @torch.no_grad()
+    def potentials(self, source: Tensor, target: Tensor, cost_matrix: Optional[Tensor] = None):
+        """Centred dual potentials (f, g), each (n, d)."""
+        source, target, cost_matrix = self.data_preprocess(source, target, cost_matrix)
+        log_u, log_v = self._iterate(source, target, cost_matrix)
+        f = self.epsilon * log_u
+        g = self.epsilon * log_v
+        return f - f.mean(dim=-1, keepdim=True), g - g.mean(dim=-1, keepdim=True)
+
+    def _iterate(self, a, b, cost_matrix):
+        iterate = _log_iterations if self.log_space else _scaling_iterations
+        return iterate(a, b, cost_matrix, self.epsilon, self.max_iter, self.threshold)
