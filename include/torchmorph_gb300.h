@@ -112,7 +112,7 @@ int tm_binary_dilation(const uint8_t *in, uint8_t *out, int64_t batch, int ndim,
  * Feature indices follow scipy.ndimage: nearest background voxel, ties to
  * the smallest last-axis coordinate, then the previous axis, and so on.
  */
-size_t tm_edt_workspace_size(int64_t batch, int ndim, const int64_t *shape);
+size_t tm_edt_workspace_size(int64_t batch, int ndim, const int64_t *shape, const float *sampling);
 int tm_edt(const void *input, int in_dtype, int64_t batch, int ndim, const int64_t *shape,
            const float *sampling, float *dist, int32_t *indices, int32_t *sqdist,
            void *workspace, size_t workspace_bytes, tm_stream_t stream);

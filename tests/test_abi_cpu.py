@@ -85,9 +85,11 @@ def test_rejects_bad_geometry_without_touching_the_device():
 
 def test_workspace_sizes():
     lib = _lib.load()
-    assert lib.tm_edt_workspace_size(1, 1, _lib.i64_array([10])) == 0
-    n2 = lib.tm_edt_workspace_size(4, 3, _lib.i64_array([8, 8, 8]))
-    assert n2 >= 2 * 2 * 4 * 512 * 4
+    assert lib.tm_edt_workspace_size(1, 1, _lib.i64_array([10]), None) == 0
+    n2 = lib.tm_edt_workspace_size(4, 3, _lib.i64_array([8, 8, 8]), None)
+    assert n2 >= 4 * 512 * (2 + 4)
+    n3 = lib.tm_edt_workspace_size(4, 3, _lib.i64_array([8, 8, 8]), _lib.f32_array([1.0, 1.0, 2.5]))
+    assert n3 >= 2 * 2 * 4 * 512 * 4
     assert lib.tm_bfdt_workspace_size(2, 2, _lib.i64_array([5, 5])) >= 2 * 25 * 4
 
 

@@ -153,9 +153,9 @@ def edt(input, sampling=None, return_distances=True, return_indices=False, sqdis
     lib = _lib.load()
     with torch.cuda.device(dev):
         shp = _lib.i64_array(shape)
-        ws = _workspace(lib.tm_edt_workspace_size(batch, nd, shp), dev)
-        st = lib.tm_edt(_lib.ptr(input), _TORCH_TO_TM[input.dtype], batch, nd, shp,
-                        None if sampling is None else _lib.f32_array(sampling), _lib.ptr(dist),
+        samp = None if sampling is None else _lib.f32_array(sampling)
+        ws = _workspace(lib.tm_edt_workspace_size(batch, nd, shp, samp), dev)
+        st = lib.tm_edt(_lib.ptr(input), _TORCH_TO_TM[input.dtype], batch, nd, shp, samp, _lib.ptr(dist),
                         _lib.ptr(ind), _lib.ptr(sq), _lib.ptr(ws),
                         0 if ws is None else ws.numel(), _lib.stream_of(dev))
     _lib.check(st, "tm_edt")

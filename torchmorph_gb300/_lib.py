@@ -41,7 +41,7 @@ SIGNATURES = {
                                   c_void]),
     "tm_binary_dilation": (c_int, [c_void, c_void, c_i64, c_int, I64P, U8P, I64P, I64P, c_int,
                                    c_void]),
-    "tm_edt_workspace_size": (c_size, [c_i64, c_int, I64P]),
+    "tm_edt_workspace_size": (c_size, [c_i64, c_int, I64P, F32P]),
     "tm_edt": (c_int, [c_void, c_int, c_i64, c_int, I64P, F32P, c_void, c_void, c_void, c_void,
                        c_size, c_void]),
     "tm_cdt_workspace_size": (c_size, [c_i64, c_int, I64P]),

@@ -38,7 +38,7 @@
 #include <cstring>
 #include <type_traits>
 
-#include "tm_common.cuh"
+#include "edt_internal.cuh"
 
 namespace tmc {
 namespace {
@@ -493,9 +493,17 @@ int check_edt_args(const void *input, int in_dtype, const Geometry &g, const flo
 }  // namespace
 }  // namespace tmc
 
-extern "C" size_t tm_edt_workspace_size(int64_t batch, int ndim, const int64_t *shape) {
+static bool unit_sampling(int ndim, const float *sampling) {
+    if (!sampling) return true;
+    for (int d = 0; d < ndim; d++)
+        if (sampling[d] != 1.0f) return false;
+    return true;
+}
+
+extern "C" size_t tm_edt_workspace_size(int64_t batch, int ndim, const int64_t *shape, const float *sampling) {
     tmc::Geometry g;
     if (tmc::make_geometry(batch, ndim, shape, &g) != TM_OK) return 0;
+    if (tmc::edt_compact_eligible(g, unit_sampling(ndim, sampling))) return tmc::edt_compact_workspace(g);
     return tmc::plan_edt(g).total;
 }
 
@@ -511,12 +519,18 @@ extern "C" int tm_edt(const void *input, int in_dtype, int64_t batch, int ndim, 
     if (st != TM_OK) return st;
     if (!dist && !indices && !sqdist) return fail(TM_ERR_INVALID_ARGUMENT, "at least one output must be requested");
     if (sqdist && !unit) return fail(TM_ERR_INVALID_ARGUMENT, "squared integer distances need unit sampling");
+    unsigned char *ws = static_cast<unsigned char *>(workspace);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (edt_compact_eligible(g, unit)) {
+        const size_t need = edt_compact_workspace(g);
+        if (!workspace || workspace_bytes < need)
+            return fail(TM_ERR_WORKSPACE, "workspace of %zu bytes required, got %zu", need, workspace_bytes);
+        return edt_compact_run(input, in_dtype, g, dist, indices, sqdist, ws, s);
+    }
     EdtPlan pl = plan_edt(g);
     if (pl.total > 0 && (!workspace || workspace_bytes < pl.total))
         return fail(TM_ERR_WORKSPACE, "workspace of %zu bytes required, got %zu", pl.total, workspace_bytes);
     EdtOutputs o{dist, indices, sqdist};
-    unsigned char *ws = static_cast<unsigned char *>(workspace);
-    cudaStream_t s = (cudaStream_t)stream;
     if (unit) {
         if (in_dtype == TM_F32) return launch_edt<float, int32_t>((const float *)input, g, nullptr, o, ws, pl, s);
         return launch_edt<uint8_t, int32_t>((const uint8_t *)input, g, nullptr, o, ws, pl, s);
