@@ -194,3 +194,17 @@ def test_noncontiguous_input(cuda):
     ed, ei = per_item_indices(inp.cpu().numpy(), ndi.distance_transform_edt)
     np.testing.assert_array_equal(d.cpu().numpy(), ed.astype(np.float32))
     np.testing.assert_array_equal(i.cpu().numpy(), ei)
+
+
+def test_edt_vector_path_and_offset_outputs(cuda):
+    x = rng(11).random((2, 1, 64, 256)) < 0.95
+    sq, od, oi = oracle.edt(x)
+    d, i = tm.euclidean_distance_transform(_t(x), return_indices=True)
+    np.testing.assert_array_equal(d.cpu().numpy(), od.astype(np.float32))
+    np.testing.assert_array_equal(i.cpu().numpy(), oi)
+    # outputs that start 4 bytes into their storage take the scalar store path
+    dbuf = torch.empty(x.size + 1, dtype=torch.float32, device="cuda")[1:].view(x.shape)
+    ibuf = torch.empty(2 * x.size + 1, dtype=torch.int32, device="cuda")[1:].view((2, *x.shape))
+    tm.euclidean_distance_transform(_t(x), distances=dbuf, indices=ibuf)
+    np.testing.assert_array_equal(dbuf.cpu().numpy(), od.astype(np.float32))
+    np.testing.assert_array_equal(ibuf.cpu().numpy(), oi)
