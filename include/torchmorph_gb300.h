@@ -117,6 +117,22 @@ int tm_edt(const void *input, int in_dtype, int64_t batch, int ndim, const int64
            const float *sampling, float *dist, int32_t *indices, int32_t *sqdist,
            void *workspace, size_t workspace_bytes, tm_stream_t stream);
 
+/* Allocation-free EDT.  No counterpart in the reference: this entry point
+ * exists for callers that cannot hand the library a device workspace (for
+ * example code paths where allocating device memory is not allowed, or C
+ * callers without an allocator of their own).  It runs the same kernels as
+ * tm_edt for 2-D and 3-D items with unit spacing, on a fixed 32 MiB scratch
+ * area that the library keeps on every GPU that loads it until the process
+ * exits; larger batches (above ~4M voxels of 3-D items or ~16M of 2-D items)
+ * are rejected with TM_ERR_TOO_LARGE, other shapes with TM_ERR_UNSUPPORTED.
+ * The first call on a device looks up the scratch area's device address;
+ * make that first call outside any CUDA stream capture.  All calls on a
+ * device share the scratch: calls whose GPU work may overlap must be
+ * serialised by the caller.  Outputs as for tm_edt.
+ */
+int tm_edt_noalloc(const void *input, int in_dtype, int64_t batch, int ndim, const int64_t *shape,
+                   float *dist, int32_t *indices, int32_t *sqdist, tm_stream_t stream);
+
 /* ------------------------------------------------------------------- cdt --
  * Replaces cdt_cuda (torchmorph/csrc/torchmorph.cpp:42-47,
  * torchmorph/csrc/cdt_kernel.cu:269-463).

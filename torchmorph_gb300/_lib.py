@@ -44,6 +44,7 @@ SIGNATURES = {
     "tm_edt_workspace_size": (c_size, [c_i64, c_int, I64P, F32P]),
     "tm_edt": (c_int, [c_void, c_int, c_i64, c_int, I64P, F32P, c_void, c_void, c_void, c_void,
                        c_size, c_void]),
+    "tm_edt_noalloc": (c_int, [c_void, c_int, c_i64, c_int, I64P, c_void, c_void, c_void, c_void]),
     "tm_cdt_workspace_size": (c_size, [c_i64, c_int, I64P]),
     "tm_cdt": (c_int, [c_void, c_int, c_i64, c_int, I64P, c_int, c_void, c_void, c_void, c_size,
                        c_void]),
