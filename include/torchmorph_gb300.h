@@ -73,6 +73,13 @@ const char *tm_status_string(int status);
 const char *tm_last_error(void);
 int tm_version(void);
 
+/* Device-side status of the current device: 0 when no kernel has recorded a
+ * failure, 1 when a bounded wait inside a kernel gave up (the kernel then
+ * stopped early and its outputs are incomplete).  Synchronous; `reset`
+ * clears the word.  No counterpart in the reference (its kernels have no
+ * waits). */
+int tm_device_error(int reset);
+
 /* ------------------------------------------------------------------ grey --
  * Replaces grey_erosion_cuda / grey_dilation_cuda
  * (torchmorph/csrc/torchmorph.cpp:3-19, torchmorph/csrc/grey_kernel.cu:332-356).

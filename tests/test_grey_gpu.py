@@ -176,3 +176,37 @@ def test_deterministic(cuda):
     a = tm.grey_erosion(x, footprint=_t(CROSS, torch.bool))
     b = tm.grey_erosion(x, footprint=_t(CROSS, torch.bool))
     assert torch.equal(a, b)
+
+
+def _device_error():
+    from torchmorph_gb300 import _lib
+
+    return _lib.load().tm_device_error(1)
+
+
+@pytest.mark.parametrize("dilation", [False, True])
+@pytest.mark.parametrize("mode", ["reflect", "constant", "wrap"])
+@pytest.mark.parametrize("size", [(3, 3), (1, 5), (15, 15), (4, 9), (31, 2)])
+def test_flat_2d_tma_tiles_vs_oracle(cuda, dilation, mode, size):
+    """Images with 16-byte rows take the TMA path for every interior tile."""
+    r = rng(hash((dilation, mode, size, 1)) % 2**32)
+    x = r.random((3, 1, 150, 512)).astype(np.float32)
+    origin = (r.integers(-(size[0] // 2), (size[0] - 1) // 2 + 1),
+              r.integers(-(size[1] // 2), (size[1] - 1) // 2 + 1))
+    op = tm.grey_dilation if dilation else tm.grey_erosion
+    got = op(_t(x), size=size, mode=mode, cval=0.75, origin=origin)
+    exp = oracle.grey(x, np.zeros(size, np.float32), origin=origin, mode=mode, cval=0.75,
+                      dilation=dilation)
+    np.testing.assert_array_equal(got.cpu().numpy(), exp)
+    assert _device_error() == 0
+
+
+@pytest.mark.parametrize("dilation", [False, True])
+def test_binary_box_tma_tiles_vs_oracle(cuda, dilation):
+    x = rng(9).random((2, 2, 97, 384)) > 0.4
+    st = np.ones((5, 3), bool)
+    op = tm.binary_dilation if dilation else tm.binary_erosion
+    got = op(_t(x), structure=_t(st))
+    exp = oracle.binary(x, st, dilation=dilation)
+    np.testing.assert_array_equal(got.cpu().numpy(), exp)
+    assert _device_error() == 0

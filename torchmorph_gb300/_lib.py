@@ -33,6 +33,7 @@ SIGNATURES = {
     "tm_status_string": (ctypes.c_char_p, [c_int]),
     "tm_last_error": (ctypes.c_char_p, []),
     "tm_version": (c_int, []),
+    "tm_device_error": (c_int, [c_int]),
     "tm_grey_erosion": (c_int, [c_void, c_void, c_i64, c_int, I64P, F32P, U8P, I64P, I64P, c_int,
                                 c_float, c_void]),
     "tm_grey_dilation": (c_int, [c_void, c_void, c_i64, c_int, I64P, F32P, U8P, I64P, I64P, c_int,

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "tm_common.cuh"
+#include "tm_tma.cuh"
 
 namespace tmc {
 namespace {
@@ -101,6 +102,7 @@ struct Flat2DParams {
     float sval;  // constant structure value (flat footprint)
 };
 
+
 // One run of kRun consecutive outputs of a 1-D sliding window of width k
 // over src[0 .. kRun + k - 2] (src elements `step` apart in shared memory).
 template <typename T, bool MAX>
@@ -133,7 +135,105 @@ __device__ __forceinline__ void window_run(const T *src, int step, int k, T *res
     }
 }
 
+// Row pass then column pass of one staged tile: `tile` points at the first
+// input column the tile needs (row stride ld), `rows` receives the row-pass
+// result (RH x kTileW); outputs go to dst at (y0.., x0..).
 template <typename T, bool MAX>
+__device__ __forceinline__ void flat_tile_compute(const T *tile, int ld, T *rows, const Flat2DParams &p, T *dst,
+                                                  int x0, int y0) {
+    using Op = MorphOp<T, MAX>;
+    const int RH = kTileH + p.kh - 1;
+    if (p.kw <= kRun) {
+        // narrow windows: one output per thread, adjacent lanes on adjacent
+        // columns, so every shared-memory access of a warp is conflict free
+        for (int w = threadIdx.x; w < RH * kTileW; w += kFlatThreads) {
+            const int r = w / kTileW, c = w % kTileW;
+            const T *src = tile + r * ld + c;
+            T acc = src[0];
+            for (int t = 1; t < p.kw; t++) acc = Op::combine(acc, src[t]);
+            rows[r * kTileW + c] = acc;
+        }
+    } else {
+        const int runs_per_row = kTileW / kRun;
+        for (int w = threadIdx.x; w < RH * runs_per_row; w += kFlatThreads) {
+            int r = w / runs_per_row, c = (w % runs_per_row) * kRun;
+            T res[kRun];
+            window_run<T, MAX>(tile + r * ld + c, 1, p.kw, res);
+#pragma unroll
+            for (int j = 0; j < kRun; j++) rows[r * kTileW + c + j] = res[j];
+        }
+    }
+    __syncthreads();
+    const int runs_per_col = kTileH / kRun;
+    for (int w = threadIdx.x; w < kTileW * runs_per_col; w += kFlatThreads) {
+        int c = w % kTileW, r = (w / kTileW) * kRun;
+        int gx = x0 + c;
+        // kTileH is a multiple of kRun, so the run reads rows
+        // r .. r + kRun + kh - 2 <= RH - 1: always inside the row buffer
+        T res[kRun];
+        window_run<T, MAX>(rows + r * kTileW + c, kTileW, p.kh, res);
+        if (gx < p.W) {
+#pragma unroll
+            for (int j = 0; j < kRun; j++) {
+                int gy = y0 + r + j;
+                if (gy < p.H) dst[(int64_t)gy * p.W + gx] = MorphOp<T, MAX>::apply(res[j], p.sval);
+            }
+        }
+    }
+}
+
+// Compile-time window (KH x KW): each thread walks down one column of the
+// tile (two threads per column, 16 output rows each), computes every input
+// row's horizontal minimum/maximum once and keeps the last KH of them in
+// registers, so one pass produces the outputs without a row buffer.
+// Adjacent lanes own adjacent columns: conflict-free shared-memory reads and
+// 128-byte global stores.
+template <typename T, bool MAX, int KH, int KW>
+__device__ __forceinline__ void flat_tile_walk(const T *tile, int ld, const Flat2DParams &p, T *dst, int x0,
+                                               int y0) {
+    using Op = MorphOp<T, MAX>;
+    constexpr int kSegRows = kTileH / 2;
+    const int c = threadIdx.x % kTileW, seg = threadIdx.x / kTileW;
+    const int gx = x0 + c;
+    if (gx >= p.W) return;
+    const int r0 = seg * kSegRows;
+    const T *src = tile + r0 * ld + c;
+    T h[KH];
+#pragma unroll
+    for (int k = 0; k < KH - 1; k++) {
+        T acc = src[k * ld];
+#pragma unroll
+        for (int t = 1; t < KW; t++) acc = Op::combine(acc, src[k * ld + t]);
+        h[k] = acc;
+    }
+    T *o = dst + (int64_t)(y0 + r0) * p.W + gx;
+    const int rows_left = p.H - (y0 + r0);
+#pragma unroll 4
+    for (int r = 0; r < kSegRows; r++) {
+        const T *row = src + (r + KH - 1) * ld;
+        T acc = row[0];
+#pragma unroll
+        for (int t = 1; t < KW; t++) acc = Op::combine(acc, row[t]);
+        h[KH - 1] = acc;
+        T v = h[0];
+#pragma unroll
+        for (int k = 1; k < KH; k++) v = Op::combine(v, h[k]);
+        if (r < rows_left) o[(int64_t)r * p.W] = Op::apply(v, p.sval);
+#pragma unroll
+        for (int k = 0; k < KH - 1; k++) h[k] = h[k + 1];
+    }
+}
+
+template <typename T, bool MAX, int KH, int KW>
+__device__ __forceinline__ void tile_compute(const T *tile, int ld, T *rows, const Flat2DParams &p, T *dst, int x0,
+                                             int y0) {
+    if constexpr (KH > 0)
+        flat_tile_walk<T, MAX, KH, KW>(tile, ld, p, dst, x0, y0);
+    else
+        flat_tile_compute<T, MAX>(tile, ld, rows, p, dst, x0, y0);
+}
+
+template <typename T, bool MAX, int KH, int KW>
 __global__ void __launch_bounds__(kFlatThreads) flat2d_kernel(const T *__restrict__ in, T *__restrict__ out,
                                                               Flat2DParams p) {
     using Op = MorphOp<T, MAX>;
@@ -143,12 +243,12 @@ __global__ void __launch_bounds__(kFlatThreads) flat2d_kernel(const T *__restric
     const int RWp = RW + (kRun - 1);       // padded so full runs never read past a row
     T *tile = reinterpret_cast<T *>(smem_raw);
     T *rows = tile + RH * RWp;             // row-pass result, RH x kTileW (+ pad)
-    const int x0 = blockIdx.x * kTileW;
-    const int y0 = blockIdx.y * kTileH;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = kFlatThreads / 32;
     const T cval = (T)p.cval;
 
+    const int x0 = blockIdx.x * kTileW;
+    const int y0 = blockIdx.y * kTileH;
     for (int64_t item = blockIdx.z; item < p.batch; item += gridDim.z) {
         const T *src = in + item * (int64_t)p.H * p.W;
         T *dst = out + item * (int64_t)p.H * p.W;
@@ -171,33 +271,155 @@ __global__ void __launch_bounds__(kFlatThreads) flat2d_kernel(const T *__restric
             }
         }
         __syncthreads();
-        // 2. row pass: RH rows x kTileW outputs, runs of kRun
-        const int runs_per_row = kTileW / kRun;
-        for (int w = threadIdx.x; w < RH * runs_per_row; w += kFlatThreads) {
-            int r = w / runs_per_row, c = (w % runs_per_row) * kRun;
-            T res[kRun];
-            window_run<T, MAX>(tile + r * RWp + c, 1, p.kw, res);
-#pragma unroll
-            for (int j = 0; j < kRun; j++) rows[r * kTileW + c + j] = res[j];
-        }
+        tile_compute<T, MAX, KH, KW>(tile, RWp, rows, p, dst, x0, y0);
         __syncthreads();
-        // 3. column pass and store: kTileH x kTileW outputs, runs down columns
-        const int runs_per_col = kTileH / kRun;
-        for (int w = threadIdx.x; w < kTileW * runs_per_col; w += kFlatThreads) {
-            int c = w % kTileW, r = (w / kTileW) * kRun;
-            int gx = x0 + c;
-            // kTileH is a multiple of kRun, so the run reads rows
-            // r .. r + kRun + kh - 2 <= RH - 1: always inside the row buffer
-            T res[kRun];
-            window_run<T, MAX>(rows + r * kTileW + c, kTileW, p.kh, res);
-            if (gx < p.W) {
+    }
+}
+
+// ------------------------------------------------ flat 2-D tile, TMA staged
+// Persistent kernel for the tiles whose input region lies inside the item
+// (every tile of a large image but the outer ring).  Each CTA walks the
+// interior tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...; thread 0 issues
+// one TMA tensor copy per tile into one of two shared-memory buffers, so the
+// next tile's load is in flight while the current one is computed.  The TMA
+// box starts at the 16-byte-aligned column at or left of the tile's first
+// input column; the compute reads from the offset inside the buffer.
+struct TmaTileParams {
+    int bw;     // box width in elements (multiple of align)
+    int align;  // elements per 16 bytes
+    int ntx, nty;
+    int64_t ntiles;
+    // interior tiles: rows [ya, yb) x columns [xa, xb) of every item; work
+    // units 0 .. n_interior-1 are interior tiles, the rest the border ring
+    int ya, yb, xa, xb;
+    int64_t n_interior;
+};
+
+// Work unit u -> (item, tx, ty): interior tiles first, then each item's ring
+// (full rows above ya and from yb on, then the side columns of the rows in
+// between).
+__device__ __forceinline__ void unit_to_tile(const TmaTileParams &tp, int64_t u, int64_t &item, int &tx, int &ty,
+                                             bool &inner) {
+    const int iw = tp.xb - tp.xa, ih = tp.yb - tp.ya;
+    if (u < tp.n_interior) {
+        const int64_t per = (int64_t)iw * ih;
+        item = u / per;
+        const int k = (int)(u - item * per);
+        ty = tp.ya + k / iw;
+        tx = tp.xa + k % iw;
+        inner = true;
+        return;
+    }
+    inner = false;
+    const int64_t ring = (int64_t)tp.ntx * tp.nty - (int64_t)iw * ih;
+    const int64_t v = u - tp.n_interior;
+    item = v / ring;
+    int i = (int)(v - item * ring);
+    const int top = tp.ya * tp.ntx, bottom = (tp.nty - tp.yb) * tp.ntx, side = tp.xa + (tp.ntx - tp.xb);
+    if (i < top) {
+        ty = i / tp.ntx;
+        tx = i % tp.ntx;
+    } else if (i < top + bottom) {
+        i -= top;
+        ty = tp.yb + i / tp.ntx;
+        tx = i % tp.ntx;
+    } else {
+        i -= top + bottom;
+        ty = tp.ya + i / side;
+        const int k = i % side;
+        tx = k < tp.xa ? k : tp.xb + (k - tp.xa);
+    }
+}
+
+__host__ __device__ __forceinline__ size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+constexpr int kMaxStageCols = 8;  // TMA tiles are at most 256 columns wide
+
+template <typename T, bool MAX, int KH, int KW>
+__global__ void __launch_bounds__(kFlatThreads) flat2d_tma_kernel(const __grid_constant__ CUtensorMap tmap,
+                                                                  const T *__restrict__ in, T *__restrict__ out,
+                                                                  Flat2DParams p, TmaTileParams tp, int *status) {
+    extern __shared__ __align__(16) unsigned char smem_dyn[];
+    // TMA destinations must be 128-byte aligned: round the dynamic base up (the
+    // launch asks for 1 KB of slack)
+    unsigned char *smem_raw = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~static_cast<uintptr_t>(1023));
+    const int RH = kTileH + p.kh - 1;
+    const int RW = kTileW + p.kw - 1;
+    const size_t buf_bytes = round_up((size_t)RH * tp.bw * sizeof(T), 1024);
+    T *buf[2] = {reinterpret_cast<T *>(smem_raw), reinterpret_cast<T *>(smem_raw + buf_bytes)};
+    T *rows = reinterpret_cast<T *>(smem_raw + 2 * buf_bytes);
+    const size_t rows_bytes = KH == 0 ? round_up((size_t)RH * kTileW * sizeof(T), 16) : 0;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + 2 * buf_bytes + rows_bytes);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const uint32_t bytes = (uint32_t)(RH * tp.bw * sizeof(T));
+    auto interior = [&](int64_t u) { return u < tp.n_interior; };
+    auto issue = [&](int64_t u, int s) {
+        int64_t item;
+        int tx, ty;
+        bool inner;
+        unit_to_tile(tp, u, item, tx, ty, inner);
+        const int gx0 = tx * kTileW + p.lo_x, gy0 = ty * kTileH + p.lo_y;
+        mbar_arrive_expect_tx(&bar[s], bytes);
+        tma_load_3d(buf[s], &tmap, gx0 & ~(tp.align - 1), gy0, (int)item, &bar[s]);
+    };
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const T cval = (T)p.cval;
+    uint32_t phase0 = 0, phase1 = 0;
+    int64_t t = blockIdx.x;
+    if (threadIdx.x == 0 && t < tp.ntiles && interior(t)) issue(t, 0);
+    for (int it = 0; t < tp.ntiles; it++, t += gridDim.x) {
+        const int s = it & 1;
+        const int64_t tn = t + gridDim.x;
+        if (threadIdx.x == 0 && tn < tp.ntiles && interior(tn)) issue(tn, s ^ 1);
+        int64_t item;
+        int tx, ty;
+        bool inner;
+        unit_to_tile(tp, t, item, tx, ty, inner);
+        const int gx0 = tx * kTileW + p.lo_x, gy0 = ty * kTileH + p.lo_y;
+        int off = 0;
+        if (inner) {
+            const uint32_t ph = s == 0 ? phase0 : phase1;
+            const bool landed = mbar_wait(&bar[s], ph, status);
+            if (s == 0)
+                phase0 ^= 1;
+            else
+                phase1 ^= 1;
+            if (__syncthreads_or(!landed)) {
+                // give the copy already issued for the next tile a bounded chance to land
+                if (threadIdx.x == 0 && tn < tp.ntiles && interior(tn))
+                    mbar_wait(&bar[s ^ 1], s == 0 ? phase1 : phase0, status);
+                return;
+            }
+            off = gx0 - (gx0 & ~(tp.align - 1));
+        } else {
+            // border tile: stage the mapped region by hand; each lane maps its
+            // (at most kMaxStageCols) columns once
+            const T *src = in + item * (int64_t)p.H * p.W;
+            int mxs[kMaxStageCols];
 #pragma unroll
-                for (int j = 0; j < kRun; j++) {
-                    int gy = y0 + r + j;
-                    if (gy < p.H) dst[(int64_t)gy * p.W + gx] = Op::apply(res[j], p.sval);
+            for (int k = 0; k < kMaxStageCols; k++) {
+                const int c = lane + 32 * k;
+                mxs[k] = c < RW ? map_coord(gx0 + c, p.W, p.mode) : -1;
+            }
+            for (int rr = warp; rr < RH; rr += kFlatThreads / 32) {
+                const int my = map_coord(gy0 + rr, p.H, p.mode);
+                const T *srow = src + (int64_t)(my < 0 ? 0 : my) * p.W;
+#pragma unroll
+                for (int k = 0; k < kMaxStageCols; k++) {
+                    const int c = lane + 32 * k;
+                    if (c < RW) buf[s][rr * tp.bw + c] = (my < 0 || mxs[k] < 0) ? cval : srow[mxs[k]];
                 }
             }
+            __syncthreads();
         }
+        tile_compute<T, MAX, KH, KW>(buf[s] + off, tp.bw, rows, p, out + item * (int64_t)p.H * p.W, tx * kTileW,
+                                     ty * kTileH);
         __syncthreads();
     }
 }
@@ -283,6 +505,85 @@ struct Tap {
     float val;
 };
 
+// Flat 1-D/2-D box: the mapped-border kernel for every tile (or only the
+// border ring when the TMA kernel takes the interior), then the TMA kernel.
+template <typename T, bool MAX, int KH, int KW>
+int launch_flat2d(const T *in, T *out, Flat2DParams p, int64_t batch, int sms, cudaStream_t stream) {
+    const int RH = kTileH + p.kh - 1, RWp = kTileW + p.kw - 1 + (kRun - 1);
+    const size_t rows_bytes = KH == 0 ? (size_t)RH * kTileW * sizeof(T) : 0;
+    const size_t smem = (size_t)RH * RWp * sizeof(T) + rows_bytes;
+    if (smem > 48 * 1024)
+        TM_CHECK_CUDA(cudaFuncSetAttribute(flat2d_kernel<T, MAX, KH, KW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem));
+    dim3 grid((unsigned)ceil_div(p.W, kTileW), (unsigned)ceil_div(p.H, kTileH),
+              (unsigned)(batch < 65535 ? batch : 65535));
+    // TMA path for the interior tiles: needs 16-byte aligned rows and a box of at most 256 x 256
+    TmaTileParams tp;
+    tp.align = 16 / (int)sizeof(T);
+    tp.bw = (int)round_up((size_t)(kTileW + p.kw - 1 + tp.align - 1), (size_t)tp.align);
+    tp.ntx = (int)grid.x;
+    tp.nty = (int)grid.y;
+    tp.ntiles = (int64_t)tp.ntx * tp.nty * batch;
+    {
+        // interior tile rows/columns: the region of tile t starts at
+        // t * tile + lo and is RH (RW) long
+        auto first_ge = [](int lo, int tile) { return lo >= 0 ? 0 : (-lo + tile - 1) / tile; };
+        const int RW = kTileW + p.kw - 1;
+        tp.ya = first_ge(p.lo_y, kTileH);
+        tp.yb = (p.H - RH - p.lo_y) >= 0 ? (p.H - RH - p.lo_y) / kTileH + 1 : 0;
+        tp.xa = first_ge(p.lo_x, kTileW);
+        tp.xb = (p.W - RW - p.lo_x) >= 0 ? (p.W - RW - p.lo_x) / kTileW + 1 : 0;
+        tp.yb = std::min(std::max(tp.yb, tp.ya), tp.nty);
+        tp.xb = std::min(std::max(tp.xb, tp.xa), tp.ntx);
+        tp.ya = std::min(tp.ya, tp.yb);
+        tp.xa = std::min(tp.xa, tp.xb);
+        tp.n_interior = (int64_t)(tp.yb - tp.ya) * (tp.xb - tp.xa) * batch;
+    }
+    // one persistent launch takes every tile (TMA for interior tiles) once a
+    // batch has a few tiles per SM; otherwise the plain kernel does all
+    const bool tma_ok = (p.W % tp.align) == 0 && ((uintptr_t)in & 15) == 0 && tp.bw <= 256 && RH <= 256 &&
+                        p.H >= RH && p.W >= tp.bw && tp.ntiles >= 2LL * sms && tp.ntiles < ((int64_t)1 << 31) &&
+                        batch < ((int64_t)1 << 31);
+    if (!tma_ok) {
+        flat2d_kernel<T, MAX, KH, KW><<<grid, kFlatThreads, smem, stream>>>(in, out, p);
+        TM_LAUNCH_CHECK("flat2d_kernel");
+        return TM_OK;
+    }
+    CUtensorMap map;
+    const uint64_t dims[3] = {(uint64_t)p.W, (uint64_t)p.H, (uint64_t)batch};
+    const uint64_t strides[2] = {(uint64_t)p.W * sizeof(T), (uint64_t)p.W * p.H * sizeof(T)};
+    const uint32_t box[3] = {(uint32_t)tp.bw, (uint32_t)RH, 1};
+    int st = encode_tensor_map(&map, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT8,
+                               3, in, dims, strides, box);
+    if (st != TM_OK) return st;
+    int *status = nullptr;
+    st = device_status_word(&status);
+    if (st != TM_OK) return st;
+    const size_t tsmem = 2 * round_up((size_t)RH * tp.bw * sizeof(T), 1024) +
+                         (KH == 0 ? round_up((size_t)RH * kTileW * sizeof(T), 16) : 0) + 2 * sizeof(uint64_t) + 1024;
+    if (tsmem > 220 * 1024) return fail(TM_ERR_UNSUPPORTED, "TMA tile does not fit in shared memory");
+    // attribute + occupancy depend only on the instantiation and the smem size: cache the last answer
+    static thread_local size_t cached_smem = 0;
+    static thread_local int cached_dev = -1, cached_per_sm = 1;
+    int dev = 0;
+    TM_CHECK_CUDA(cudaGetDevice(&dev));
+    if (cached_smem != tsmem || cached_dev != dev) {
+        TM_CHECK_CUDA(cudaFuncSetAttribute(flat2d_tma_kernel<T, MAX, KH, KW>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
+        int per_sm = 0;
+        TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, flat2d_tma_kernel<T, MAX, KH, KW>,
+                                                                    kFlatThreads, tsmem));
+        cached_per_sm = per_sm < 1 ? 1 : per_sm;
+        cached_smem = tsmem;
+        cached_dev = dev;
+    }
+    const int per_sm = cached_per_sm;
+    const int64_t ctas = std::min<int64_t>(tp.ntiles, (int64_t)sms * per_sm);
+    flat2d_tma_kernel<T, MAX, KH, KW><<<(unsigned)ctas, kFlatThreads, tsmem, stream>>>(map, in, out, p, tp, status);
+    TM_LAUNCH_CHECK("flat2d_tma_kernel");
+    return TM_OK;
+}
+
 template <typename T, bool MAX>
 int run_morphology(const T *in, T *out, int64_t batch, int ndim, const int64_t *shape,
                    const float *structure, const uint8_t *footprint, const int64_t *sshape,
@@ -350,16 +651,11 @@ int run_morphology(const T *in, T *out, int64_t batch, int ndim, const int64_t *
         if (p.kh > 4096 || p.kw > 4096) goto stencil;  // tile would not fit on chip
         {
             const int RH = kTileH + p.kh - 1, RW = kTileW + p.kw - 1 + (kRun - 1);
-            size_t smem = (size_t)RH * RW * sizeof(T) + (size_t)RH * kTileW * sizeof(T);
-            if (smem > 200 * 1024) goto stencil;
-            if (smem > 48 * 1024)
-                TM_CHECK_CUDA(cudaFuncSetAttribute(flat2d_kernel<T, MAX>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            dim3 grid((unsigned)ceil_div(p.W, kTileW), (unsigned)ceil_div(p.H, kTileH),
-                      (unsigned)(batch < 65535 ? batch : 65535));
-            flat2d_kernel<T, MAX><<<grid, kFlatThreads, smem, stream>>>(in, out, p);
-            TM_LAUNCH_CHECK("flat2d_kernel");
-            return TM_OK;
+            if ((size_t)RH * RW * sizeof(T) + (size_t)RH * kTileW * sizeof(T) > 200 * 1024) goto stencil;
+            if (p.kh == 3 && p.kw == 3) return launch_flat2d<T, MAX, 3, 3>(in, out, p, batch, sms, stream);
+            if (p.kh == 5 && p.kw == 5) return launch_flat2d<T, MAX, 5, 5>(in, out, p, batch, sms, stream);
+            if (p.kh == 1 && p.kw == 3) return launch_flat2d<T, MAX, 1, 3>(in, out, p, batch, sms, stream);
+            return launch_flat2d<T, MAX, 0, 0>(in, out, p, batch, sms, stream);
         }
     }
 stencil:

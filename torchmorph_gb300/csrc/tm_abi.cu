@@ -1,7 +1,11 @@
 // Status strings, error reporting and geometry helpers of libtmcore.
+#include <cudaTypedefs.h>
+
 #include <cstring>
+#include <mutex>
 
 #include "tm_common.cuh"
+#include "tm_tma.cuh"
 
 namespace tmc {
 
@@ -67,7 +71,71 @@ int make_geometry(int64_t batch, int ndim, const int64_t *shape, Geometry *g) {
     return TM_OK;
 }
 
+// ----------------------------------------------------------------------------
+// Device status word: kernels record device-side failures here (for example a
+// bounded wait that gave up); tm_device_error() reads and optionally clears it.
+static __device__ int g_device_status;
+static std::mutex g_status_mutex;
+static int *g_status_ptr[64] = {nullptr};
+
+int device_status_word(int **out) {
+    int dev = 0;
+    int st = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    if (st != TM_OK) return st;
+    if (dev < 0 || dev >= 64) return fail(TM_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_status_mutex);
+    if (!g_status_ptr[dev]) {
+        void *p = nullptr;
+        st = cuda_check(cudaGetSymbolAddress(&p, g_device_status), "cudaGetSymbolAddress(status word)");
+        if (st != TM_OK) return st;
+        g_status_ptr[dev] = static_cast<int *>(p);
+    }
+    *out = g_status_ptr[dev];
+    return TM_OK;
+}
+
+int encode_tensor_map(CUtensorMap *map, CUtensorMapDataType dtype, int rank, const void *gaddr,
+                      const uint64_t *dims, const uint64_t *strides_bytes, const uint32_t *box) {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    static cudaError_t once_err = cudaSuccess;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void *f = nullptr;
+        once_err = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q);
+        if (once_err == cudaSuccess && q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    });
+    if (!fn) return fail(TM_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    cuuint64_t gdim[5];
+    cuuint64_t gstride[4];
+    cuuint32_t bdim[5], estride[5];
+    for (int i = 0; i < rank; i++) {
+        gdim[i] = dims[i];
+        bdim[i] = box[i];
+        estride[i] = 1;
+    }
+    for (int i = 0; i < rank - 1; i++) gstride[i] = strides_bytes[i];
+    CUresult r = fn(map, dtype, (cuuint32_t)rank, const_cast<void *>(gaddr), gdim, gstride, bdim, estride,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(TM_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return TM_OK;
+}
+
 }  // namespace tmc
+
+extern "C" int tm_device_error(int reset) {
+    int *word = nullptr;
+    if (tmc::device_status_word(&word) != TM_OK) return -1;
+    int v = 0;
+    if (cudaMemcpy(&v, word, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    if (reset && v != 0) {
+        const int zero = 0;
+        if (cudaMemcpy(word, &zero, sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) return -1;
+    }
+    return v;
+}
 
 extern "C" const char *tm_status_string(int status) {
     switch (status) {
