@@ -178,6 +178,45 @@ int tm_sinkhorn_logiter(const float *log_a, const float *log_b, const float *M,
                         const float *M_T, float *log_u, float *log_v, int64_t n, int64_t d,
                         int64_t n_iter, double epsilon, tm_stream_t stream);
 
+/* ------------------------------------------------ sinkhorn, tensor cores --
+ * Shared-cost batched Sinkhorn on the tcgen05 tensor cores.  Replaces, for
+ * n histogram pairs sharing one (d, d) cost, the iterations of
+ * _scaling_iterations / _log_iterations (torchmorph/optimal_transport.py:
+ * 71-125, fused path sinkhorn_fastiter / sinkhorn_logiter) and the plan
+ * materialisation of _SinkhornDistance.forward (:136-144):
+ *   init     builds K = exp(-C/eps), K^T and K o C (bf16 hi + lo) and sets
+ *            log u = log v = 0 (the reference's start);
+ *   iterate  runs n_iter iterations (u update, then v update); when row_err
+ *            (device, fp64[n]) is given it receives the L1 row-marginal
+ *            residual sum_i |a_i - (P 1)_i| of the plan the last iteration
+ *            started from;
+ *   finish   writes log_u, log_v (device fp32 (n, d)), cost[h] = <P_h, C>
+ *            and row_err[h] (device fp64[n]) for the current potentials;
+ *            any output may be NULL.
+ * a, b: device fp32 (n, d), rows summing to 1; C: device fp32 (d, d).
+ * The workspace (256-byte aligned, tm_sinkhorn_tc_workspace_size bytes)
+ * holds the whole solver state between the calls.  No counterpart in the
+ * reference's extension. */
+size_t tm_sinkhorn_tc_workspace_size(int64_t n, int64_t d);
+int tm_sinkhorn_tc_init(const float *a, const float *b, const float *C, int64_t n, int64_t d,
+                        double epsilon, void *workspace, size_t workspace_bytes,
+                        tm_stream_t stream);
+int tm_sinkhorn_tc_iterate(int64_t n, int64_t d, int64_t n_iter, double *row_err,
+                           void *workspace, size_t workspace_bytes, tm_stream_t stream);
+int tm_sinkhorn_tc_finish(int64_t n, int64_t d, float *log_u, float *log_v, double *cost,
+                          double *row_err, void *workspace, size_t workspace_bytes,
+                          tm_stream_t stream);
+
+/* Error-compensated BF16 tensor-core product D = A B^T in fp32, with
+ * A = a_hi + a_lo (M x K) and B = b_hi + b_lo (N x K), all bf16 row-major
+ * device arrays, D fp32 M x N row-major: three tcgen05 MMAs per k-step
+ * (hi.hi + lo.hi + hi.lo).  M and N multiples of 128, K a multiple of 64,
+ * pointers 16-byte aligned.  No counterpart in the reference: this is the
+ * product the shared-cost Sinkhorn solver below runs on, exported so that
+ * callers can test it on its own. */
+int tm_gemm_bf16x3(const void *a_hi, const void *a_lo, const void *b_hi, const void *b_lo,
+                   float *d, int64_t M, int64_t N, int64_t K, tm_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

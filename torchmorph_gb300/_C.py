@@ -289,3 +289,51 @@ def sinkhorn_logiter(log_a, log_b, M, M_T, log_u, log_v, n_iter, epsilon):
                                      float(epsilon), _lib.stream_of(log_u.device))
     _lib.check(st, "sinkhorn_logiter")
     return log_u, log_v
+
+
+# ----------------------------------------------- sinkhorn on tensor cores
+def sinkhorn_tc_solve(a, b, cost_matrix, epsilon, max_iter, threshold=0.0, check_every=10):
+    """Shared-cost batched Sinkhorn on the tensor cores (libtmcore tm_sinkhorn_tc_*).
+
+    a, b: (n, d) float32 CUDA histograms (rows summing to 1); cost_matrix (d, d).
+    Runs max_iter iterations, or stops after the first multiple of
+    `check_every` iterations whose L1 row-marginal residual is <= threshold
+    for every pair (threshold > 0).  Returns (log_u, log_v, cost, row_err,
+    iterations): fp32 (n, d) log-potentials with the reference's meaning,
+    fp64 (n,) transport costs <P, C> and L1 row-marginal residuals of the
+    returned potentials, and the number of iterations run.
+    """
+    _require(epsilon > 0, f"epsilon must be positive, got {epsilon}")
+    _require(a.dim() == 2 and a.shape == b.shape, "a and b must be (n, d) of the same shape")
+    n, d = a.shape
+    for t, name in ((a, "a"), (b, "b")):
+        _ot_check(t, n * d, name)
+    _ot_check(cost_matrix, d * d, "cost_matrix")
+    lib = _lib.load()
+    dev = a.device
+    with torch.cuda.device(dev):
+        stream = _lib.stream_of(dev)
+        nbytes = lib.tm_sinkhorn_tc_workspace_size(n, d)
+        ws = _workspace(nbytes, dev)
+        _lib.check(lib.tm_sinkhorn_tc_init(_lib.ptr(a), _lib.ptr(b), _lib.ptr(cost_matrix), n, d,
+                                           float(epsilon), _lib.ptr(ws), nbytes, stream),
+                   "sinkhorn_tc_init")
+        err = torch.zeros(n, dtype=torch.float64, device=dev)
+        done = 0
+        max_iter = int(max_iter)
+        while done < max_iter:
+            step = min(int(check_every), max_iter - done) if threshold > 0 else max_iter - done
+            _lib.check(lib.tm_sinkhorn_tc_iterate(n, d, step, _lib.ptr(err) if threshold > 0 else None,
+                                                  _lib.ptr(ws), nbytes, stream),
+                       "sinkhorn_tc_iterate")
+            done += step
+            if threshold > 0 and err.max().item() <= threshold:
+                break
+        log_u = torch.empty((n, d), dtype=torch.float32, device=dev)
+        log_v = torch.empty_like(log_u)
+        cost = torch.empty(n, dtype=torch.float64, device=dev)
+        row_err = torch.empty_like(cost)
+        _lib.check(lib.tm_sinkhorn_tc_finish(n, d, _lib.ptr(log_u), _lib.ptr(log_v), _lib.ptr(cost),
+                                             _lib.ptr(row_err), _lib.ptr(ws), nbytes, stream),
+                   "sinkhorn_tc_finish")
+    return log_u, log_v, cost, row_err, done

@@ -56,6 +56,14 @@ SIGNATURES = {
                                      c_i64, c_void]),
     "tm_sinkhorn_logiter": (c_int, [c_void, c_void, c_void, c_void, c_void, c_void, c_i64, c_i64,
                                     c_i64, c_double, c_void]),
+    "tm_gemm_bf16x3": (c_int, [c_void, c_void, c_void, c_void, c_void, c_i64, c_i64, c_i64,
+                               c_void]),
+    "tm_sinkhorn_tc_workspace_size": (c_size, [c_i64, c_i64]),
+    "tm_sinkhorn_tc_init": (c_int, [c_void, c_void, c_void, c_i64, c_i64, c_double, c_void, c_size,
+                                    c_void]),
+    "tm_sinkhorn_tc_iterate": (c_int, [c_i64, c_i64, c_i64, c_void, c_void, c_size, c_void]),
+    "tm_sinkhorn_tc_finish": (c_int, [c_i64, c_i64, c_void, c_void, c_void, c_void, c_void, c_size,
+                                      c_void]),
 }
 
 TM_F32 = 0

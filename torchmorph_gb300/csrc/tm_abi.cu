@@ -95,7 +95,8 @@ int device_status_word(int **out) {
 }
 
 int encode_tensor_map(CUtensorMap *map, CUtensorMapDataType dtype, int rank, const void *gaddr,
-                      const uint64_t *dims, const uint64_t *strides_bytes, const uint32_t *box) {
+                      const uint64_t *dims, const uint64_t *strides_bytes, const uint32_t *box,
+                      CUtensorMapSwizzle swizzle) {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     static std::once_flag once;
     static cudaError_t once_err = cudaSuccess;
@@ -117,7 +118,7 @@ int encode_tensor_map(CUtensorMap *map, CUtensorMapDataType dtype, int rank, con
     }
     for (int i = 0; i < rank - 1; i++) gstride[i] = strides_bytes[i];
     CUresult r = fn(map, dtype, (cuuint32_t)rank, const_cast<void *>(gaddr), gdim, gstride, bdim, estride,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(TM_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return TM_OK;

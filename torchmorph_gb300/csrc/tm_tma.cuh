@@ -22,7 +22,8 @@ int device_status_word(int **out);
 // Encode a tiled tensor map (rank <= 5).  dims[0] is the innermost
 // (contiguous) extent; strides_bytes has rank-1 entries (dims 1..rank-1).
 int encode_tensor_map(CUtensorMap *map, CUtensorMapDataType dtype, int rank, const void *gaddr,
-                      const uint64_t *dims, const uint64_t *strides_bytes, const uint32_t *box);
+                      const uint64_t *dims, const uint64_t *strides_bytes, const uint32_t *box,
+                      CUtensorMapSwizzle swizzle = CU_TENSOR_MAP_SWIZZLE_NONE);
 
 constexpr long long kSpinLimit = 1LL << 26;
 

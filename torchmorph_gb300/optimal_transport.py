@@ -1,9 +1,19 @@
 """Entropic optimal transport (reference torchmorph/optimal_transport.py).
 
 ``SinkhornSolver`` keeps the reference's constructor, forward/plan/potentials
-API, preprocessing and autograd contract.  CUDA float32 inputs run the fused
-libtmcore iterations (``_C.sinkhorn_logiter`` / ``_C.sinkhorn_fastiter``);
-other dtypes/devices run the same iterations in plain torch, exactly as the
+API, preprocessing and autograd contract.  CUDA float32 inputs run libtmcore:
+
+* many histogram pairs sharing one cost (``tensor_cores=None`` picks this
+  for n >= 32 pairs of d >= 256 points; ``True`` forces it) run the
+  tensor-core solver ``_C.sinkhorn_tc_solve``: the K v and K^T u products of
+  all pairs as one error-compensated BF16 GEMM per half-iteration, the
+  transport cost as one more GEMM (no (n, d, d) plan is materialised), and,
+  when ``threshold > 0``, a stop once every pair's L1 row-marginal residual
+  is <= threshold (checked every 10 iterations, fp64);
+* otherwise the fused FP32 iterations (``_C.sinkhorn_logiter`` /
+  ``_C.sinkhorn_fastiter``), as in the reference.
+
+Other dtypes/devices run the same iterations in plain torch, exactly as the
 reference does.
 """
 
@@ -24,6 +34,27 @@ def build_cost_matrix(shape, p=2, device=None) -> Tensor:
 
 def _use_fused_kernels(t: Tensor) -> bool:
     return t.is_cuda and t.dtype == torch.float32
+
+
+_TC_MIN_PAIRS = 32
+_TC_MIN_POINTS = 256
+_TC_CHECK_EVERY = 10
+
+
+def _use_tensor_cores(a: Tensor, cost_matrix: Tensor, tensor_cores) -> bool:
+    eligible = _use_fused_kernels(a) and cost_matrix.shape == (a.shape[1], a.shape[1])
+    if tensor_cores is None:
+        return eligible and a.shape[0] >= _TC_MIN_PAIRS and a.shape[1] >= _TC_MIN_POINTS
+    if tensor_cores and not eligible:
+        raise ValueError("tensor_cores=True needs CUDA float32 histograms and a (d, d) cost.")
+    return bool(tensor_cores)
+
+
+def _tensor_core_solve(a, b, cost_matrix, epsilon, max_iter, threshold):
+    from . import _C
+
+    return _C.sinkhorn_tc_solve(a.contiguous(), b.contiguous(), cost_matrix, epsilon, max_iter,
+                                threshold, _TC_CHECK_EVERY)
 
 
 def _transpose_or_self(matrix: Tensor) -> Tensor:
@@ -110,11 +141,16 @@ class _SinkhornDistance(torch.autograd.Function):
     """<P, C> with envelope-theorem gradients (centred dual potentials) for a and b."""
 
     @staticmethod
-    def forward(ctx, a, b, cost_matrix, epsilon, max_iter, threshold, log_space):
-        iterate = _log_iterations if log_space else _scaling_iterations
-        log_u, log_v = iterate(a, b, cost_matrix, epsilon, max_iter, threshold)
-        plan = torch.exp(log_u.unsqueeze(-1) - cost_matrix / epsilon + log_v.unsqueeze(-2))
-        distance = (plan * cost_matrix).sum(dim=(-2, -1))
+    def forward(ctx, a, b, cost_matrix, epsilon, max_iter, threshold, log_space, tensor_cores):
+        if _use_tensor_cores(a, cost_matrix, tensor_cores):
+            log_u, log_v, cost, _, _ = _tensor_core_solve(a, b, cost_matrix, epsilon, max_iter,
+                                                          threshold)
+            distance = cost.to(a.dtype)
+        else:
+            iterate = _log_iterations if log_space else _scaling_iterations
+            log_u, log_v = iterate(a, b, cost_matrix, epsilon, max_iter, threshold)
+            plan = torch.exp(log_u.unsqueeze(-1) - cost_matrix / epsilon + log_v.unsqueeze(-2))
+            distance = (plan * cost_matrix).sum(dim=(-2, -1))
         f = epsilon * log_u
         g = epsilon * log_v
         ctx.save_for_backward(f - f.mean(dim=-1, keepdim=True), g - g.mean(dim=-1, keepdim=True))
@@ -124,13 +160,14 @@ class _SinkhornDistance(torch.autograd.Function):
     def backward(ctx, grad_output):
         f, g = ctx.saved_tensors
         grad = grad_output.unsqueeze(-1)
-        return grad * f, grad * g, None, None, None, None, None
+        return grad * f, grad * g, None, None, None, None, None, None
 
 
 class SinkhornSolver(nn.Module):
     """Entropy-regularised balanced OT between (n, d) histogram batches sharing a (d, d) cost."""
 
-    def __init__(self, epsilon=1.0, max_iter=100, threshold=0.0, p=2, log_space=False):
+    def __init__(self, epsilon=1.0, max_iter=100, threshold=0.0, p=2, log_space=False,
+                 tensor_cores=None):
         super().__init__()
         if epsilon <= 0:
             raise ValueError("epsilon must be positive.")
@@ -143,6 +180,7 @@ class SinkhornSolver(nn.Module):
         self.threshold = threshold
         self.p = p
         self.log_space = log_space
+        self.tensor_cores = tensor_cores
 
     def extra_repr(self):
         return (
@@ -174,7 +212,31 @@ class SinkhornSolver(nn.Module):
         """(n,) transport distances <P, C> between the rows of source and target."""
         source, target, cost_matrix = self.data_preprocess(source, target, cost_matrix)
         return _SinkhornDistance.apply(source, target, cost_matrix, self.epsilon, self.max_iter,
-                                       self.threshold, self.log_space)
+                                       self.threshold, self.log_space, self.tensor_cores)
+
+    @torch.no_grad()
+    def solve(self, source: Tensor, target: Tensor, cost_matrix: Optional[Tensor] = None):
+        """One solve with its diagnostics: a dict with ``distance`` (n,), centred
+        potentials ``f``, ``g`` (n, d), ``marginal_error`` (n,) -- the L1 distance
+        between the plan's row sums and the source histogram, in float64 -- and
+        ``iterations``."""
+        source, target, cost_matrix = self.data_preprocess(source, target, cost_matrix)
+        if _use_tensor_cores(source, cost_matrix, self.tensor_cores):
+            log_u, log_v, cost, row_err, its = _tensor_core_solve(
+                source, target, cost_matrix, self.epsilon, self.max_iter, self.threshold)
+            distance = cost.to(source.dtype)
+        else:
+            log_u, log_v = self._iterate(source, target, cost_matrix)
+            plan = torch.exp(log_u.unsqueeze(-1) - cost_matrix / self.epsilon
+                             + log_v.unsqueeze(-2))
+            distance = (plan * cost_matrix).sum(dim=(-2, -1))
+            row_err = (plan.double().sum(-1) - source.double()).abs().sum(-1)
+            its = self.max_iter
+        f = self.epsilon * log_u
+        g = self.epsilon * log_v
+        return {"distance": distance, "f": f - f.mean(dim=-1, keepdim=True),
+                "g": g - g.mean(dim=-1, keepdim=True), "marginal_error": row_err,
+                "iterations": its}
 
     @torch.no_grad()
     def plan(self, source: Tensor, target: Tensor, cost_matrix: Optional[Tensor] = None):
@@ -193,5 +255,9 @@ class SinkhornSolver(nn.Module):
         return f - f.mean(dim=-1, keepdim=True), g - g.mean(dim=-1, keepdim=True)
 
     def _iterate(self, a, b, cost_matrix):
+        if _use_tensor_cores(a, cost_matrix, self.tensor_cores):
+            log_u, log_v, _, _, _ = _tensor_core_solve(a, b, cost_matrix, self.epsilon,
+                                                       self.max_iter, self.threshold)
+            return log_u, log_v
         iterate = _log_iterations if self.log_space else _scaling_iterations
         return iterate(a, b, cost_matrix, self.epsilon, self.max_iter, self.threshold)
