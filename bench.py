@@ -4,8 +4,10 @@ Headline workload: exact 3-D Euclidean distance transform with feature
 indices -- 4 bool volumes of 128^3, foreground iid Bernoulli(0.9) (seed 0),
 unit sampling, float32 distances + int32 indices.  Secondary workloads in
 the same JSON line: flat 3x3 grey dilation (8 x 256^2 and an HBM-resident
-8 x 4096^2), binary dilation, chessboard chamfer on the EDT volumes and the
-plain FP32 log-domain Sinkhorn iteration.
+8 x 4096^2), binary dilation, chessboard chamfer on the EDT volumes, and the
+shared-cost batched Sinkhorn solve (256 pairs x 8192 points, eps 0.05 and
+0.01, to an L1 marginal residual of 1e-6) on the tensor cores with its
+float64 errors, next to the plain FP32 fused iterations.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -286,21 +288,142 @@ def secondary(args, dev, stream, hbm_peak):
     out["cdt_chessboard_4x128^3"] = {"Gvoxel/s": round(vol.numel() / (t / 3) / 1e9, 3),
                                      "ms_per_call": round(t / 3 * 1e3, 3)}
 
-    # plain FP32 log-domain Sinkhorn iteration, 256 histograms x d = 8192
-    n, d = 256, 8192
-    pts = torch.rand((d, 3), generator=g)
-    cost = torch.cdist(pts, pts).square()
-    cost = (cost / cost.max()).to(dev)
-    la = torch.log(torch.distributions.Dirichlet(torch.ones(d)).sample((n,))).to(dev)
-    lb = torch.log(torch.distributions.Dirichlet(torch.ones(d)).sample((n,))).to(dev)
-    lu = torch.zeros_like(la)
-    lv = torch.zeros_like(lb)
+    out.update(sinkhorn_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline))
+    return out
 
-    def sstep(_):
-        _C.sinkhorn_logiter(la, lb, cost, cost, lu, lv, 1, 0.05)
 
-    t = time_device(sstep, [None], 3, 1, stream)
-    out["sinkhorn_fp32_log_iteration_256x8192"] = {"ms_per_iteration": round(t / 3 * 1e3, 3)}
+def sinkhorn_problem(dev, n=256, d=8192, seed=0):
+    """Shared-cost Sinkhorn workload: x, y iid U[0,1]^3 (d points each), C = |x - y|^2
+    scaled to max 1, n histogram pairs iid Dirichlet(1), float32."""
+    import torch
+
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    x = torch.rand((d, 3), generator=g, dtype=torch.float64)
+    y = torch.rand((d, 3), generator=g, dtype=torch.float64)
+    cost = torch.cdist(x, y).square()
+    cost = (cost / cost.max()).float()
+    rng = np.random.default_rng(seed)
+    a = torch.tensor(rng.dirichlet(np.ones(d), n), dtype=torch.float32)
+    b = torch.tensor(rng.dirichlet(np.ones(d), n), dtype=torch.float32)
+    return a.to(dev), b.to(dev), cost.to(dev)
+
+
+def fp64_sinkhorn_errors(a, b, cost, eps, log_u, log_v, dist, iterations, pairs=8):
+    """Errors of a solve against float64 Sinkhorn (the reference's scaling iteration,
+    optimal_transport.py:84-93, run in float64 on the device for `pairs` pairs and
+    iterations + 2000 iterations): relative OT-cost error, and the float64 L1 row and
+    column marginal errors of the returned plan."""
+    import torch
+
+    K = torch.exp(-cost.double() / eps)
+    A, B = a[:pairs].double(), b[:pairs].double()
+    u, v = torch.ones_like(A), torch.ones_like(B)
+    for _ in range(iterations + 2000):
+        u = A / (v @ K.T)
+        v = B / (u @ K)
+    ref = ((u @ (K * cost.double())) * v).sum(-1)
+    U, V = torch.exp(log_u[:pairs].double()), torch.exp(log_v[:pairs].double())
+    rows = (U * (V @ K.T) - A).abs().sum(-1)
+    cols = (V * (U @ K) - B).abs().sum(-1)
+    rel = ((dist[:pairs].double() - ref).abs() / ref).max().item()
+    return {"rel_cost_error_vs_fp64": float(f"{rel:.3e}"),
+            "marginal_l1_rows_fp64": float(f"{rows.max().item():.3e}"),
+            "marginal_l1_cols_fp64": float(f"{cols.max().item():.3e}"),
+            "fp64_pairs_checked": pairs}
+
+
+def sinkhorn_cpu_baseline(a, b, cost, eps, iterations, pairs=2, sample_iters=6):
+    """The float64 Sinkhorn oracle (scaling form, OpenMP over all host threads) on a
+    sample of `pairs` pairs x `sample_iters` iterations, extrapolated to solves/s at the
+    GPU run's iteration count."""
+    import oracle
+
+    oracle.build()
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    A = a[:pairs].double().cpu().numpy()
+    B = b[:pairs].double().cpu().numpy()
+    C = cost.double().cpu().numpy()
+    oracle.sinkhorn(A, B, C, eps, 1, log_space=False, nthreads=cores)
+    t0 = time.perf_counter()
+    oracle.sinkhorn(A, B, C, eps, sample_iters, log_space=False, nthreads=cores)
+    per_pair_iter = (time.perf_counter() - t0) / (pairs * sample_iters)
+    return {"value": round(1.0 / (per_pair_iter * iterations), 3), "unit": "solves/s",
+            "cores": cores, "kind": "port",
+            "sample": f"{pairs} pairs x {sample_iters} float64 scaling iterations of the oracle, "
+                      f"extrapolated to {iterations} iterations per solve"}
+
+
+def sinkhorn_lines(dev, stream, cpu_baseline=True):
+    """Shared-cost batched Sinkhorn, 256 pairs x 8192 points, eps 0.05 and 0.01, run to
+    an L1 row-marginal residual <= 1e-6 on the tensor cores, against the plain FP32
+    fused iterations on the same GPU."""
+    import torch
+
+    from torchmorph_gb300 import SinkhornSolver, _C
+
+    a, b, cost = sinkhorn_problem(dev)
+    n, d = a.shape
+    out = {}
+    for eps in (0.05, 0.01):
+        solver = SinkhornSolver(epsilon=eps, max_iter=20000, threshold=1e-6, tensor_cores=True)
+        solver.solve(a, b, cost)  # warm-up
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        res = solver.solve(a, b, cost)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        its = int(res["iterations"])
+        log_u, log_v, dist, _, _ = _C.sinkhorn_tc_solve(a, b, cost, eps, its)
+        line = {"solves/s": round(n / t, 1), "ms_per_solve_batch": round(t * 1e3, 3),
+                "iterations": its, "us_per_iteration": round(t / its * 1e6, 1),
+                "max_marginal_l1_reported": float(f"{res['marginal_error'].max().item():.3e}")}
+        line.update(fp64_sinkhorn_errors(a, b, cost, eps, log_u, log_v, dist, its))
+        if cpu_baseline:
+            line["cpu_baseline"] = sinkhorn_cpu_baseline(a, b, cost, eps, its)
+        out[f"sinkhorn_tc_256x8192_eps{eps}"] = line
+
+    # pure iteration time (no setup / final cost): 60 minus 10 fixed iterations
+    times = {}
+    for k in (10, 60):
+        _C.sinkhorn_tc_solve(a, b, cost, 0.05, k)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        _C.sinkhorn_tc_solve(a, b, cost, 0.05, k)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times[k] = e0.elapsed_time(e1) / 1e3
+    t_it = (times[60] - times[10]) / 50
+    # per iteration: two products of (d x d) by (d x n), each as 3 bf16 MMA passes
+    flops = 2 * 3 * 2.0 * d * d * n
+    _, tc_peak, peak_kind = peaks()
+    out["sinkhorn_tc_iteration_256x8192"] = {
+        "us_per_iteration": round(t_it * 1e6, 1),
+        "roofline": {"bound": "tensor", "achieved": round(flops / t_it / 1e12, 1),
+                     "peak": tc_peak, "unit": "TFLOP/s", "frac": round(flops / t_it / 1e12 / tc_peak, 4),
+                     "peak_kind": peak_kind,
+                     "scope": "whole iteration (2 split-bf16 GEMMs of 8192x256x8192 with 3 MMA "
+                              "passes each + 2 potential-split kernels); executed bf16 MMA flops"}}
+
+    # the plain FP32 fused iterations (reference sinkhorn_fastiter / sinkhorn_logiter)
+    K = torch.exp(-cost / 0.05)
+    K_T = K.T.contiguous()
+    C_T = cost.T.contiguous()
+    u, v = torch.ones_like(a), torch.ones_like(b)
+    la, lb = a.log(), b.log()
+    lu, lv = torch.zeros_like(a), torch.zeros_like(b)
+    t_scal = time_device(lambda _: _C.sinkhorn_fastiter(a, b, K, K_T, u, v, 1), [None], 5, 1,
+                         stream) / 5
+    t_log = time_device(lambda _: _C.sinkhorn_logiter(la, lb, cost, C_T, lu, lv, 1, 0.05), [None],
+                        2, 1, stream) / 2
+    tc_it = t_it
+    out["sinkhorn_fp32_fused_256x8192"] = {
+        "ms_per_iteration_scaling": round(t_scal * 1e3, 3),
+        "ms_per_iteration_log": round(t_log * 1e3, 3),
+        "tensor_core_speedup_per_iteration_vs_scaling": round(t_scal / tc_it, 1),
+        "tensor_core_speedup_per_iteration_vs_log": round(t_log / tc_it, 1)}
     return out
 
 
@@ -363,8 +486,17 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--case", choices=["all", "sinkhorn"], default="all",
+                    help="sinkhorn: only the shared-cost Sinkhorn lines (one JSON object)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.case == "sinkhorn" and args.impl == "ours":
+        import torch
+
+        dev = torch.device("cuda", 0)
+        print(json.dumps(sinkhorn_lines(dev, torch.cuda.current_stream(dev),
+                                        cpu_baseline=not args.no_cpu_baseline)))
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
