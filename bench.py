@@ -288,8 +288,64 @@ def secondary(args, dev, stream, hbm_peak):
     out["cdt_chessboard_4x128^3"] = {"Gvoxel/s": round(vol.numel() / (t / 3) / 1e9, 3),
                                      "ms_per_call": round(t / 3 * 1e3, 3)}
 
+    out.update(ragged_lines(dev, stream, max(args.steps, 10), args.warmup))
     out.update(sinkhorn_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline))
     return out
+
+
+def ragged_images(seed=0, n=256):
+    """256 2-D float32 images, H and W iid uniform integers in [32, 1024], values U[0, 1)."""
+    rng = np.random.default_rng(seed)
+    shapes = [(int(rng.integers(32, 1025)), int(rng.integers(32, 1025))) for _ in range(n)]
+    return [rng.random(s, dtype=np.float32) for s in shapes]
+
+
+def ragged_lines(dev, stream, steps, warmup):
+    """Ragged batch: grey erosion size 5 and 15 plus binary opening of x > 0.5 (cross) on 256
+    uneven images -- one persistent launch per operator, the sequence replayed as one CUDA
+    graph -- against per-image launches of the drop-in operators."""
+    import torch
+
+    import torchmorph_gb300 as tm
+    from torchmorph_gb300 import RaggedBatch, ragged
+
+    imgs = ragged_images()
+    rb = RaggedBatch.from_images([torch.from_numpy(im).to(dev) for im in imgs])
+    views = [v[None, None] for v in rb.images()]
+    npx = rb.numel
+
+    def pipeline(b):
+        return (ragged.grey_erosion(b, size=5), ragged.grey_erosion(b, size=15),
+                ragged.binary_opening(b.map(lambda x: x > 0.5)))
+
+    def per_image(_):
+        for v in views:
+            tm.grey_erosion(v, size=5)
+            tm.grey_erosion(v, size=15)
+            tm.binary_opening(v > 0.5)
+
+    # correctness gate: persistent results equal the per-image operators
+    outs = pipeline(rb)
+    for i in (0, 100, 255):
+        assert torch.equal(outs[0][i], tm.grey_erosion(views[i], size=5)[0, 0])
+        assert torch.equal(outs[1][i], tm.grey_erosion(views[i], size=15)[0, 0])
+        assert torch.equal(outs[2][i], tm.binary_opening(views[i] > 0.5)[0, 0])
+    graph, _ = ragged.capture(pipeline, rb)
+    t_graph = time_device(lambda _: graph.replay(), [None], steps, warmup, stream) / steps
+    t_eager = time_device(lambda _: pipeline(rb), [None], steps, warmup, stream) / steps
+    t_img = time_device(per_image, [None], 3, 1, stream) / 3
+    hbm, _, kind = peaks()
+    algo = 18.0 * npx  # 4+4 (erosion 5) + 4+4 (erosion 15) + 1+1 (binary opening) bytes per pixel
+    return {"ragged_256_images_erosion5_15_binary_opening": {
+        "pixels": npx, "ms_persistent_graph": round(t_graph * 1e3, 3),
+        "ms_persistent_eager": round(t_eager * 1e3, 3), "ms_per_image_launches": round(t_img * 1e3, 3),
+        "speedup_vs_per_image": round(t_img / t_graph, 2),
+        "Gpixel/s": round(npx / t_graph / 1e9, 3),
+        "roofline": {"bound": "hbm", "achieved": round(algo / t_graph / 1e9, 1), "peak": hbm,
+                     "unit": "GB/s", "frac": round(algo / t_graph / 1e9 / hbm, 4), "peak_kind": kind,
+                     "scope": "whole pipeline (5 launches incl. the x > 0.5 threshold), 18 "
+                              "algorithmic B/pixel"},
+        "gpu_launches_per_step": 5}}
 
 
 def sinkhorn_problem(dev, n=256, d=8192, seed=0):
@@ -486,16 +542,19 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--case", choices=["all", "sinkhorn"], default="all",
-                    help="sinkhorn: only the shared-cost Sinkhorn lines (one JSON object)")
+    ap.add_argument("--case", choices=["all", "sinkhorn", "ragged"], default="all",
+                    help="only the shared-cost Sinkhorn or the ragged-batch lines (one JSON object)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    if args.case == "sinkhorn" and args.impl == "ours":
+    if args.case != "all" and args.impl == "ours":
         import torch
 
         dev = torch.device("cuda", 0)
-        print(json.dumps(sinkhorn_lines(dev, torch.cuda.current_stream(dev),
-                                        cpu_baseline=not args.no_cpu_baseline)))
+        stream = torch.cuda.current_stream(dev)
+        if args.case == "sinkhorn":
+            print(json.dumps(sinkhorn_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline)))
+        else:
+            print(json.dumps(ragged_lines(dev, stream, max(args.steps, 10), args.warmup)))
         return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -160,6 +160,41 @@ int tm_bfdt(const void *input, int in_dtype, int64_t batch, int ndim, const int6
             int metric, const float *sampling, float *dist, int32_t *indices,
             void *workspace, size_t workspace_bytes, tm_stream_t stream);
 
+/* ---------------------------------------------------------------- ragged --
+ * Ragged batches: n_items 2-D images of different sizes packed in one
+ * buffer (image i: heights[i] x widths[i] elements from element offsets[i],
+ * row-major).  Each operator is ONE persistent launch over the 128 x 32
+ * tiles of all images, taking tiles from a work queue in the plan; the
+ * result per image equals the uniform-batch operator on that image
+ * (tm_grey_erosion ... with batch 1, ndim 2), i.e. the reference's per-image
+ * calls of grey_erosion_cuda ... (torchmorph/csrc/torchmorph.cpp:3-33).
+ * No counterpart in the reference, which has no ragged batches.
+ *
+ * tm_ragged_plan writes the device descriptor table into `plan` (device,
+ * 256-byte aligned, tm_ragged_plan_size(n_items) bytes); one plan serves
+ * every operator and dtype on that layout, and may be reused across CUDA
+ * graph replays.  Operators sharing a plan must not run concurrently.
+ * Structures are 2-D, sizes 1..255 per axis; grey ops take the same
+ * structure/footprint/origin/mode/cval as tm_grey_erosion, binary ops a
+ * uint8 structure and border_value as tm_binary_erosion (one iteration). */
+size_t tm_ragged_plan_size(int64_t n_items);
+int tm_ragged_plan(int64_t n_items, const int64_t *heights, const int64_t *widths,
+                   const int64_t *offsets, void *plan, size_t plan_bytes, tm_stream_t stream);
+int tm_ragged_grey_erosion(const float *in, float *out, const void *plan, size_t plan_bytes,
+                           int64_t n_items, const float *structure, const uint8_t *footprint,
+                           const int64_t *sshape, const int64_t *origin, int mode, float cval,
+                           tm_stream_t stream);
+int tm_ragged_grey_dilation(const float *in, float *out, const void *plan, size_t plan_bytes,
+                            int64_t n_items, const float *structure, const uint8_t *footprint,
+                            const int64_t *sshape, const int64_t *origin, int mode, float cval,
+                            tm_stream_t stream);
+int tm_ragged_binary_erosion(const uint8_t *in, uint8_t *out, const void *plan, size_t plan_bytes,
+                             int64_t n_items, const uint8_t *structure, const int64_t *sshape,
+                             const int64_t *origin, int border_value, tm_stream_t stream);
+int tm_ragged_binary_dilation(const uint8_t *in, uint8_t *out, const void *plan, size_t plan_bytes,
+                              int64_t n_items, const uint8_t *structure, const int64_t *sshape,
+                              const int64_t *origin, int border_value, tm_stream_t stream);
+
 /* -------------------------------------------------------------- sinkhorn --
  * Replaces sinkhorn_fastiter (torchmorph/csrc/torchmorph.cpp:58-66,
  * torchmorph/csrc/ot_kernel.cu:188-233): n_iter scaling iterations

@@ -31,6 +31,8 @@ from .morphology import (
     white_tophat,
 )
 from .optimal_transport import SinkhornSolver, build_cost_matrix
+from . import ragged
+from .ragged import RaggedBatch
 
 __all__ = [
     "euclidean_distance_transform",
@@ -56,4 +58,6 @@ __all__ = [
     "black_tophat",
     "SinkhornSolver",
     "build_cost_matrix",
+    "ragged",
+    "RaggedBatch",
 ]

@@ -64,6 +64,16 @@ SIGNATURES = {
     "tm_sinkhorn_tc_iterate": (c_int, [c_i64, c_i64, c_i64, c_void, c_void, c_size, c_void]),
     "tm_sinkhorn_tc_finish": (c_int, [c_i64, c_i64, c_void, c_void, c_void, c_void, c_void, c_size,
                                       c_void]),
+    "tm_ragged_plan_size": (c_size, [c_i64]),
+    "tm_ragged_plan": (c_int, [c_i64, I64P, I64P, I64P, c_void, c_size, c_void]),
+    "tm_ragged_grey_erosion": (c_int, [c_void, c_void, c_void, c_size, c_i64, F32P, U8P, I64P, I64P,
+                                       c_int, c_float, c_void]),
+    "tm_ragged_grey_dilation": (c_int, [c_void, c_void, c_void, c_size, c_i64, F32P, U8P, I64P, I64P,
+                                        c_int, c_float, c_void]),
+    "tm_ragged_binary_erosion": (c_int, [c_void, c_void, c_void, c_size, c_i64, U8P, I64P, I64P, c_int,
+                                         c_void]),
+    "tm_ragged_binary_dilation": (c_int, [c_void, c_void, c_void, c_size, c_i64, U8P, I64P, I64P, c_int,
+                                          c_void]),
 }
 
 TM_F32 = 0
@@ -123,6 +133,16 @@ def i64_array(values):
 def f32_array(values):
     values = [float(v) for v in values]
     return (ctypes.c_float * max(1, len(values)))(*values)
+
+
+def ctypes_f32(t: torch.Tensor):
+    """float* view of a contiguous float32 CPU tensor (kept alive by the caller)."""
+    return ctypes.cast(t.data_ptr(), F32P)
+
+
+def ctypes_u8(t: torch.Tensor):
+    """uint8* view of a contiguous bool/uint8 CPU tensor (kept alive by the caller)."""
+    return ctypes.cast(t.data_ptr(), U8P)
 
 
 def ptr(t: torch.Tensor | None):
