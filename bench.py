@@ -336,7 +336,24 @@ def ragged_lines(dev, stream, steps, warmup):
     t_img = time_device(per_image, [None], 3, 1, stream) / 3
     hbm, _, kind = peaks()
     algo = 18.0 * npx  # 4+4 (erosion 5) + 4+4 (erosion 15) + 1+1 (binary opening) bytes per pixel
-    return {"ragged_256_images_erosion5_15_binary_opening": {
+    # opt-in backward of grey dilation (3x3, reflect) on an HBM-resident uniform batch
+    x = torch.rand((8, 1, 2048, 2048), device=dev)
+    st3 = torch.zeros((3, 3), dtype=torch.float32)
+    fp0 = torch.empty(0, dtype=torch.bool)
+    _, arg = _C.grey_dilation_arg(x, st3, fp0, [0, 0], 1, 0.0)
+    g = torch.randn_like(x)
+    t_fwd = time_device(lambda _: _C.grey_dilation_arg(x, st3, fp0, [0, 0], 1, 0.0), [None], steps,
+                        warmup, stream) / steps
+    t_bwd = time_device(lambda _: _C.grey_morphology_backward(g, arg, [3, 3], fp0, [0, 0], 1, True),
+                        [None], steps, warmup, stream) / steps
+    nb = x.numel()
+    backward = {"grey_dilation_3x3_backward_8x2048x2048": {
+        "forward_with_arg_us": round(t_fwd * 1e6, 1), "backward_us": round(t_bwd * 1e6, 1),
+        "forward_with_arg_GBps": round(9.0 * nb / t_fwd / 1e9, 1),
+        "backward_GBps": round(9.0 * nb / t_bwd / 1e9, 1),
+        "backward_frac_of_hbm": round(9.0 * nb / t_bwd / 1e9 / hbm, 4),
+        "bytes_per_pixel": "forward 4 in + 4 out + 1 arg; backward 4 grad_out + 1 arg + 4 grad_in"}}
+    return {**backward, "ragged_256_images_erosion5_15_binary_opening": {
         "pixels": npx, "ms_persistent_graph": round(t_graph * 1e3, 3),
         "ms_persistent_eager": round(t_eager * 1e3, 3), "ms_per_image_launches": round(t_img * 1e3, 3),
         "speedup_vs_per_image": round(t_img / t_graph, 2),

@@ -96,6 +96,32 @@ int tm_grey_dilation(const float *in, float *out, int64_t batch, int ndim,
                      const int64_t *sshape, const int64_t *origin, int mode, float cval,
                      tm_stream_t stream);
 
+/* Opt-in backward of grey erosion / dilation, 1-3 spatial dimensions, at
+ * most 255 active taps.  No counterpart in the reference (its operators are
+ * not differentiable, torchmorph/morphology/grey.py:92-100).
+ * *_arg: the forward (same arguments and output as tm_grey_erosion /
+ * tm_grey_dilation) that also writes arg[i] = index of the first active tap,
+ * in footprint raster order, attaining the extremum (255: none).
+ * *_backward: grad_in[j] = sum of grad_out[o] over the outputs o whose
+ * recorded tap reads j through the border mode (reads of the constant
+ * border route nothing); deterministic gather, no atomics. */
+int tm_grey_erosion_arg(const float *in, float *out, uint8_t *arg, int64_t batch, int ndim,
+                        const int64_t *shape, const float *structure, const uint8_t *footprint,
+                        const int64_t *sshape, const int64_t *origin, int mode, float cval,
+                        tm_stream_t stream);
+int tm_grey_dilation_arg(const float *in, float *out, uint8_t *arg, int64_t batch, int ndim,
+                         const int64_t *shape, const float *structure, const uint8_t *footprint,
+                         const int64_t *sshape, const int64_t *origin, int mode, float cval,
+                         tm_stream_t stream);
+int tm_grey_erosion_backward(const float *grad_out, const uint8_t *arg, float *grad_in,
+                             int64_t batch, int ndim, const int64_t *shape,
+                             const uint8_t *footprint, const int64_t *sshape,
+                             const int64_t *origin, int mode, tm_stream_t stream);
+int tm_grey_dilation_backward(const float *grad_out, const uint8_t *arg, float *grad_in,
+                              int64_t batch, int ndim, const int64_t *shape,
+                              const uint8_t *footprint, const int64_t *sshape,
+                              const int64_t *origin, int mode, tm_stream_t stream);
+
 /* ---------------------------------------------------------------- binary --
  * Replaces binary_erosion_cuda / binary_dilation_cuda
  * (torchmorph/csrc/torchmorph.cpp:21-33, torchmorph/csrc/binary_kernel.cu:252-272).

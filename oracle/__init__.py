@@ -199,3 +199,89 @@ def sinkhorn_cost(cost, log_u, log_v, eps, nthreads=0):
     _load().tmo_sinkhorn_cost(_ptr(c), _ptr(lu), _ptr(lv), n, d1, d2, float(eps), _ptr(dist),
                               _ptr(rm), _ptr(cm), nthreads)
     return dist, rm, cm
+
+
+# ------------------------------------------------ grey morphology gradient
+# numpy restatement (small cases): the forward with the first extremum tap
+# recorded, and the gradient routed to that tap's input voxel.  Taps follow
+# torchmorph/csrc/grey_kernel.cu:271-291 (erosion reads x + delta, dilation
+# x - delta, delta = k - (size // 2 + origin)); borders follow map_coord
+# (grey_kernel.cu:63-97).  There is no gradient in the reference; the tie
+# rule (first tap in footprint raster order) is the one the GB300 backward
+# documents.
+
+_MODES = {"constant": 0, "reflect": 1, "nearest": 2, "mirror": 3, "wrap": 4}
+
+
+def map_coords(c, n, mode):
+    """Border mapping of integer coordinates; -1 where the constant is used."""
+    c = np.asarray(c, dtype=np.int64)
+    if mode == "constant":
+        return np.where((c >= 0) & (c < n), c, -1)
+    if mode == "nearest":
+        return np.clip(c, 0, n - 1)
+    if mode == "reflect":
+        r = np.mod(c, 2 * n)
+        return np.where(r >= n, 2 * n - 1 - r, r)
+    if mode == "mirror":
+        if n == 1:
+            return np.zeros_like(c)
+        p = 2 * (n - 1)
+        r = np.mod(c, p)
+        return np.where(r >= n, p - r, r)
+    if mode == "wrap":
+        return np.mod(c, n)
+    raise ValueError(mode)
+
+
+def _grey_taps(structure, footprint, origin, dilation):
+    s = np.asarray(structure)
+    fp = np.ones(s.shape, bool) if footprint is None else np.asarray(footprint, bool)
+    origin = [0] * s.ndim if origin is None else list(origin)
+    taps = []
+    for k in np.ndindex(*s.shape):
+        if not fp[k]:
+            continue
+        delta = [k[d] - (s.shape[d] // 2 + origin[d]) for d in range(s.ndim)]
+        taps.append(([-v for v in delta] if dilation else delta, s[k]))
+    return taps
+
+
+def grey_arg(x, structure, footprint=None, origin=None, mode="reflect", cval=0.0, dilation=False):
+    """(out, arg) of grey erosion/dilation of a (B, C, *S) array in x's float dtype:
+    arg = index of the first active tap (raster order) attaining the extremum, 255 if none."""
+    x = np.asarray(x)
+    dt = x.dtype
+    shape = x.shape[2:]
+    grids = np.meshgrid(*[np.arange(n) for n in shape], indexing="ij")
+    best = np.full(x.shape, -np.inf if dilation else np.inf, dt)
+    arg = np.full(x.shape, 255, np.uint8)
+    for t, (off, val) in enumerate(_grey_taps(structure, footprint, origin, dilation)):
+        idx = [map_coords(g + o, n, mode) for g, o, n in zip(grids, off, shape)]
+        valid = np.logical_and.reduce([i >= 0 for i in idx])
+        safe = tuple(np.where(valid, i, 0) for i in idx)
+        v = np.where(valid, x[(slice(None), slice(None)) + safe], dt.type(cval)).astype(dt)
+        v = (v + dt.type(val)) if dilation else (v - dt.type(val))
+        better = (v > best) if dilation else (v < best)
+        best = np.where(better, v, best)
+        arg = np.where(better, np.uint8(t), arg)
+    return best, arg
+
+
+def grey_backward(grad_out, arg, structure_shape, footprint=None, origin=None, mode="reflect",
+                  dilation=False):
+    """float64 input gradient: each output's gradient added to the voxel its recorded tap read."""
+    g = np.asarray(grad_out, np.float64)
+    shape = g.shape[2:]
+    gin = np.zeros_like(g)
+    grids = np.meshgrid(*[np.arange(n) for n in shape], indexing="ij")
+    taps = _grey_taps(np.zeros(structure_shape), footprint, origin, dilation)
+    b_idx, c_idx = np.meshgrid(np.arange(g.shape[0]), np.arange(g.shape[1]), indexing="ij")
+    for t, (off, _) in enumerate(taps):
+        idx = [map_coords(gr + o, n, mode) for gr, o, n in zip(grids, off, shape)]
+        valid = np.logical_and.reduce([i >= 0 for i in idx])
+        sel = (arg == t) & valid[None, None]
+        bb, cc, *pos = np.nonzero(sel)
+        tgt = tuple(idx[d][tuple(pos)] for d in range(len(shape)))
+        np.add.at(gin, (bb, cc) + tgt, g[sel])
+    return gin

@@ -83,6 +83,54 @@ def grey_dilation_cuda(input, structure, footprint, origin, mode, cval):
     return _grey("tm_grey_dilation", input, structure, footprint, origin, mode, cval)
 
 
+def _grey_arg(fn_name, input, structure, footprint, origin, mode, cval):
+    """(output, argument) of the forward with the first extremum tap recorded per output."""
+    _require(input.is_cuda and input.is_contiguous() and input.dtype == torch.float32,
+             "input must be a contiguous float32 CUDA tensor")
+    nd = structure.dim()
+    _require(len(origin) == nd and input.dim() == nd + 2, "structure/origin/input dimensions disagree")
+    use_fp = footprint.numel() != 0
+    batch, shape = _batch_shape(input)
+    out = torch.empty_like(input)
+    arg = torch.empty(input.shape, dtype=torch.uint8, device=input.device)
+    lib = _lib.load()
+    with torch.cuda.device(input.device):
+        st = getattr(lib, fn_name)(
+            _lib.ptr(input), _lib.ptr(out), _lib.ptr(arg), batch, nd, _lib.i64_array(shape),
+            _host_f32(structure), _host_u8(footprint) if use_fp else None,
+            _lib.i64_array(structure.shape), _lib.i64_array(origin), int(mode), float(cval),
+            _lib.stream_of(input.device))
+    _lib.check(st, fn_name)
+    return out, arg
+
+
+def grey_erosion_arg(input, structure, footprint, origin, mode, cval):
+    return _grey_arg("tm_grey_erosion_arg", input, structure, footprint, origin, mode, cval)
+
+
+def grey_dilation_arg(input, structure, footprint, origin, mode, cval):
+    return _grey_arg("tm_grey_dilation_arg", input, structure, footprint, origin, mode, cval)
+
+
+def grey_morphology_backward(grad_output, arg, sshape, footprint, origin, mode, dilation):
+    """grad_input of grey erosion/dilation from grad_output and the recorded argument."""
+    g = grad_output.contiguous().float()
+    _require(g.is_cuda and arg.is_cuda and arg.shape == g.shape, "grad_output/argument mismatch")
+    nd = len(sshape)
+    batch, shape = _batch_shape(g)
+    gin = torch.empty_like(g)
+    use_fp = footprint.numel() != 0
+    name = "tm_grey_dilation_backward" if dilation else "tm_grey_erosion_backward"
+    lib = _lib.load()
+    with torch.cuda.device(g.device):
+        st = getattr(lib, name)(
+            _lib.ptr(g), _lib.ptr(arg), _lib.ptr(gin), batch, nd, _lib.i64_array(shape),
+            _host_u8(footprint) if use_fp else None, _lib.i64_array(sshape), _lib.i64_array(origin),
+            int(mode), _lib.stream_of(g.device))
+    _lib.check(st, name)
+    return gin
+
+
 # ----------------------------------------------------------------- binary
 def _binary(fn_name, input, structure, origin, border_value, out=None):
     _require(input.is_cuda, "input must be a CUDA tensor")

@@ -84,10 +84,16 @@ def _grey_morphology(
     origin=0,
     *,
     operation: str,
+    differentiable: bool = False,
 ) -> Tensor:
     validate_bcs_input(input)
     validate_output(input, output)
     struct, fp, o, m = _prepare(input, size, footprint, structure, mode, origin)
+    if differentiable and input.requires_grad and torch.is_grad_enabled():
+        result = _GreyMorphologyFunction.apply(input, struct, fp, o, m, cval, operation == "dilation")
+        if output is not None:
+            raise ValueError("output= is not supported for a differentiable call")
+        return result
     kernel = _C.grey_erosion_cuda if operation == "erosion" else _C.grey_dilation_cuda
     result = kernel(input.detach().contiguous().float(), struct, fp, o, m, cval)
     if output is not None:
@@ -96,32 +102,61 @@ def _grey_morphology(
     return result
 
 
+class _GreyMorphologyFunction(torch.autograd.Function):
+    """Grey erosion/dilation with a hand-written backward: the forward records, per
+    output, the first footprint tap attaining the extremum; the backward gathers each
+    input's gradient from the outputs whose recorded tap reads it."""
+
+    @staticmethod
+    def forward(ctx, input, struct, fp, origin, mode, cval, dilation):
+        kernel = _C.grey_dilation_arg if dilation else _C.grey_erosion_arg
+        out, arg = kernel(input.detach().contiguous().float(), struct, fp, origin, mode, cval)
+        ctx.save_for_backward(arg)
+        ctx.meta = (list(struct.shape), fp, origin, mode, dilation, input.dtype)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_output):
+        (arg,) = ctx.saved_tensors
+        sshape, fp, origin, mode, dilation, dtype = ctx.meta
+        grad = _C.grey_morphology_backward(grad_output, arg, sshape, fp, origin, mode, dilation)
+        return grad.to(dtype), None, None, None, None, None, None
+
+
 def grey_erosion(input, size=None, footprint=None, structure=None, output=None, mode="reflect",
-                 cval=0.0, origin=0) -> Tensor:
-    """N-dimensional grey erosion of a (B, C, *spatial) CUDA tensor, computed in float32."""
+                 cval=0.0, origin=0, *, differentiable=False) -> Tensor:
+    """N-dimensional grey erosion of a (B, C, *spatial) CUDA tensor, computed in float32.
+
+    ``differentiable=True`` (opt-in; 1-3 spatial dims, <= 255 footprint taps) makes the
+    result track gradients w.r.t. ``input`` when it requires grad: the gradient of each
+    output goes to the input voxel its first minimising tap read."""
     return _grey_morphology(input, size, footprint, structure, output, mode, cval, origin,
-                            operation="erosion")
+                            operation="erosion", differentiable=differentiable)
 
 
 def grey_dilation(input, size=None, footprint=None, structure=None, output=None, mode="reflect",
-                  cval=0.0, origin=0) -> Tensor:
-    """N-dimensional grey dilation of a (B, C, *spatial) CUDA tensor, computed in float32."""
+                  cval=0.0, origin=0, *, differentiable=False) -> Tensor:
+    """N-dimensional grey dilation of a (B, C, *spatial) CUDA tensor, computed in float32.
+
+    ``differentiable=True``: see :func:`grey_erosion` (first maximising tap)."""
     return _grey_morphology(input, size, footprint, structure, output, mode, cval, origin,
-                            operation="dilation")
+                            operation="dilation", differentiable=differentiable)
 
 
 def grey_opening(input, size=None, footprint=None, structure=None, output=None, mode="reflect",
-                 cval=0.0, origin=0) -> Tensor:
+                 cval=0.0, origin=0, *, differentiable=False) -> Tensor:
     """Grey opening: dilation of the erosion."""
     kw = _element_kwargs(size, footprint, structure, mode, cval, origin)
-    return grey_dilation(grey_erosion(input, **kw), output=output, **kw)
+    return grey_dilation(grey_erosion(input, differentiable=differentiable, **kw), output=output,
+                         differentiable=differentiable, **kw)
 
 
 def grey_closing(input, size=None, footprint=None, structure=None, output=None, mode="reflect",
-                 cval=0.0, origin=0) -> Tensor:
+                 cval=0.0, origin=0, *, differentiable=False) -> Tensor:
     """Grey closing: erosion of the dilation."""
     kw = _element_kwargs(size, footprint, structure, mode, cval, origin)
-    return grey_erosion(grey_dilation(input, **kw), output=output, **kw)
+    return grey_erosion(grey_dilation(input, differentiable=differentiable, **kw), output=output,
+                        differentiable=differentiable, **kw)
 
 
 def _finish(result, output):
@@ -132,12 +167,13 @@ def _finish(result, output):
 
 
 def morphological_gradient(input, size=None, footprint=None, structure=None, output=None,
-                           mode="reflect", cval=0.0, origin=0) -> Tensor:
+                           mode="reflect", cval=0.0, origin=0, *, differentiable=False) -> Tensor:
     """Dilation minus erosion."""
     validate_bcs_input(input)
     validate_output(input, output)
     kw = _element_kwargs(size, footprint, structure, mode, cval, origin)
-    return _finish(grey_dilation(input, **kw) - grey_erosion(input, **kw), output)
+    return _finish(grey_dilation(input, differentiable=differentiable, **kw)
+                   - grey_erosion(input, differentiable=differentiable, **kw), output)
 
 
 def white_tophat(input, size=None, footprint=None, structure=None, output=None, mode="reflect",
