@@ -268,6 +268,39 @@ int tm_sinkhorn_tc_finish(int64_t n, int64_t d, float *log_u, float *log_v, doub
                           double *row_err, void *workspace, size_t workspace_bytes,
                           tm_stream_t stream);
 
+/* ----------------------------------------------- sinkhorn, point clouds --
+ * Ragged batch of OT problems between point clouds in R^3 with the
+ * squared-Euclidean cost recomputed from the points: problem p has n[p]
+ * source points (x, packed (sum n, 3) fp32) and m[p] target points (y),
+ * log weights log_a / log_b (packed like the points).  Log-domain Sinkhorn
+ * (the iteration of torchmorph/optimal_transport.py:96-125 without a cost
+ * matrix) for all problems in ONE cooperative persistent launch; a problem
+ * stops once the L1 column-marginal error of its plan is <= threshold
+ * (checked every check_every iterations) or after max_iter iterations.
+ * Outputs: potentials f (sum n), g (sum m) (fp32, the reference's
+ * epsilon * log u / log v), cost[p] = <f, a> + <g, b> (the regularised
+ * cost, fp64) and iterations[p] (both optional).  The workspace
+ * (tm_pointcloud_sinkhorn_workspace_size bytes, 256-byte aligned) is
+ * scratch.  No counterpart in the reference (no ragged OT API).
+ *
+ * tm_pointcloud_sinkhorn_grad: gradient of the regularised cost w.r.t. the
+ * points (envelope theorem: d cost_p / d x_i = 2 sum_j P_ij (x_i - y_j),
+ * plan entries recomputed from f, g), scaled by grad_cost[p] (device fp32);
+ * grad_x / grad_y may be NULL; the workspace holds n_problems * 32 bytes. */
+size_t tm_pointcloud_sinkhorn_workspace_size(int64_t n_problems, int64_t max_iter);
+int tm_pointcloud_sinkhorn(const float *x, const float *y, const float *log_a,
+                           const float *log_b, int64_t n_problems, const int64_t *n,
+                           const int64_t *m, double epsilon, int64_t max_iter, double threshold,
+                           int64_t check_every, float *f, float *g, double *cost,
+                           int32_t *iterations, void *workspace, size_t workspace_bytes,
+                           tm_stream_t stream);
+int tm_pointcloud_sinkhorn_grad(const float *x, const float *y, const float *log_a,
+                                const float *log_b, const float *f, const float *g,
+                                int64_t n_problems, const int64_t *n, const int64_t *m,
+                                double epsilon, const float *grad_cost, float *grad_x,
+                                float *grad_y, void *workspace, size_t workspace_bytes,
+                                tm_stream_t stream);
+
 /* Error-compensated BF16 tensor-core product D = A B^T in fp32, with
  * A = a_hi + a_lo (M x K) and B = b_hi + b_lo (N x K), all bf16 row-major
  * device arrays, D fp32 M x N row-major: three tcgen05 MMAs per k-step

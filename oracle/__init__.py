@@ -285,3 +285,39 @@ def grey_backward(grad_out, arg, structure_shape, footprint=None, origin=None, m
         tgt = tuple(idx[d][tuple(pos)] for d in range(len(shape)))
         np.add.at(gin, (bb, cc) + tgt, g[sel])
     return gin
+
+
+# ------------------------------------------------- point-cloud Sinkhorn
+def _lse(z, axis):
+    m = np.max(z, axis=axis, keepdims=True)
+    m = np.where(np.isfinite(m), m, 0.0)
+    return np.squeeze(m, axis) + np.log(np.sum(np.exp(z - m), axis=axis))
+
+
+def pointcloud_sinkhorn(x, y, eps, max_iter, threshold=0.0, check_every=10, log_a=None, log_b=None):
+    """float64 log-domain Sinkhorn between two point clouds (squared-Euclidean cost):
+    the reference's _log_iterations (optimal_transport.py:96-125) in dual-potential form,
+    f = eps (log_u - log a), g = eps (log_v - log b), started from the reference's
+    log_u = log_v = 0.  Stops after the first multiple of `check_every` iterations whose
+    g-update moved the column marginals of (f, g_old) by an L1 of <= threshold.
+    Returns (f, g, iterations, regularised cost <f, a> + <g, b>)."""
+    x = np.asarray(x, np.float64)
+    y = np.asarray(y, np.float64)
+    n, m = len(x), len(y)
+    la = np.full(n, -np.log(n)) if log_a is None else np.asarray(log_a, np.float64)
+    lb = np.full(m, -np.log(m)) if log_b is None else np.asarray(log_b, np.float64)
+    C = ((x[:, None] - y[None]) ** 2).sum(-1)
+    f = -eps * la
+    g = -eps * lb
+    it = 0
+    while it < max_iter:
+        f = -eps * _lse((g[None] - C) / eps + lb[None], 1)
+        g_new = -eps * _lse((f[:, None] - C) / eps + la[:, None], 0)
+        it += 1
+        check = it % check_every == 0 or it == max_iter
+        err = np.sum(np.exp(lb) * np.abs(np.expm1((g - g_new) / eps))) if check else None
+        g = g_new
+        if check and threshold > 0 and err <= threshold:
+            break
+    cost = np.sum(np.exp(la) * f) + np.sum(np.exp(lb) * g)
+    return f, g, it, cost

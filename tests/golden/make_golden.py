@@ -161,6 +161,33 @@ def sinkhorn_cases(out, ref_root):
             out[key + "_dist"] = solver(src, tgt).detach().numpy()
 
 
+def pointcloud_cases(out, ref_root):
+    """Log-domain iterations of the reference (optimal_transport.py:96-125) on rectangular
+    squared-Euclidean costs between point clouds, float64, fixed iteration counts."""
+    path = os.path.join(ref_root, "torchmorph", "optimal_transport.py")
+    spec = importlib.util.spec_from_file_location("ref_optimal_transport_pc", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    import torch
+
+    rng = np.random.default_rng(77)
+    for n, m, eps, iters in [(7, 11, 0.5, 40), (20, 13, 0.1, 60), (5, 5, 0.05, 80)]:
+        means = rng.uniform(-1, 1, (4, 3))
+        x = means[rng.integers(0, 4, n)] + 0.2 * rng.standard_normal((n, 3))
+        y = means[rng.integers(0, 4, m)] + 0.2 * rng.standard_normal((m, 3))
+        cost = ((x[:, None] - y[None]) ** 2).sum(-1)
+        a = torch.full((1, n), 1.0 / n, dtype=torch.float64)
+        b = torch.full((1, m), 1.0 / m, dtype=torch.float64)
+        log_u, log_v = mod._log_iterations(a, b, torch.from_numpy(cost), eps, iters, 0.0)
+        key = f"pc_{n}x{m}"
+        out[key + "_x"] = x
+        out[key + "_y"] = y
+        out[key + "_eps"] = np.array(eps)
+        out[key + "_iters"] = np.array(iters)
+        out[key + "_log_u"] = log_u.numpy()[0]
+        out[key + "_log_v"] = log_v.numpy()[0]
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     out = {}
@@ -168,6 +195,7 @@ def main():
     binary_cases(out)
     distance_cases(out)
     sinkhorn_cases(out, ref_root)
+    pointcloud_cases(out, ref_root)
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print(f"wrote {len(out)} arrays")
 

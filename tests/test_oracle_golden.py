@@ -113,3 +113,14 @@ def test_chamfer345_matches_closed_form():
         diff = np.abs(bg - np.array(p))
         exp[p] = (diff.sum(1) + 2 * diff.max(1)).min()
     np.testing.assert_array_equal(d[0, 0], exp)
+
+
+@pytest.mark.parametrize("nm", ["7x11", "20x13", "5x5"])
+def test_pointcloud_sinkhorn_vs_reference_log_iterations(nm):
+    key = f"pc_{nm}"
+    x, y, eps, iters = G[key + "_x"], G[key + "_y"], float(G[key + "_eps"]), int(G[key + "_iters"])
+    f, g, its, _ = oracle.pointcloud_sinkhorn(x, y, eps, iters)
+    assert its == iters
+    n, m = len(x), len(y)
+    np.testing.assert_allclose(f / eps - np.log(n), G[key + "_log_u"], rtol=1e-10, atol=1e-10)
+    np.testing.assert_allclose(g / eps - np.log(m), G[key + "_log_v"], rtol=1e-10, atol=1e-10)

@@ -32,6 +32,7 @@ from .morphology import (
 )
 from .optimal_transport import SinkhornSolver, build_cost_matrix
 from . import ragged
+from .pointcloud_ot import PointCloudSinkhorn, pack_clouds
 from .ragged import RaggedBatch
 
 __all__ = [
@@ -60,4 +61,6 @@ __all__ = [
     "build_cost_matrix",
     "ragged",
     "RaggedBatch",
+    "PointCloudSinkhorn",
+    "pack_clouds",
 ]

@@ -1,0 +1,534 @@
+// Ragged point-cloud Sinkhorn: many OT problems of uneven sizes (n_p source
+// and m_p target points in R^3, squared-Euclidean cost) solved together in
+// ONE cooperative persistent launch, and the gradient of the regularised
+// cost w.r.t. the points.
+//
+// Per problem, log-domain Sinkhorn iterations (the form of
+// torchmorph/optimal_transport.py:96-125, with the cost recomputed from the
+// points instead of read from a matrix):
+//
+//   f_i = -eps LSE_j( (g_j - C_ij)/eps + log b_j ),
+//   g_j = -eps LSE_i( (f_i - C_ij)/eps + log a_i ),   C_ij = |x_i - y_j|^2.
+//
+// Work: the rows of all problems form 128-row tiles (the f-update), the
+// columns 128-column tiles (the g-update).  The persistent CTAs take tiles
+// from one queue per phase; a grid barrier separates the phases.  Inside a
+// tile each row keeps an online log-sum-exp in base 2 (one ex2 per pair)
+// over target points staged in shared memory 256 at a time.
+//
+// Potentials use the dual form f = eps (log u - log a), g = eps (log v -
+// log b) of the reference's log_u / log_v and start where log_u = log_v = 0.
+//
+// Stopping: on check iterations the g-update also accumulates, per problem,
+// sum_j b_j |exp((g_old_j - g_new_j)/eps) - 1|, the L1 column-marginal
+// error of the plan (f, g_old) whose rows the f-update just made exact;
+// problems at or below the threshold stop and their tiles are skipped
+// (threshold <= 0: every problem runs max_iter iterations, as the
+// reference's threshold = 0).
+//
+// Every wait in the grid barrier is bounded; a barrier that gives up sets
+// the library's device status word and an abort flag that makes every CTA
+// leave.  The launch is cooperative, so all CTAs are co-resident.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "tm_common.cuh"
+#include "tm_tma.cuh"
+
+namespace tmc {
+namespace {
+
+constexpr int kPcThreads = 256;
+constexpr int kPcTile = 128;   // rows (or columns) per tile
+constexpr int kPcChunk = 256;  // partner points staged per pass
+constexpr float kLog2e = 1.4426950408889634f;
+constexpr float kLn2 = 0.6931471805599453f;
+
+struct PcProblem {
+    int64_t x0, y0;  // first source / target point (packed arrays)
+    int n, m;
+    int row_tile0, col_tile0;  // first row tile / column tile of the problem
+};
+
+struct PcControl {
+    unsigned barrier_count;
+    unsigned barrier_gen;
+    int n_active;
+    int abort;
+    int iterations;  // iterations run (all problems)
+    int pad[59];
+};
+static_assert(sizeof(PcControl) == 256, "control block is 256 bytes");
+
+struct PcArgs {
+    const float *x, *y;    // (Nx, 3), (Ny, 3)
+    const float *la, *lb;  // log weights (Nx), (Ny)
+    float *f, *g;          // potentials (Nx), (Ny)
+    const PcProblem *prob;
+    int nprob, row_tiles, col_tiles;
+    float *err;       // per problem: marginal error being accumulated
+    int *active;      // per problem: 1 while iterating
+    int *iters;       // per problem: iterations when it stopped
+    int *queue;       // 2 * max_iter tile counters
+    PcControl *ctl;
+    int *status;
+    float eps, threshold;
+    int max_iter, check_every;
+};
+
+// Bounded grid barrier (sense by generation).  Returns false when it gave up
+// or another CTA aborted.
+__device__ bool grid_barrier(PcControl *ctl, unsigned nblocks, int *status) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = &ctl->barrier_gen;
+        volatile int *abort = &ctl->abort;
+        const unsigned g = *gen;
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(&ctl->barrier_count, 1u) == nblocks - 1) {
+            ctl->barrier_count = 0;
+            __threadfence();
+            atomicAdd(&ctl->barrier_gen, 1u);
+        } else {
+            long long polls = 0;
+            while (*gen == g) {
+                if (*abort || ++polls > kSpinLimit) {
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        if (!ok) {
+            atomicExch(&ctl->abort, 1);
+            if (status) atomicExch(status, TM_DEV_ERR_TIMEOUT);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+__device__ __forceinline__ int find_problem(const PcProblem *prob, int nprob, int tile, bool rows) {
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((rows ? prob[mid].row_tile0 : prob[mid].col_tile0) <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// One tile of one half-iteration.  "Own" side: the 128 points being updated
+// (rows for the f-update); "other" side: all points of the partner cloud.
+// Thread t handles own point t % 128 and partner points of parity t / 128.
+__device__ void update_tile(const float *own_pts, const float *other_pts, const float *other_pot,
+                            const float *other_lw, float *own_pot, int own0, int n_own, int n_other, float eps,
+                            float *err_acc, const float *own_lw, float *s_buf) {
+    float *sy = s_buf;                 // [kPcChunk][3]
+    float *sw = s_buf + 3 * kPcChunk;  // [kPcChunk]
+    float *sm = sw + kPcChunk;         // [kPcThreads] partial maxima
+    float *ss = sm + kPcThreads;       // [kPcThreads] partial sums
+    const int r = threadIdx.x % kPcTile, half = threadIdx.x / kPcTile;
+    const int i = own0 + r;
+    const bool valid = i < n_own;
+    float px = 0.f, py = 0.f, pz = 0.f;
+    if (valid) {
+        px = own_pts[3 * i];
+        py = own_pts[3 * i + 1];
+        pz = own_pts[3 * i + 2];
+    }
+    const float k = kLog2e / eps;
+    float mx = -INFINITY, sum = 0.f;
+    for (int j0 = 0; j0 < n_other; j0 += kPcChunk) {
+        const int cnt = min(kPcChunk, n_other - j0);
+        for (int t = threadIdx.x; t < cnt; t += kPcThreads) {
+            const int j = j0 + t;
+            sy[3 * t] = other_pts[3 * j];
+            sy[3 * t + 1] = other_pts[3 * j + 1];
+            sy[3 * t + 2] = other_pts[3 * j + 2];
+            // log2 of exp(pot / eps) * weight
+            sw[t] = (other_pot[j] / eps + other_lw[j]) * kLog2e;
+        }
+        __syncthreads();
+        if (valid) {
+            for (int t0 = half * 8; t0 < cnt; t0 += 16) {
+                float z[8];
+                float bm = -INFINITY;
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    const int t = t0 + q;
+                    if (t < cnt) {
+                        const float dx = px - sy[3 * t], dy = py - sy[3 * t + 1], dz = pz - sy[3 * t + 2];
+                        const float c = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        z[q] = fmaf(-k, c, sw[t]);
+                    } else {
+                        z[q] = -INFINITY;
+                    }
+                    bm = fmaxf(bm, z[q]);
+                }
+                if (bm > mx) {
+                    sum = (mx == -INFINITY) ? 0.f : sum * exp2f(mx - bm);
+                    mx = bm;
+                }
+                if (mx != -INFINITY) {
+#pragma unroll
+                    for (int q = 0; q < 8; q++) sum += exp2f(z[q] - mx);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    sm[threadIdx.x] = mx;
+    ss[threadIdx.x] = sum;
+    __syncthreads();
+    if (half == 0 && valid) {
+        const float m1 = sm[r + kPcTile], s1 = ss[r + kPcTile];
+        float m = fmaxf(mx, m1), s = 0.f;
+        if (m != -INFINITY) s = sum * exp2f(mx - m) + s1 * exp2f(m1 - m);
+        // pot = -eps * ln(sum 2^z) = -eps ln2 (m + log2 s)
+        const float pot = (m == -INFINITY) ? INFINITY : -eps * kLn2 * (m + log2f(s));
+        if (err_acc) {
+            const float d = (own_pot[i] - pot) / eps;
+            *err_acc += expf(own_lw[i]) * fabsf(expm1f(d));
+        }
+        own_pot[i] = pot;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kPcThreads) pc_sinkhorn_kernel(PcArgs a) {
+    __shared__ float s_buf[4 * kPcChunk + 2 * kPcThreads];
+    __shared__ int s_tile;
+    __shared__ float s_err;
+    const unsigned nblocks = gridDim.x;
+    int it = 0;
+    for (; it < a.max_iter; it++) {
+        // f-update over the row tiles of the active problems
+        for (;;) {
+            if (threadIdx.x == 0) s_tile = atomicAdd(&a.queue[2 * it], 1);
+            __syncthreads();
+            const int tile = s_tile;
+            __syncthreads();
+            if (tile >= a.row_tiles) break;
+            const int p = find_problem(a.prob, a.nprob, tile, true);
+            if (!a.active[p]) continue;
+            const PcProblem P = a.prob[p];
+            update_tile(a.x + 3 * P.x0, a.y + 3 * P.y0, a.g + P.y0, a.lb + P.y0, a.f + P.x0,
+                        (tile - P.row_tile0) * kPcTile, P.n, P.m, a.eps, nullptr, nullptr, s_buf);
+        }
+        if (!grid_barrier(a.ctl, nblocks, a.status)) return;
+        const bool check = ((it + 1) % a.check_every == 0) || it + 1 == a.max_iter;
+        // g-update over the column tiles (+ the column-marginal error on check iterations)
+        for (;;) {
+            if (threadIdx.x == 0) {
+                s_tile = atomicAdd(&a.queue[2 * it + 1], 1);
+                s_err = 0.f;
+            }
+            __syncthreads();
+            const int tile = s_tile;
+            __syncthreads();
+            if (tile >= a.col_tiles) break;
+            const int p = find_problem(a.prob, a.nprob, tile, false);
+            if (!a.active[p]) continue;
+            const PcProblem P = a.prob[p];
+            float e = 0.f;
+            update_tile(a.y + 3 * P.y0, a.x + 3 * P.x0, a.f + P.x0, a.la + P.x0, a.g + P.y0,
+                        (tile - P.col_tile0) * kPcTile, P.m, P.n, a.eps, check ? &e : nullptr, a.lb + P.y0, s_buf);
+            if (check) {
+                for (int o = 16; o; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+                if ((threadIdx.x & 31) == 0 && e != 0.f) atomicAdd(&s_err, e);
+                __syncthreads();
+                if (threadIdx.x == 0) atomicAdd(&a.err[p], s_err);
+            }
+        }
+        if (!grid_barrier(a.ctl, nblocks, a.status)) return;
+        if (check) {
+            if (blockIdx.x == 0) {
+                for (int p = threadIdx.x; p < a.nprob; p += kPcThreads) {
+                    if (a.active[p] && ((a.threshold > 0.f && a.err[p] <= a.threshold) || it + 1 == a.max_iter)) {
+                        a.active[p] = 0;
+                        a.iters[p] = it + 1;
+                        atomicSub(&a.ctl->n_active, 1);
+                    }
+                    a.err[p] = 0.f;
+                }
+            }
+            if (!grid_barrier(a.ctl, nblocks, a.status)) return;
+            if (*(volatile int *)&a.ctl->n_active <= 0) {
+                it++;
+                break;
+            }
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.ctl->iterations = it;
+}
+
+// Start of the reference's iteration, log_u = log_v = 0, in dual-potential
+// form: f = -eps log a, g = -eps log b.
+__global__ void pc_init_kernel(const float *lw, float *pot, int64_t count, float eps) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+        pot[i] = -eps * lw[i];
+}
+
+// Regularised cost per problem: sum_i a_i f_i + sum_j b_j g_j (fp64 sums).
+__global__ void __launch_bounds__(kPcThreads) pc_cost_kernel(const float *f, const float *g, const float *la,
+                                                             const float *lb, const PcProblem *prob, double *cost) {
+    __shared__ double red[kPcThreads / 32];
+    const PcProblem P = prob[blockIdx.x];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < P.n; i += kPcThreads) s += exp((double)la[P.x0 + i]) * f[P.x0 + i];
+    for (int j = threadIdx.x; j < P.m; j += kPcThreads) s += exp((double)lb[P.y0 + j]) * g[P.y0 + j];
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < kPcThreads / 32; w++) t += red[w];
+        cost[blockIdx.x] = t;
+    }
+}
+
+// Gradient of the regularised cost w.r.t. one cloud (envelope theorem):
+// d/dp_i = scale_p * 2 sum_j P_ij (p_i - q_j), P_ij = exp((f_i + g_j - C_ij)/eps
+// + log a_i + log b_j) recomputed per pair.  One 128-point tile per CTA
+// iteration, partner points staged in shared memory.
+__global__ void __launch_bounds__(kPcThreads) pc_grad_kernel(const float *own_pts, const float *other_pts,
+                                                             const float *own_pot, const float *other_pot,
+                                                             const float *own_lw, const float *other_lw,
+                                                             const PcProblem *prob, int nprob, int tiles, bool rows,
+                                                             float eps, const float *scale, float *grad) {
+    __shared__ float sy[kPcChunk * 3];
+    __shared__ float sw[kPcChunk];
+    __shared__ float sacc[kPcThreads * 3];
+    const float k = kLog2e / eps;
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int p = find_problem(prob, nprob, tile, rows);
+        const PcProblem P = prob[p];
+        const int64_t o0 = rows ? P.x0 : P.y0, q0 = rows ? P.y0 : P.x0;
+        const int n_own = rows ? P.n : P.m, n_other = rows ? P.m : P.n;
+        const int r = threadIdx.x % kPcTile, half = threadIdx.x / kPcTile;
+        const int i = (tile - (rows ? P.row_tile0 : P.col_tile0)) * kPcTile + r;
+        const bool valid = i < n_own;
+        float px = 0.f, py = 0.f, pz = 0.f, base = 0.f;
+        if (valid) {
+            px = own_pts[3 * (o0 + i)];
+            py = own_pts[3 * (o0 + i) + 1];
+            pz = own_pts[3 * (o0 + i) + 2];
+            base = (own_pot[o0 + i] / eps + own_lw[o0 + i]) * kLog2e;
+        }
+        float ax = 0.f, ay = 0.f, az = 0.f;
+        for (int j0 = 0; j0 < n_other; j0 += kPcChunk) {
+            const int cnt = min(kPcChunk, n_other - j0);
+            for (int t = threadIdx.x; t < cnt; t += kPcThreads) {
+                const int64_t j = q0 + j0 + t;
+                sy[3 * t] = other_pts[3 * j];
+                sy[3 * t + 1] = other_pts[3 * j + 1];
+                sy[3 * t + 2] = other_pts[3 * j + 2];
+                sw[t] = (other_pot[j] / eps + other_lw[j]) * kLog2e;
+            }
+            __syncthreads();
+            if (valid) {
+                for (int t = half; t < cnt; t += 2) {
+                    const float dx = px - sy[3 * t], dy = py - sy[3 * t + 1], dz = pz - sy[3 * t + 2];
+                    const float c = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    const float pij = exp2f(fmaf(-k, c, base + sw[t]));
+                    ax = fmaf(pij, dx, ax);
+                    ay = fmaf(pij, dy, ay);
+                    az = fmaf(pij, dz, az);
+                }
+            }
+            __syncthreads();
+        }
+        sacc[3 * threadIdx.x] = ax;
+        sacc[3 * threadIdx.x + 1] = ay;
+        sacc[3 * threadIdx.x + 2] = az;
+        __syncthreads();
+        if (half == 0 && valid) {
+            const float sc = 2.f * scale[p];
+            const int u = threadIdx.x + kPcTile;
+            grad[3 * (o0 + i)] = sc * (ax + sacc[3 * u]);
+            grad[3 * (o0 + i) + 1] = sc * (ay + sacc[3 * u + 1]);
+            grad[3 * (o0 + i) + 2] = sc * (az + sacc[3 * u + 2]);
+        }
+        __syncthreads();
+    }
+}
+
+struct PcLayout {
+    size_t prob, err, active, iters, queue, ctl, total;
+};
+
+PcLayout pc_layout(int64_t nprob, int64_t max_iter) {
+    PcLayout L{};
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = off;
+        off += (bytes + 255) / 256 * 256;
+        return at;
+    };
+    L.ctl = take(sizeof(PcControl));
+    L.prob = take((size_t)nprob * sizeof(PcProblem));
+    L.err = take((size_t)nprob * 4);
+    L.active = take((size_t)nprob * 4);
+    L.iters = take((size_t)nprob * 4);
+    L.queue = take((size_t)max_iter * 2 * 4);
+    L.total = off;
+    return L;
+}
+
+template <typename T>
+T *ws_at(void *ws, size_t off) {
+    return reinterpret_cast<T *>(static_cast<unsigned char *>(ws) + off);
+}
+
+int build_problems(int64_t nprob, const int64_t *n, const int64_t *m, std::vector<PcProblem> &out, int *row_tiles,
+                   int *col_tiles, int64_t *nx, int64_t *ny) {
+    out.resize(nprob);
+    int64_t x0 = 0, y0 = 0, rt = 0, ct = 0;
+    for (int64_t p = 0; p < nprob; p++) {
+        if (n[p] < 1 || m[p] < 1) return fail(TM_ERR_INVALID_ARGUMENT, "problem %lld has an empty cloud", (long long)p);
+        if (n[p] > (1 << 24) || m[p] > (1 << 24)) return fail(TM_ERR_TOO_LARGE, "clouds are limited to 2^24 points");
+        out[p].x0 = x0;
+        out[p].y0 = y0;
+        out[p].n = (int)n[p];
+        out[p].m = (int)m[p];
+        out[p].row_tile0 = (int)rt;
+        out[p].col_tile0 = (int)ct;
+        x0 += n[p];
+        y0 += m[p];
+        rt += ceil_div(n[p], kPcTile);
+        ct += ceil_div(m[p], kPcTile);
+        if (rt >= (1 << 30) || ct >= (1 << 30)) return fail(TM_ERR_TOO_LARGE, "too many tiles");
+    }
+    *row_tiles = (int)rt;
+    *col_tiles = (int)ct;
+    *nx = x0;
+    *ny = y0;
+    return TM_OK;
+}
+
+}  // namespace
+}  // namespace tmc
+
+extern "C" size_t tm_pointcloud_sinkhorn_workspace_size(int64_t n_problems, int64_t max_iter) {
+    if (n_problems < 1 || max_iter < 1) return 0;
+    return tmc::pc_layout(n_problems, max_iter).total;
+}
+
+extern "C" int tm_pointcloud_sinkhorn(const float *x, const float *y, const float *log_a, const float *log_b,
+                                      int64_t n_problems, const int64_t *n, const int64_t *m, double epsilon,
+                                      int64_t max_iter, double threshold, int64_t check_every, float *f, float *g,
+                                      double *cost, int32_t *iterations, void *workspace, size_t workspace_bytes,
+                                      tm_stream_t stream) {
+    using namespace tmc;
+    if (!x || !y || !log_a || !log_b || !f || !g || !n || !m)
+        return fail(TM_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n_problems < 1 || n_problems > (1 << 24)) return fail(TM_ERR_INVALID_ARGUMENT, "n_problems must be 1..2^24");
+    if (!(epsilon > 0)) return fail(TM_ERR_INVALID_ARGUMENT, "epsilon must be positive");
+    if (max_iter < 1 || max_iter > (1 << 24)) return fail(TM_ERR_INVALID_ARGUMENT, "max_iter must be 1..2^24");
+    if (check_every < 1) return fail(TM_ERR_INVALID_ARGUMENT, "check_every must be positive");
+    const PcLayout L = pc_layout(n_problems, max_iter);
+    if (!workspace || workspace_bytes < L.total)
+        return fail(TM_ERR_WORKSPACE, "point-cloud Sinkhorn workspace of %zu bytes needed", L.total);
+    if ((uintptr_t)workspace & 255) return fail(TM_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
+    std::vector<PcProblem> probs;
+    int row_tiles = 0, col_tiles = 0;
+    int64_t nx = 0, ny = 0;
+    int st = build_problems(n_problems, n, m, probs, &row_tiles, &col_tiles, &nx, &ny);
+    if (st != TM_OK) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    // control block, errors, iteration counts and queues start at zero; every problem active
+    TM_CHECK_CUDA(cudaMemsetAsync(workspace, 0, L.total, s));
+    PcControl ctl{};
+    ctl.n_active = (int)n_problems;
+    TM_CHECK_CUDA(cudaMemcpyAsync(ws_at<PcControl>(workspace, L.ctl), &ctl, sizeof(ctl), cudaMemcpyHostToDevice, s));
+    TM_CHECK_CUDA(cudaMemcpyAsync(ws_at<PcProblem>(workspace, L.prob), probs.data(), probs.size() * sizeof(PcProblem),
+                                  cudaMemcpyHostToDevice, s));
+    std::vector<int> ones((size_t)n_problems, 1);
+    TM_CHECK_CUDA(cudaMemcpyAsync(ws_at<int>(workspace, L.active), ones.data(), ones.size() * sizeof(int),
+                                  cudaMemcpyHostToDevice, s));
+    // potentials start where the reference's log_u = log_v = 0 does
+    const unsigned init_blocks = (unsigned)std::min<int64_t>(ceil_div(nx > ny ? nx : ny, 256), 1024);
+    pc_init_kernel<<<init_blocks, 256, 0, s>>>(log_a, f, nx, (float)epsilon);
+    pc_init_kernel<<<init_blocks, 256, 0, s>>>(log_b, g, ny, (float)epsilon);
+    TM_LAUNCH_CHECK("pc_init_kernel");
+    int *status = nullptr;
+    if ((st = device_status_word(&status)) != TM_OK) return st;
+    int per_sm = 0;
+    TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pc_sinkhorn_kernel, kPcThreads, 0));
+    if (per_sm < 1) return fail(TM_ERR_UNSUPPORTED, "point-cloud kernel does not fit on an SM");
+    per_sm = per_sm > 4 ? 4 : per_sm;  // fewer CTAs make the grid barrier cheaper
+    const int blocks = per_sm * sm_count();
+    PcArgs args;
+    args.x = x;
+    args.y = y;
+    args.la = log_a;
+    args.lb = log_b;
+    args.f = f;
+    args.g = g;
+    args.prob = ws_at<PcProblem>(workspace, L.prob);
+    args.nprob = (int)n_problems;
+    args.row_tiles = row_tiles;
+    args.col_tiles = col_tiles;
+    args.err = ws_at<float>(workspace, L.err);
+    args.active = ws_at<int>(workspace, L.active);
+    args.iters = ws_at<int>(workspace, L.iters);
+    args.queue = ws_at<int>(workspace, L.queue);
+    args.ctl = ws_at<PcControl>(workspace, L.ctl);
+    args.status = status;
+    args.eps = (float)epsilon;
+    args.threshold = (float)threshold;
+    args.max_iter = (int)max_iter;
+    args.check_every = (int)check_every;
+    void *params[] = {&args};
+    TM_CHECK_CUDA(cudaLaunchCooperativeKernel((const void *)pc_sinkhorn_kernel, dim3(blocks), dim3(kPcThreads), params,
+                                              0, s));
+    TM_LAUNCH_CHECK("pc_sinkhorn_kernel");
+    if (cost) {
+        pc_cost_kernel<<<(unsigned)n_problems, kPcThreads, 0, s>>>(f, g, log_a, log_b, args.prob, cost);
+        TM_LAUNCH_CHECK("pc_cost_kernel");
+    }
+    if (iterations)
+        TM_CHECK_CUDA(cudaMemcpyAsync(iterations, args.iters, (size_t)n_problems * sizeof(int32_t),
+                                      cudaMemcpyDeviceToDevice, s));
+    return TM_OK;
+}
+
+extern "C" int tm_pointcloud_sinkhorn_grad(const float *x, const float *y, const float *log_a, const float *log_b,
+                                           const float *f, const float *g, int64_t n_problems, const int64_t *n,
+                                           const int64_t *m, double epsilon, const float *grad_cost, float *grad_x,
+                                           float *grad_y, void *workspace, size_t workspace_bytes,
+                                           tm_stream_t stream) {
+    using namespace tmc;
+    if (!x || !y || !log_a || !log_b || !f || !g || !n || !m || !grad_cost)
+        return fail(TM_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n_problems < 1 || n_problems > (1 << 24)) return fail(TM_ERR_INVALID_ARGUMENT, "n_problems must be 1..2^24");
+    if (!(epsilon > 0)) return fail(TM_ERR_INVALID_ARGUMENT, "epsilon must be positive");
+    const size_t need = (size_t)n_problems * sizeof(PcProblem);
+    if (!workspace || workspace_bytes < need) return fail(TM_ERR_WORKSPACE, "gradient workspace of %zu bytes needed", need);
+    std::vector<PcProblem> probs;
+    int row_tiles = 0, col_tiles = 0;
+    int64_t nx = 0, ny = 0;
+    int st = build_problems(n_problems, n, m, probs, &row_tiles, &col_tiles, &nx, &ny);
+    if (st != TM_OK) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    auto *dprob = static_cast<PcProblem *>(workspace);
+    TM_CHECK_CUDA(cudaMemcpyAsync(dprob, probs.data(), need, cudaMemcpyHostToDevice, s));
+    const int cap = sm_count() * 8;
+    if (grad_x) {
+        pc_grad_kernel<<<row_tiles < cap ? row_tiles : cap, kPcThreads, 0, s>>>(
+            x, y, f, g, log_a, log_b, dprob, (int)n_problems, row_tiles, true, (float)epsilon, grad_cost, grad_x);
+        TM_LAUNCH_CHECK("pc_grad_kernel");
+    }
+    if (grad_y) {
+        pc_grad_kernel<<<col_tiles < cap ? col_tiles : cap, kPcThreads, 0, s>>>(
+            y, x, g, f, log_b, log_a, dprob, (int)n_problems, col_tiles, false, (float)epsilon, grad_cost, grad_y);
+        TM_LAUNCH_CHECK("pc_grad_kernel");
+    }
+    return TM_OK;
+}
