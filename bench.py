@@ -290,6 +290,7 @@ def secondary(args, dev, stream, hbm_peak):
 
     out.update(ragged_lines(dev, stream, max(args.steps, 10), args.warmup))
     out.update(sinkhorn_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline))
+    out.update(pointcloud_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline))
     return out
 
 
@@ -363,6 +364,106 @@ def ragged_lines(dev, stream, steps, warmup):
                      "scope": "whole pipeline (5 launches incl. the x > 0.5 threshold), 18 "
                               "algorithmic B/pixel"},
         "gpu_launches_per_step": 5}}
+
+
+def pointcloud_problems(seed=0, count=512):
+    """512 OT problems, n and m iid log-uniform integers in [64, 2048], points from a
+    4-component Gaussian mixture in R^3 (means U[-1, 1]^3, sigma 0.2), uniform weights."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.log(64), np.log(2048)
+    xs, ys = [], []
+    for _ in range(count):
+        n = int(np.clip(np.rint(np.exp(rng.uniform(lo, hi))), 64, 2048))
+        m = int(np.clip(np.rint(np.exp(rng.uniform(lo, hi))), 64, 2048))
+        means = rng.uniform(-1, 1, (4, 3))
+        xs.append((means[rng.integers(0, 4, n)] + 0.2 * rng.standard_normal((n, 3))).astype(np.float32))
+        ys.append((means[rng.integers(0, 4, m)] + 0.2 * rng.standard_normal((m, 3))).astype(np.float32))
+    return xs, ys
+
+
+def pointcloud_lines(dev, stream, cpu_baseline=True):
+    """Ragged differentiable point-cloud Sinkhorn: 512 problems in one persistent launch,
+    eps 0.05, to an L1 column-marginal error <= 1e-5; gradient w.r.t. the source points."""
+    import torch
+
+    import oracle
+    from torchmorph_gb300 import PointCloudSinkhorn, pack_clouds
+
+    xs, ys = pointcloud_problems()
+    x, nx = pack_clouds([torch.from_numpy(v).to(dev) for v in xs])
+    y, ny = pack_clouds([torch.from_numpy(v).to(dev) for v in ys])
+    # 1e-4: with potentials of magnitude ~10 (mass moving between mixture components),
+    # fp32 rounding of f, g alone perturbs the plan's marginals by ~1e-5
+    eps, tol = 0.05, 1e-4
+    solver = PointCloudSinkhorn(epsilon=eps, max_iter=5000, threshold=tol, check_every=10)
+    pairs = sum(a * b for a, b in zip(nx, ny))
+    # kernel efficiency with every problem active: 100 fixed iterations
+    fixed = PointCloudSinkhorn(epsilon=eps, max_iter=100, threshold=0.0)
+    fixed.solve(x, y, nx, ny)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    fixed.solve(x, y, nx, ny)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_fixed = e0.elapsed_time(e1) / 1e3 / 100
+    ex2_peak = 16 * 152 * 2.07e9  # MUFU ex2 per clock per SM x SMs x max SM clock
+    res = solver.solve(x, y, nx, ny)  # warm-up
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    res = solver.solve(x, y, nx, ny)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_solve = e0.elapsed_time(e1) / 1e3
+    its = res["iterations"].cpu().numpy()
+    # forward + backward through autograd (the solve, then the gradient kernel)
+    xg = x.clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    solver(xg, y, nx, ny).sum().backward()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_fb = e0.elapsed_time(e1) / 1e3
+    # work: per problem and iteration 2 n m pair evaluations (one ex2 each)
+    ex2 = float(sum(2.0 * a * b * int(k) for a, b, k in zip(nx, ny, its)))
+    # float64 check on 6 problems: regularised cost and the returned plan's marginals
+    f, g = res["f"].cpu().numpy().astype(np.float64), res["g"].cpu().numpy().astype(np.float64)
+    ox, oy = np.cumsum([0] + nx), np.cumsum([0] + ny)
+    rel, marg = 0.0, 0.0
+    for p in range(0, 512, 512 // 6)[:6]:
+        xp, yp = xs[p].astype(np.float64), ys[p].astype(np.float64)
+        _, _, _, c64 = oracle.pointcloud_sinkhorn(xp, yp, eps, 100000, threshold=1e-12)
+        rel = max(rel, abs(res["cost"][p].item() - c64) / abs(c64))
+        C = ((xp[:, None] - yp[None]) ** 2).sum(-1)
+        P = np.exp((f[ox[p]:ox[p + 1], None] + g[None, oy[p]:oy[p + 1]] - C) / eps) / (len(xp) * len(yp))
+        marg = max(marg, np.abs(P.sum(0) - 1 / len(yp)).sum() + np.abs(P.sum(1) - 1 / len(xp)).sum())
+    line = {"problems": 512, "pairs_per_half_iteration": pairs, "threshold": tol,
+            "ms_solve": round(t_solve * 1e3, 3),
+            "solves/s": round(512 / t_solve, 1), "ms_forward_backward": round(t_fb * 1e3, 3),
+            "iterations_max": int(its.max()), "iterations_mean": round(float(its.mean()), 1),
+            "iterations_p90": int(np.percentile(its, 90)), "problems_at_max_iter": int((its >= 5000).sum()),
+            "ex2_per_s": float(f"{ex2 / t_solve:.4g}"),
+            "ex2_frac_of_nominal": round(ex2 / t_solve / ex2_peak, 4),
+            "us_per_iteration_all_active": round(t_fixed * 1e6, 1),
+            "ex2_frac_of_nominal_all_active": round(2.0 * pairs / t_fixed / ex2_peak, 4),
+            "rel_cost_error_vs_fp64": float(f"{rel:.3e}"),
+            "marginal_l1_fp64_max": float(f"{marg:.3e}"), "fp64_problems_checked": 6,
+            "launches_per_solve": 5}
+    if cpu_baseline:
+        cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+        t0 = time.perf_counter()
+        k = 0
+        for p in range(8):
+            oracle.pointcloud_sinkhorn(xs[p], ys[p], eps, int(its[p]), threshold=0.0)
+            k += 1
+            if time.perf_counter() - t0 > 20:
+                break
+        per = (time.perf_counter() - t0) / k
+        line["cpu_baseline"] = {"value": round(1.0 / per, 3), "unit": "solves/s", "cores": cores, "kind": "port",
+                                "sample": f"{k} problems, float64 numpy log-domain oracle, same iteration "
+                                          "counts as the GPU run"}
+    return {"pointcloud_sinkhorn_512_ragged_eps0.05": line}
 
 
 def sinkhorn_problem(dev, n=256, d=8192, seed=0):
@@ -559,7 +660,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--case", choices=["all", "sinkhorn", "ragged"], default="all",
+    ap.add_argument("--case", choices=["all", "sinkhorn", "ragged", "pointcloud"], default="all",
                     help="only the shared-cost Sinkhorn or the ragged-batch lines (one JSON object)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -570,6 +671,8 @@ def main():
         stream = torch.cuda.current_stream(dev)
         if args.case == "sinkhorn":
             print(json.dumps(sinkhorn_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline)))
+        elif args.case == "pointcloud":
+            print(json.dumps(pointcloud_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline)))
         else:
             print(json.dumps(ragged_lines(dev, stream, max(args.steps, 10), args.warmup)))
         return

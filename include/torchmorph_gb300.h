@@ -286,14 +286,17 @@ int tm_sinkhorn_tc_finish(int64_t n, int64_t d, float *log_u, float *log_v, doub
  * tm_pointcloud_sinkhorn_grad: gradient of the regularised cost w.r.t. the
  * points (envelope theorem: d cost_p / d x_i = 2 sum_j P_ij (x_i - y_j),
  * plan entries recomputed from f, g), scaled by grad_cost[p] (device fp32);
- * grad_x / grad_y may be NULL; the workspace holds n_problems * 32 bytes. */
-size_t tm_pointcloud_sinkhorn_workspace_size(int64_t n_problems, int64_t max_iter);
+ * grad_x / grad_y may be NULL; the workspace holds
+ * tm_pointcloud_sinkhorn_grad_workspace_size(n_problems) bytes. */
+size_t tm_pointcloud_sinkhorn_workspace_size(int64_t n_problems, const int64_t *n,
+                                             const int64_t *m, int64_t max_iter);
 int tm_pointcloud_sinkhorn(const float *x, const float *y, const float *log_a,
                            const float *log_b, int64_t n_problems, const int64_t *n,
                            const int64_t *m, double epsilon, int64_t max_iter, double threshold,
                            int64_t check_every, float *f, float *g, double *cost,
                            int32_t *iterations, void *workspace, size_t workspace_bytes,
                            tm_stream_t stream);
+size_t tm_pointcloud_sinkhorn_grad_workspace_size(int64_t n_problems);
 int tm_pointcloud_sinkhorn_grad(const float *x, const float *y, const float *log_a,
                                 const float *log_b, const float *f, const float *g,
                                 int64_t n_problems, const int64_t *n, const int64_t *m,

@@ -72,10 +72,11 @@ SIGNATURES = {
                                          c_int, c_void]),
     "tm_grey_dilation_backward": (c_int, [c_void, c_void, c_void, c_i64, c_int, I64P, U8P, I64P, I64P,
                                           c_int, c_void]),
-    "tm_pointcloud_sinkhorn_workspace_size": (c_size, [c_i64, c_i64]),
+    "tm_pointcloud_sinkhorn_workspace_size": (c_size, [c_i64, I64P, I64P, c_i64]),
     "tm_pointcloud_sinkhorn": (c_int, [c_void, c_void, c_void, c_void, c_i64, I64P, I64P, c_double,
                                        c_i64, c_double, c_i64, c_void, c_void, c_void, c_void, c_void,
                                        c_size, c_void]),
+    "tm_pointcloud_sinkhorn_grad_workspace_size": (c_size, [c_i64]),
     "tm_pointcloud_sinkhorn_grad": (c_int, [c_void, c_void, c_void, c_void, c_void, c_void, c_i64, I64P,
                                             I64P, c_double, c_void, c_void, c_void, c_void, c_size,
                                             c_void]),

@@ -17,6 +17,7 @@ from __future__ import annotations
 
 from typing import Sequence
 
+import numpy as np
 import torch
 from torch import Tensor
 
@@ -34,9 +35,9 @@ def pack_clouds(clouds: Sequence[Tensor]) -> tuple[Tensor, list[int]]:
 
 
 def _log_weights(weights, sizes, like):
-    if weights is None:
-        return torch.cat([torch.full((k,), -float(torch.log(torch.tensor(float(k)))), dtype=torch.float32,
-                                     device=like.device) for k in sizes])
+    if weights is None:  # uniform: log(1 / k) for each of a problem's k points, one copy
+        k = np.asarray(sizes, dtype=np.float64)
+        return torch.from_numpy(np.repeat(-np.log(k), k.astype(np.int64)).astype(np.float32)).to(like.device)
     w = weights.to(device=like.device, dtype=torch.float32).reshape(-1)
     if w.numel() != sum(sizes):
         raise ValueError("weights must have one entry per point")
@@ -47,7 +48,7 @@ def _solve(x, y, la, lb, nx, ny, eps, max_iter, threshold, check_every):
     lib = _lib.load()
     P = len(nx)
     dev = x.device
-    nbytes = lib.tm_pointcloud_sinkhorn_workspace_size(P, max_iter)
+    nbytes = lib.tm_pointcloud_sinkhorn_workspace_size(P, _lib.i64_array(nx), _lib.i64_array(ny), max_iter)
     ws = torch.empty(int(nbytes), dtype=torch.uint8, device=dev)
     f = torch.empty(x.shape[0], dtype=torch.float32, device=dev)
     g = torch.empty(y.shape[0], dtype=torch.float32, device=dev)
@@ -66,7 +67,7 @@ def _grad(x, y, la, lb, f, g, nx, ny, eps, grad_cost, need_x, need_y):
     lib = _lib.load()
     P = len(nx)
     dev = x.device
-    ws = torch.empty(P * 32 + 256, dtype=torch.uint8, device=dev)
+    ws = torch.empty(int(lib.tm_pointcloud_sinkhorn_grad_workspace_size(P)), dtype=torch.uint8, device=dev)
     gx = torch.empty_like(x) if need_x else None
     gy = torch.empty_like(y) if need_y else None
     scale = grad_cost.to(device=dev, dtype=torch.float32).contiguous()
