@@ -28,7 +28,11 @@
 //    4 threads.  Pass 2 runs along the contiguous axis, one warp per line,
 //    4 voxels per lane with 16-byte loads and stores.
 #include <cmath>
+#include <algorithm>
+#include <array>
 #include <cstring>
+#include <mutex>
+#include <vector>
 
 #include "edt_internal.cuh"
 
@@ -108,10 +112,12 @@ __device__ __forceinline__ bool widen(int q, int L, GF G, uint32_t &best, int &b
 // their first/last background position through shared memory.
 template <typename In>
 __global__ void __launch_bounds__(kCols *kSegs) edt_c0_smem_kernel(const In *__restrict__ in,
-                                                                   int16_t *__restrict__ c1, CompactParams p) {
+                                                                   int16_t *__restrict__ c1, CompactParams p,
+                                                                   const int *__restrict__ todo) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = p.L0;
     const int64_t inner = p.numel_item / L;
+    if (todo && !todo[blockIdx.x / ((inner + kCols - 1) / kCols)]) return;  // item finished by the shell pass
     uint8_t *fg = smem_raw;                                              // [L][kCols]
     int16_t *prev = reinterpret_cast<int16_t *>(smem_raw + L * kCols);   // [L][kCols]
     int16_t *seg_last = prev + L * kCols;                                // [kSegs][kCols]
@@ -650,6 +656,721 @@ __global__ void __launch_bounds__(kC2Warps * 32) edt_c2_kernel(const void *__res
     }
 }
 
+// ------------------------------------------------------ passes 1 + 2 fused
+// 3-D items with L0, L1 <= 255 and L2 a multiple of 4: one CTA per (item, z)
+// plane runs pass 1 (axis 1) and pass 2 (axis 2) back to back on chip.  The
+// plane's pass-0 features are staged as bytes (f0, 255 = none); pass 1
+// writes packed (f0 | f1 << 8) uint16 features (0xFFFF = none) to a second
+// shared-memory plane, which pass 2 reads row by row; only the final
+// outputs go to global memory.  Same windows, widening, tie rules and
+// envelope fallbacks as edt_c1_kernel / edt_c2_kernel.
+constexpr int kC12Threads = 256;
+constexpr int kC12Warps = kC12Threads / 32;
+constexpr int kC12Cols = 128;  // pass-1 columns per group (2 threads per column)
+constexpr int kC12PadTop = kNear1;
+constexpr int kC12PadBot = kNear1 + kQB;
+constexpr int kC12PadX = 4;
+constexpr uint8_t kNoF0 = 255;
+constexpr uint16_t kNoF01 = 0xFFFF;
+
+struct C12Smem {
+    int L1, L2, rowp;  // rowp: padded pass-2 row length
+    size_t tab, f0s, p1, stk, flag, total;
+};
+
+__host__ __device__ inline C12Smem c12_smem(int L1, int L2) {
+    C12Smem m;
+    m.L1 = L1;
+    m.L2 = L2;
+    m.rowp = L2 + 2 * kC12PadX;
+    size_t off = 0;
+    m.tab = off;
+    off += kSqrtTab * 4;
+    m.f0s = off;
+    off += ((size_t)(L1 + kC12PadTop + kC12PadBot) * L2 + 15) / 16 * 16;
+    m.p1 = off;
+    off += ((size_t)L1 * m.rowp * 2 + 15) / 16 * 16;
+    m.stk = off;
+    off += ((size_t)kC12Warps * L2 * 2 + 15) / 16 * 16;
+    m.flag = off;
+    off += (size_t)kC12Cols * 4;
+    m.total = off;
+    return m;
+}
+
+__global__ void __launch_bounds__(kC12Threads) edt_c12_kernel(const int16_t *__restrict__ c1, float *__restrict__ dist,
+                                                              int32_t *__restrict__ indices,
+                                                              int32_t *__restrict__ sqdist,
+                                                              int16_t *__restrict__ gstack, CompactParams p,
+                                                              const int *__restrict__ todo) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int L0 = p.L0, L1 = p.L1, W = p.L2;
+    if (todo && !todo[blockIdx.x / L0]) return;  // item finished by the shell pass
+    const C12Smem sm = c12_smem(L1, W);
+    float *tab = reinterpret_cast<float *>(smem_raw + sm.tab);
+    uint8_t *f0s = smem_raw + sm.f0s + kC12PadTop * W;  // row y at f0s + y * W, y in -4 .. L1+11
+    uint16_t *p1 = reinterpret_cast<uint16_t *>(smem_raw + sm.p1);  // row y at p1 + y * rowp + kC12PadX
+    int16_t *stk_all = reinterpret_cast<int16_t *>(smem_raw + sm.stk);
+    int *colflag = reinterpret_cast<int *>(smem_raw + sm.flag);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t item = blockIdx.x / L0;
+    const int z = (int)(blockIdx.x - item * L0);
+    const int64_t plane = item * p.numel_item + (int64_t)z * L1 * W;
+    const int rowp = sm.rowp;
+    for (int i = tid; i < kSqrtTab; i += kC12Threads) tab[i] = __fsqrt_rn((float)i);
+    // padding: "no site" rows around the f0 plane and columns around each p1 row
+    for (int i = tid; i < (kC12PadTop + kC12PadBot) * W; i += kC12Threads) {
+        const int r = i / W, c = i % W;
+        const int y = r < kC12PadTop ? r - kC12PadTop : L1 + r - kC12PadTop;
+        f0s[y * W + c] = kNoF0;
+    }
+    for (int i = tid; i < L1 * 2 * kC12PadX; i += kC12Threads) {
+        const int y = i / (2 * kC12PadX), k = i % (2 * kC12PadX);
+        p1[y * rowp + (k < kC12PadX ? k : W + k)] = kNoF01;
+    }
+    // stage the pass-0 features of the plane as bytes, 4 per lane per row
+    for (int i = tid; i < L1 * (W / 4); i += kC12Threads) {
+        const int y = i / (W / 4), c4 = i % (W / 4);
+        const short4 v = *reinterpret_cast<const short4 *>(c1 + plane + (int64_t)y * W + 4 * c4);
+        const uint32_t b0 = v.x < 0 ? kNoF0 : (uint32_t)v.x, b1 = v.y < 0 ? kNoF0 : (uint32_t)v.y;
+        const uint32_t b2 = v.z < 0 ? kNoF0 : (uint32_t)v.z, b3 = v.w < 0 ? kNoF0 : (uint32_t)v.w;
+        reinterpret_cast<uint32_t *>(f0s + y * W)[c4] = b0 | (b1 << 8) | (b2 << 16) | (b3 << 24);
+    }
+    __syncthreads();
+
+    // ---- pass 1: columns along axis 1, 2 threads per column
+    const int64_t nlines1 = p.batch * (int64_t)L0 * W;
+    for (int xg = 0; xg < W; xg += kC12Cols) {
+        const int xl = tid % kC12Cols, seg = tid / kC12Cols;
+        const int x = xg + xl;
+        const uint8_t *fcol = f0s + x;
+        auto G1 = [&](int pp) -> uint32_t {
+            const int f = fcol[pp * W];
+            return f == kNoF0 ? kBig : (uint32_t)((z - f) * (z - f));
+        };
+        bool fallback = false;
+        if (tid < kC12Cols) colflag[tid] = 0;
+        __syncthreads();
+        if (x < W) {
+            const int qa = seg * L1 / 2, qb = (seg + 1) * L1 / 2;
+            constexpr int NW = kQB + 2 * kNear1;
+            for (int q0 = qa; q0 < qb && !fallback; q0 += kQB) {
+                uint32_t w[NW];
+#pragma unroll
+                for (int j = 0; j < NW; j++) {
+                    const int f = fcol[(q0 - kNear1 + j) * W];
+                    w[j] = (f == kNoF0 ? kBig : (uint32_t)((z - f) * (z - f))) << kKeyShift;
+                }
+#pragma unroll
+                for (int i = 0; i < kQB; i++) {
+                    const int q = q0 + i;
+                    if (q < qb && !fallback) {
+                        const uint32_t key = window_key<kNear1>(w + i);
+                        uint32_t best = key >> kKeyShift;
+                        int bp = q - kNear1 + (int)(key & 31u);
+                        if (best >= (kNear1 + 1) * (kNear1 + 1) && !widen<kNear1>(q, L1, G1, best, bp)) {
+                            fallback = true;
+                        } else {
+                            p1[q * rowp + kC12PadX + x] =
+                                best >= kBig ? kNoF01 : (uint16_t)(fcol[bp * W] | (bp << 8));
+                        }
+                    }
+                }
+            }
+        }
+        if (fallback) colflag[xl] = 1;
+        __syncthreads();
+        if (seg == 0 && x < W && colflag[xl]) {
+            // exact lower envelope of the column, stack in the workspace
+            const int64_t lid = (item * L0 + z) * (int64_t)W + x;
+            int k = -1, top = 0, sec = 0;
+            int32_t Gtop = 0, Gsec = 0;
+            for (int q = 0; q < L1; q++) {
+                const uint32_t gq = G1(q);
+                if (gq >= kBig) continue;
+                const int32_t Gq = (int32_t)gq + q * q;
+                while (k >= 1) {
+                    const long long lhs = (long long)(Gq - Gtop) * (top - sec);
+                    const long long rhs = (long long)(Gtop - Gsec) * (q - top);
+                    if (lhs > rhs) break;
+                    k--;
+                    top = sec;
+                    Gtop = Gsec;
+                    if (k >= 1) {
+                        sec = gstack[(int64_t)(k - 1) * nlines1 + lid];
+                        Gsec = (int32_t)G1(sec) + sec * sec;
+                    }
+                }
+                k++;
+                gstack[(int64_t)k * nlines1 + lid] = (int16_t)q;
+                sec = top;
+                Gsec = Gtop;
+                top = q;
+                Gtop = Gq;
+            }
+            if (k < 0) {
+                for (int q = 0; q < L1; q++) p1[q * rowp + kC12PadX + x] = kNoF01;
+            } else {
+                int j = 0, cur = gstack[lid], nxt = 0;
+                uint32_t gcur = G1(cur), gnxt = 0;
+                if (k >= 1) {
+                    nxt = gstack[nlines1 + lid];
+                    gnxt = G1(nxt);
+                }
+                for (int q = 0; q < L1; q++) {
+                    uint32_t fc = (uint32_t)((q - cur) * (q - cur)) + gcur;
+                    while (j < k) {
+                        const uint32_t fn = (uint32_t)((q - nxt) * (q - nxt)) + gnxt;
+                        if (!(fn < fc)) break;
+                        j++;
+                        cur = nxt;
+                        gcur = gnxt;
+                        fc = fn;
+                        if (j < k) {
+                            nxt = gstack[(int64_t)(j + 1) * nlines1 + lid];
+                            gnxt = G1(nxt);
+                        }
+                    }
+                    p1[q * rowp + kC12PadX + x] = (uint16_t)(fcol[cur * W] | (cur << 8));
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    // ---- pass 2: rows along axis 2, one warp per row, 4 voxels per lane
+    const int64_t numel = p.numel;
+    int16_t *st = stk_all + warp * W;
+    for (int y = warp; y < L1; y += kC12Warps) {
+        const uint16_t *row = p1 + y * rowp + kC12PadX;
+        auto dec = [&](uint32_t f) -> uint32_t {
+            if (f == kNoF01) return kBig;
+            const int f0 = (int)(f & 255u), f1 = (int)(f >> 8);
+            return (uint32_t)((z - f0) * (z - f0) + (y - f1) * (y - f1));
+        };
+        auto G2 = [&](int pp) { return dec(row[pp]); };
+        const int64_t base = plane + (int64_t)y * W;
+        bool any = false;
+        for (int q = lane; q < W; q += 32) any |= row[q] != kNoF01;
+        any = __any_sync(0xffffffffu, any);
+        if (!any) {
+            // no background anywhere in the item: virtual site (-1, 0, 0)
+            for (int q = lane; q < W; q += 32) {
+                const int64_t gi = base + q;
+                const uint32_t s2 = (uint32_t)((z + 1) * (z + 1) + y * y + q * q);
+                if (dist) dist[gi] = dist_of(s2, tab);
+                if (sqdist) sqdist[gi] = (int32_t)s2;
+                if (indices) {
+                    indices[gi] = -1;
+                    indices[numel + gi] = 0;
+                    indices[2 * numel + gi] = 0;
+                }
+            }
+            continue;
+        }
+        bool fallback = false;
+        for (int c = 0; c < W && !fallback; c += 128) {
+            const int q0 = c + 4 * lane;
+            if (q0 >= W) break;
+            uint32_t w[12];  // shifted g at q0-4 .. q0+7
+            uint32_t fv[12];
+#pragma unroll
+            for (int j = 0; j < 12; j++) {
+                fv[j] = row[q0 - 4 + j];
+                w[j] = dec(fv[j]) << kKeyShift;
+            }
+            float dv[4];
+            int32_t i0[4], i1[4], i2[4], sq[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int q = q0 + i;
+                const uint32_t key = window_key<kNear2>(w + i + 2);
+                uint32_t best = key >> kKeyShift;
+                int bp = q - kNear2 + (int)(key & 31u);
+                if (best >= (kNear2 + 1) * (kNear2 + 1) && !widen<kNear2>(q, W, G2, best, bp)) fallback = true;
+                const uint32_t f = row[bp];
+                dv[i] = dist_of(best, tab);
+                sq[i] = (int32_t)best;
+                i0[i] = (int32_t)(f & 255u);
+                i1[i] = (int32_t)(f >> 8);
+                i2[i] = bp;
+            }
+            if (fallback) break;
+            const int64_t gi = base + q0;
+            if (dist) *reinterpret_cast<float4 *>(dist + gi) = make_float4(dv[0], dv[1], dv[2], dv[3]);
+            if (sqdist) *reinterpret_cast<int4 *>(sqdist + gi) = make_int4(sq[0], sq[1], sq[2], sq[3]);
+            if (indices) {
+                *reinterpret_cast<int4 *>(indices + gi) = make_int4(i0[0], i0[1], i0[2], i0[3]);
+                *reinterpret_cast<int4 *>(indices + numel + gi) = make_int4(i1[0], i1[1], i1[2], i1[3]);
+                *reinterpret_cast<int4 *>(indices + 2 * numel + gi) = make_int4(i2[0], i2[1], i2[2], i2[3]);
+            }
+        }
+        if (!__any_sync(0xffffffffu, fallback)) continue;
+        // exact lower envelope of the row: lane 0 builds it, every lane searches it
+        int ktop = 0;
+        if (lane == 0) {
+            int k = -1, top = 0, sec = 0;
+            int32_t Gtop = 0, Gsec = 0;
+            for (int q = 0; q < W; q++) {
+                const uint32_t gq = G2(q);
+                if (gq >= kBig) continue;
+                const int32_t Gq = (int32_t)gq + q * q;
+                while (k >= 1) {
+                    const long long lhs = (long long)(Gq - Gtop) * (top - sec);
+                    const long long rhs = (long long)(Gtop - Gsec) * (q - top);
+                    if (lhs > rhs) break;
+                    k--;
+                    top = sec;
+                    Gtop = Gsec;
+                    if (k >= 1) {
+                        sec = st[k - 1];
+                        Gsec = (int32_t)G2(sec) + sec * sec;
+                    }
+                }
+                st[++k] = (int16_t)q;
+                sec = top;
+                Gsec = Gtop;
+                top = q;
+                Gtop = Gq;
+            }
+            ktop = k;
+        }
+        ktop = __shfl_sync(0xffffffffu, ktop, 0);
+        __syncwarp();
+        for (int q = lane; q < W; q += 32) {
+            int lo = 0, hi = ktop;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                const int a = st[mid - 1], b = st[mid];
+                const uint32_t fa = (uint32_t)((q - a) * (q - a)) + G2(a);
+                const uint32_t fb = (uint32_t)((q - b) * (q - b)) + G2(b);
+                if (fb < fa)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            const int bp = st[lo];
+            const uint32_t best = (uint32_t)((q - bp) * (q - bp)) + G2(bp);
+            const uint32_t f = row[bp];
+            const int64_t gi = base + q;
+            if (dist) dist[gi] = dist_of(best, tab);
+            if (sqdist) sqdist[gi] = (int32_t)best;
+            if (indices) {
+                indices[gi] = (int32_t)(f & 255u);
+                indices[numel + gi] = (int32_t)(f >> 8);
+                indices[2 * numel + gi] = bp;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// -------------------------------------------------------- shell search
+// 3-D items whose voxels all have a background voxel within squared distance
+// kShellD2 (dense backgrounds, e.g. 10 %): the answer is the first background
+// offset in the list of all offsets with |d|^2 <= kShellD2 sorted by
+// (|d|^2, dx, dy, dz) -- nearest first, ties to the smallest last-axis, then
+// middle-axis, then first-axis coordinate, which is the separable passes'
+// (scipy's) tie rule.  Background is kept as bitmaps (bit b of word w of a
+// row = voxel 32 w + b), so one funnel shift tests an offset for 32 voxels.
+// Voxels without a background within the radius mark their item; those
+// items then run the separable passes (which skip every other item).
+constexpr int kShellR = 4;
+constexpr int kShellD2 = 16;
+constexpr int kShellN = 257;  // offsets with |d|^2 <= 16
+constexpr int kShellRows = 32;  // rows (axis 1) per CTA
+constexpr int kShellThreads = 128;
+__constant__ uint32_t c_shell[kShellN];  // packed (dz+8) | (dy+8) << 4 | (dx+8) << 8 | d2 << 12
+
+// Background bitmap, ceil(L2 / 32) words per row, one word per thread.  When
+// rows are a multiple of 32 voxels (and the input 16-byte aligned) a word is
+// read with 16-byte loads and the bytes tested four at a time.
+__device__ __forceinline__ uint32_t zero_bytes4(uint32_t v) {
+    // bit k set when byte k of v is zero
+    const uint32_t m = __vcmpeq4(v, 0u);
+    return ((m >> 7) & 1u) | ((m >> 14) & 2u) | ((m >> 21) & 4u) | ((m >> 28) & 8u);
+}
+
+template <typename In, bool VEC>
+__global__ void __launch_bounds__(256) edt_bitmap_kernel(const In *__restrict__ in, uint32_t *__restrict__ bm,
+                                                         CompactParams p, int ww, int64_t nwords) {
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = w / ww;
+        const int wi = (int)(w - row * ww);
+        const In *src = in + row * p.L2 + 32 * wi;
+        uint32_t bits = 0;
+        if (VEC) {
+            if (sizeof(In) == 1) {
+                const uint4 a = reinterpret_cast<const uint4 *>(src)[0], b = reinterpret_cast<const uint4 *>(src)[1];
+                const uint32_t v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+                for (int k = 0; k < 8; k++) bits |= zero_bytes4(v[k]) << (4 * k);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const float4 f = reinterpret_cast<const float4 *>(src)[k];
+                    bits |= ((uint32_t)(f.x == 0.f) | ((uint32_t)(f.y == 0.f) << 1) | ((uint32_t)(f.z == 0.f) << 2) |
+                             ((uint32_t)(f.w == 0.f) << 3))
+                            << (4 * k);
+                }
+            }
+        } else {
+            const int nb = min(32, p.L2 - 32 * wi);
+            for (int b = 0; b < nb; b++) bits |= (uint32_t)(src[b] == (In)0) << b;
+        }
+        bm[w] = bits;
+    }
+}
+
+struct ShellSmem {
+    int ww, pitch, planep;  // words per row, padded words per row, words per padded plane
+    size_t bits, res, tab, tab2, total;
+};
+
+// Padded bitmap rows: a zero word, the row's words, a zero word.
+constexpr int kShellPadW = 1;
+
+__host__ __device__ inline ShellSmem shell_smem(int L2) {
+    ShellSmem m;
+    m.ww = (L2 + 31) / 32;
+    m.pitch = m.ww + 2 * kShellPadW;
+    m.planep = (kShellRows + 2 * kShellR) * m.pitch;
+    size_t off = 0;
+    m.bits = off;
+    off += (size_t)(2 * kShellR + 1) * m.planep * 4;
+    m.res = off;
+    off += ((size_t)kShellRows * L2 * 2 + 15) / 16 * 16;
+    m.tab = off;
+    off += (size_t)kShellN * 8;
+    m.tab2 = off;
+    off += (size_t)kShellN * 4;
+    m.total = off;
+    return m;
+}
+
+// One CTA: rows y0 .. y0+31 of plane z of one item.  Stage the bitmaps of
+// planes z-4 .. z+4, rows y0-4 .. y0+35 (zero outside the item), search each
+// 32-voxel word through the sorted offsets until all its voxels are
+// resolved, then write distances / indices 4 voxels per thread.
+__global__ void __launch_bounds__(kShellThreads) edt_shell_kernel(const uint32_t *__restrict__ bm,
+                                                                  float *__restrict__ dist,
+                                                                  int32_t *__restrict__ indices,
+                                                                  int32_t *__restrict__ sqdist, int *__restrict__ todo,
+                                                                  CompactParams p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int L0 = p.L0, L1 = p.L1, W = p.L2;
+    const ShellSmem sm = shell_smem(W);
+    uint32_t *bits = reinterpret_cast<uint32_t *>(smem_raw + sm.bits);
+    uint16_t *res = reinterpret_cast<uint16_t *>(smem_raw + sm.res);
+    int2 *tab = reinterpret_cast<int2 *>(smem_raw + sm.tab);  // (word delta, shift | d2 << 8)
+    uint32_t *tab2 = reinterpret_cast<uint32_t *>(smem_raw + sm.tab2);  // packed offsets
+    __shared__ int s_unresolved;
+    const int ybl = (L1 + kShellRows - 1) / kShellRows;
+    const int64_t item = blockIdx.x / ((int64_t)L0 * ybl);
+    const int rem = (int)(blockIdx.x - item * L0 * ybl);
+    const int z = rem / ybl, y0 = (rem % ybl) * kShellRows;
+    const int nrows = min(kShellRows, L1 - y0);
+    const int ww = sm.ww, pitch = sm.pitch, planep = sm.planep;
+    const int tid = threadIdx.x;
+    if (tid == 0) s_unresolved = 0;
+    for (int t = tid; t < kShellN; t += kShellThreads) {
+        const uint32_t e = c_shell[t];
+        const int dz = (int)(e & 15u) - 8, dy = (int)((e >> 4) & 15u) - 8, dx = (int)((e >> 8) & 15u) - 8;
+        const int d2 = (int)(e >> 12);
+        tab[t] = make_int2(dz * planep + dy * pitch + (dx >= 0 ? 0 : -1), (dx >= 0 ? dx : 32 + dx) | (d2 << 8));
+        tab2[t] = e;
+    }
+    // stage bitmaps: plane k = z-4+k, padded row r = y0-4+r; zero outside the item
+    const uint32_t *ibm = bm + item * (int64_t)L0 * L1 * ww;
+    constexpr int kRowsP = kShellRows + 2 * kShellR;
+    for (int i = tid; i < (2 * kShellR + 1) * kRowsP; i += kShellThreads) {
+        const int k = i / kRowsP, r = i - k * kRowsP;
+        const int zz = z - kShellR + k, yy = y0 - kShellR + r;
+        uint32_t *dst = bits + k * planep + r * pitch;
+        const bool in_item = (unsigned)zz < (unsigned)L0 && (unsigned)yy < (unsigned)L1;
+        const uint32_t *src = ibm + ((int64_t)zz * L1 + yy) * ww;
+        dst[0] = 0u;
+        dst[kShellPadW + ww] = 0u;
+        if ((ww & 3) == 0) {  // 16-byte global loads (rows of the bitmap are 16-byte aligned)
+            for (int c = 0; c < ww; c += 4) {
+                const uint4 v = in_item ? *reinterpret_cast<const uint4 *>(src + c) : make_uint4(0, 0, 0, 0);
+                dst[kShellPadW + c] = v.x;
+                dst[kShellPadW + c + 1] = v.y;
+                dst[kShellPadW + c + 2] = v.z;
+                dst[kShellPadW + c + 3] = v.w;
+            }
+        } else {
+            for (int c = 0; c < ww; c++) dst[kShellPadW + c] = in_item ? src[c] : 0u;
+        }
+    }
+    __syncthreads();
+    // search: one 32-voxel word per thread
+    const uint32_t *center = bits + kShellR * planep + kShellR * pitch + kShellPadW;  // (z, y0, word 0)
+    for (int e = tid; e < nrows * ww; e += kShellThreads) {
+        const int r = e / ww, wi = e % ww;
+        const int nb = min(32, W - 32 * wi);
+        uint32_t U = nb == 32 ? 0xffffffffu : ((1u << nb) - 1u);
+        const uint32_t *here = center + r * pitch + wi;
+        uint16_t *out = res + r * W + 32 * wi;
+        // four offsets per step: their loads are independent, the hits are
+        // applied in list order so earlier offsets keep priority
+        for (int t = 0; t < kShellN && U; t += 4) {
+            uint32_t bg[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                bg[k] = 0;
+                if (t + k < kShellN) {
+                    const int2 tb = tab[t + k];
+                    bg[k] = __funnelshift_r(here[tb.x], here[tb.x + 1], tb.y & 31);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                uint32_t hit = bg[k] & U;
+                if (hit) {
+                    U &= ~hit;
+                    do {
+                        const int b = __ffs(hit) - 1;
+                        out[b] = (uint16_t)(t + k);
+                        hit &= hit - 1;
+                    } while (hit);
+                }
+            }
+        }
+        if (U) {
+            s_unresolved = 1;
+            do {
+                const int b = __ffs(U) - 1;
+                out[b] = 0xFFFF;
+                U &= U - 1;
+            } while (U);
+        }
+    }
+    __syncthreads();
+    if (s_unresolved) {  // the separable passes redo this item
+        if (tid == 0) atomicExch(&todo[item], 1);
+        return;
+    }
+    // outputs: a warp per row, 4 consecutive voxels per lane (16-byte stores)
+    const int64_t numel = p.numel;
+    const int64_t rowbase = item * p.numel_item + ((int64_t)z * L1 + y0) * W;
+    const int warp = tid >> 5, lane = tid & 31;
+    for (int r = warp; r < nrows; r += kShellThreads / 32) {
+        const uint16_t *rres = res + r * W;
+        for (int x = 4 * lane; x < W; x += 128) {
+            float dv[4];
+            int32_t i0[4], i1[4], i2[4], sq[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const uint32_t c = tab2[rres[x + k]];
+                const uint32_t d2 = c >> 12;
+                dv[k] = __fsqrt_rn((float)d2);
+                sq[k] = (int32_t)d2;
+                i0[k] = z + (int)(c & 15u) - 8;
+                i1[k] = y0 + r + (int)((c >> 4) & 15u) - 8;
+                i2[k] = x + k + (int)((c >> 8) & 15u) - 8;
+            }
+            const int64_t gi = rowbase + (int64_t)r * W + x;
+            if (dist) *reinterpret_cast<float4 *>(dist + gi) = make_float4(dv[0], dv[1], dv[2], dv[3]);
+            if (sqdist) *reinterpret_cast<int4 *>(sqdist + gi) = make_int4(sq[0], sq[1], sq[2], sq[3]);
+            if (indices) {
+                *reinterpret_cast<int4 *>(indices + gi) = make_int4(i0[0], i0[1], i0[2], i0[3]);
+                *reinterpret_cast<int4 *>(indices + numel + gi) = make_int4(i1[0], i1[1], i1[2], i1[3]);
+                *reinterpret_cast<int4 *>(indices + 2 * numel + gi) = make_int4(i2[0], i2[1], i2[2], i2[3]);
+            }
+        }
+    }
+}
+
+// Compile-time variant for rows of WW words: the offsets, word deltas and
+// shifts are constants, so the search is straight-line code with immediate
+// shared-memory offsets (no table reads, no address arithmetic).
+struct ShellOff {
+    int dz, dy, dx, d2;
+};
+
+struct ShellList {
+    ShellOff o[kShellN];
+};
+
+__host__ __device__ constexpr ShellList make_shell_list() {
+    ShellList l{};
+    int n = 0;
+    for (int d2 = 0; d2 <= kShellD2; d2++)
+        for (int dx = -kShellR; dx <= kShellR; dx++)
+            for (int dy = -kShellR; dy <= kShellR; dy++)
+                for (int dz = -kShellR; dz <= kShellR; dz++)
+                    if (dz * dz + dy * dy + dx * dx == d2) l.o[n++] = ShellOff{dz, dy, dx, d2};
+    return l;
+}
+
+template <int WW>
+__global__ void __launch_bounds__(kShellThreads) edt_shell_ct_kernel(const uint32_t *__restrict__ bm,
+                                                                     float *__restrict__ dist,
+                                                                     int32_t *__restrict__ indices,
+                                                                     int32_t *__restrict__ sqdist,
+                                                                     int *__restrict__ todo, CompactParams p) {
+    constexpr ShellList kL = make_shell_list();
+    constexpr int kPitch = WW + 2 * kShellPadW;
+    constexpr int kRowsP = kShellRows + 2 * kShellR;
+    constexpr int kPlaneP = kRowsP * kPitch;
+    __shared__ __align__(16) uint32_t bits[(2 * kShellR + 1) * kPlaneP];
+    __shared__ __align__(16) uint16_t res[kShellRows * WW * 32];
+    __shared__ int2 tab2[kShellN];  // (packed offset, distance as float bits)
+    __shared__ int s_unresolved;
+    const int L0 = p.L0, L1 = p.L1, W = p.L2;
+    const int ybl = (L1 + kShellRows - 1) / kShellRows;
+    const int64_t item = blockIdx.x / ((int64_t)L0 * ybl);
+    const int rem = (int)(blockIdx.x - item * L0 * ybl);
+    const int z = rem / ybl, y0 = (rem % ybl) * kShellRows;
+    const int nrows = min(kShellRows, L1 - y0);
+    const int tid = threadIdx.x;
+    if (tid == 0) s_unresolved = 0;
+    for (int t = tid; t < kShellN; t += kShellThreads) {
+        const uint32_t c = c_shell[t];
+        tab2[t] = make_int2((int)c, __float_as_int(__fsqrt_rn((float)(c >> 12))));
+    }
+    const uint32_t *ibm = bm + item * (int64_t)L0 * L1 * WW;
+    for (int i = tid; i < (2 * kShellR + 1) * kRowsP; i += kShellThreads) {
+        const int k = i / kRowsP, r = i - k * kRowsP;
+        const int zz = z - kShellR + k, yy = y0 - kShellR + r;
+        uint32_t *dst = bits + k * kPlaneP + r * kPitch;
+        const bool in_item = (unsigned)zz < (unsigned)L0 && (unsigned)yy < (unsigned)L1;
+        const uint32_t *src = ibm + ((int64_t)zz * L1 + yy) * WW;
+        dst[0] = 0u;
+        dst[kShellPadW + WW] = 0u;
+        if constexpr ((WW & 3) == 0) {
+#pragma unroll
+            for (int c = 0; c < WW; c += 4) {
+                const uint4 v = in_item ? *reinterpret_cast<const uint4 *>(src + c) : make_uint4(0, 0, 0, 0);
+                dst[kShellPadW + c] = v.x;
+                dst[kShellPadW + c + 1] = v.y;
+                dst[kShellPadW + c + 2] = v.z;
+                dst[kShellPadW + c + 3] = v.w;
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < WW; c++) dst[kShellPadW + c] = in_item ? src[c] : 0u;
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < nrows * WW; e += kShellThreads) {
+        const int r = e / WW, wi = e % WW;
+        const int nb = min(32, W - 32 * wi);
+        uint32_t U = nb == 32 ? 0xffffffffu : ((1u << nb) - 1u);
+        const uint32_t *here = bits + kShellR * kPlaneP + (kShellR + r) * kPitch + kShellPadW + wi;
+        uint16_t *out = res + r * W + 32 * wi;
+        // batches of 8 offsets in list order: 16 independent loads, one
+        // branch on the union of the batch's hits; inside a hit batch the
+        // offsets are applied in order, so earlier ones keep priority
+        constexpr int kB = 8;
+#pragma unroll
+        for (int t0 = 0; t0 < kShellN; t0 += kB) {
+            if (U == 0u) break;
+            uint32_t bg[kB];
+            uint32_t any = 0;
+#pragma unroll
+            for (int i = 0; i < kB; i++) {
+                const int t = t0 + i < kShellN ? t0 + i : kShellN - 1;
+                const int delta = kL.o[t].dz * kPlaneP + kL.o[t].dy * kPitch + (kL.o[t].dx >= 0 ? 0 : -1);
+                const int sh = kL.o[t].dx >= 0 ? kL.o[t].dx : 32 + kL.o[t].dx;
+                bg[i] = t0 + i < kShellN ? __funnelshift_r(here[delta], here[delta + 1], sh) : 0u;
+                any |= bg[i];
+            }
+            uint32_t H = any & U;
+            if (H) {
+                U &= ~H;
+#pragma unroll
+                for (int i = 0; i < kB; i++) {
+                    uint32_t hit = bg[i] & H;
+                    if (hit) {
+                        H &= ~hit;
+                        do {
+                            const int b = __ffs(hit) - 1;
+                            out[b] = (uint16_t)(t0 + i);
+                            hit &= hit - 1;
+                        } while (hit);
+                    }
+                }
+            }
+        }
+        if (U) {
+            s_unresolved = 1;
+            do {
+                const int b = __ffs(U) - 1;
+                out[b] = 0xFFFF;
+                U &= U - 1;
+            } while (U);
+        }
+    }
+    __syncthreads();
+    if (s_unresolved) {
+        if (tid == 0) atomicExch(&todo[item], 1);
+        return;
+    }
+    const int64_t numel = p.numel;
+    const int64_t rowbase = item * p.numel_item + ((int64_t)z * L1 + y0) * W;
+    const int warp = tid >> 5, lane = tid & 31;
+    for (int r = warp; r < nrows; r += kShellThreads / 32) {
+        const uint16_t *rres = res + r * W;
+        for (int x = 4 * lane; x < W; x += 128) {
+            float dv[4];
+            int32_t i0[4], i1[4], i2[4], sq[4];
+            const uint2 rr = *reinterpret_cast<const uint2 *>(rres + x);  // 4 offset numbers
+            const int tt[4] = {(int)(rr.x & 0xffffu), (int)(rr.x >> 16), (int)(rr.y & 0xffffu), (int)(rr.y >> 16)};
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int2 e = tab2[tt[k]];
+                const uint32_t c = (uint32_t)e.x;
+                dv[k] = __int_as_float(e.y);
+                sq[k] = (int32_t)(c >> 12);
+                i0[k] = z + (int)(c & 15u) - 8;
+                i1[k] = y0 + r + (int)((c >> 4) & 15u) - 8;
+                i2[k] = x + k + (int)((c >> 8) & 15u) - 8;
+            }
+            const int64_t gi = rowbase + (int64_t)r * W + x;
+            if (dist) *reinterpret_cast<float4 *>(dist + gi) = make_float4(dv[0], dv[1], dv[2], dv[3]);
+            if (sqdist) *reinterpret_cast<int4 *>(sqdist + gi) = make_int4(sq[0], sq[1], sq[2], sq[3]);
+            if (indices) {
+                *reinterpret_cast<int4 *>(indices + gi) = make_int4(i0[0], i0[1], i0[2], i0[3]);
+                *reinterpret_cast<int4 *>(indices + numel + gi) = make_int4(i1[0], i1[1], i1[2], i1[3]);
+                *reinterpret_cast<int4 *>(indices + 2 * numel + gi) = make_int4(i2[0], i2[1], i2[2], i2[3]);
+            }
+        }
+    }
+}
+
+// The offset table lives in constant memory: upload it once per device.
+int upload_shell_table() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    TM_CHECK_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(TM_ERR_UNSUPPORTED, "device index %d", dev);
+    std::lock_guard<std::mutex> lock(mu);
+    if (done[dev]) return TM_OK;
+    int status = TM_OK;
+    {
+        std::vector<std::array<int, 4>> v;  // (d2, dx, dy, dz)
+        for (int dz = -kShellR; dz <= kShellR; dz++)
+            for (int dy = -kShellR; dy <= kShellR; dy++)
+                for (int dx = -kShellR; dx <= kShellR; dx++) {
+                    const int d2 = dz * dz + dy * dy + dx * dx;
+                    if (d2 <= kShellD2) v.push_back({d2, dx, dy, dz});
+                }
+        std::sort(v.begin(), v.end());
+        uint32_t packed[kShellN];
+        for (int t = 0; t < kShellN; t++)
+            packed[t] = (uint32_t)(v[t][3] + 8) | ((uint32_t)(v[t][2] + 8) << 4) | ((uint32_t)(v[t][1] + 8) << 8) |
+                        ((uint32_t)v[t][0] << 12);
+        status = (int)v.size() == kShellN ? cuda_check(cudaMemcpyToSymbol(c_shell, packed, sizeof(packed)),
+                                                          "cudaMemcpyToSymbol(c_shell)")
+                                          : fail(TM_ERR_UNSUPPORTED, "shell table size mismatch");
+    }
+    if (status == TM_OK) done[dev] = true;
+    return status;
+}
+
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 }  // namespace
@@ -690,6 +1411,51 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
     int16_t *c1 = reinterpret_cast<int16_t *>(ws);
     int32_t *c2 = g.ndim == 3 ? reinterpret_cast<int32_t *>(ws + align256(n * 2)) : nullptr;
     int16_t *stack1 = g.ndim == 3 ? reinterpret_cast<int16_t *>(ws + align256(n * 2) + align256(n * 4)) : nullptr;
+    const bool fused = g.ndim == 3 && p.L0 <= 254 && p.L1 <= 254 && (p.L2 % 4) == 0 && ((uintptr_t)dist & 15) == 0 &&
+                       ((uintptr_t)indices & 15) == 0 && ((uintptr_t)sqdist & 15) == 0 && (g.numel % 4) == 0 &&
+                       c12_smem(p.L1, p.L2).total <= 200 * 1024;
+    // dense backgrounds: shell search first; the separable passes then run only
+    // for the items it could not finish (todo flags).  The (f0, f1) plane of
+    // the unfused pass 1 is unused on this path and holds the bitmap + flags.
+    int *todo = nullptr;
+    if (fused && p.L2 <= 1024) {
+        int st = upload_shell_table();
+        if (st != TM_OK) return st;
+        const int ww = (p.L2 + 31) / 32;
+        const int64_t nwords = g.batch * (int64_t)p.L0 * p.L1 * ww;
+        uint32_t *bm = reinterpret_cast<uint32_t *>(c2);
+        todo = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(c2) + align256((size_t)nwords * 4));
+        TM_CHECK_CUDA(cudaMemsetAsync(todo, 0, (size_t)g.batch * sizeof(int), stream));
+        const unsigned bblocks = (unsigned)std::min<int64_t>(ceil_div(nwords, 256), (int64_t)sm_count() * 16);
+        const bool vrow = (p.L2 % 32) == 0 && ((uintptr_t)input & 15) == 0;
+        if (in_dtype == TM_F32) {
+            const float *in = static_cast<const float *>(input);
+            if (vrow) edt_bitmap_kernel<float, true><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
+            else edt_bitmap_kernel<float, false><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
+        } else {
+            const uint8_t *in = static_cast<const uint8_t *>(input);
+            if (vrow) edt_bitmap_kernel<uint8_t, true><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
+            else edt_bitmap_kernel<uint8_t, false><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
+        }
+        TM_LAUNCH_CHECK("edt_bitmap_kernel");
+        const ShellSmem sm = shell_smem(p.L2);
+        const int64_t sblocks = g.batch * (int64_t)p.L0 * ceil_div(p.L1, kShellRows);
+        if (sblocks >= ((int64_t)1 << 31)) return fail(TM_ERR_TOO_LARGE, "too many blocks");
+        if (ww == 4) {
+            edt_shell_ct_kernel<4><<<(unsigned)sblocks, kShellThreads, 0, stream>>>(bm, dist, indices, sqdist, todo, p);
+        } else if (ww == 2) {
+            edt_shell_ct_kernel<2><<<(unsigned)sblocks, kShellThreads, 0, stream>>>(bm, dist, indices, sqdist, todo, p);
+        } else if (ww == 8) {
+            edt_shell_ct_kernel<8><<<(unsigned)sblocks, kShellThreads, 0, stream>>>(bm, dist, indices, sqdist, todo, p);
+        } else {
+            if (sm.total > 48 * 1024)
+                TM_CHECK_CUDA(cudaFuncSetAttribute(edt_shell_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)sm.total));
+            edt_shell_kernel<<<(unsigned)sblocks, kShellThreads, sm.total, stream>>>(bm, dist, indices, sqdist, todo,
+                                                                                    p);
+        }
+        TM_LAUNCH_CHECK("edt_shell_kernel");
+    }
     // pass 0
     const int64_t inner0 = g.numel_item / g.shape[0];
     if (p.L0 <= kMaxL0Smem) {
@@ -704,10 +1470,10 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
         }
         if (in_dtype == TM_F32)
             edt_c0_smem_kernel<float><<<(unsigned)blocks, kCols * kSegs, smem, stream>>>(
-                static_cast<const float *>(input), c1, p);
+                static_cast<const float *>(input), c1, p, todo);
         else
             edt_c0_smem_kernel<uint8_t><<<(unsigned)blocks, kCols * kSegs, smem, stream>>>(
-                static_cast<const uint8_t *>(input), c1, p);
+                static_cast<const uint8_t *>(input), c1, p, todo);
         TM_LAUNCH_CHECK("edt_c0_smem_kernel");
     } else {
         const int64_t nlines0 = g.batch * inner0;
@@ -717,6 +1483,18 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
         else
             edt_c0_kernel<uint8_t><<<b0, 128, 0, stream>>>(static_cast<const uint8_t *>(input), c1, p);
         TM_LAUNCH_CHECK("edt_c0_kernel");
+    }
+    // passes 1 + 2 fused per plane when the plane fits on chip
+    if (fused) {
+        const size_t smem = c12_smem(p.L1, p.L2).total;
+        const int64_t blocks = g.batch * (int64_t)p.L0;
+        if (blocks >= ((int64_t)1 << 31)) return fail(TM_ERR_TOO_LARGE, "too many blocks");
+        if (smem > 48 * 1024)
+            TM_CHECK_CUDA(cudaFuncSetAttribute(edt_c12_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)smem));
+        edt_c12_kernel<<<(unsigned)blocks, kC12Threads, smem, stream>>>(c1, dist, indices, sqdist, stack1, p, todo);
+        TM_LAUNCH_CHECK("edt_c12_kernel");
+        return TM_OK;
     }
     // pass 1 (3-D)
     if (g.ndim == 3) {
