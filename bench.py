@@ -219,9 +219,9 @@ def bench_ours(args, rank, world):
                      "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
                      "peak_kind": peak_kind,
                      "traffic": load_traffic("edt"),
-                     "scope": "whole EDT op (3 kernels: axis-0 scan + 2 envelope passes), "
-                              "17 algorithmic B/voxel"},
-        "gpu_launches": 3 * args.steps,
+                     "scope": "whole EDT op (background bitmap + shell search; the separable passes "
+                              "launch and exit for items the search finished), 17 algorithmic B/voxel"},
+        "gpu_launches": 4 * args.steps,
         "clocks": clk.summary(),
         "secondary": extra,
     }
