@@ -12,6 +12,7 @@ from scipy import ndimage as ndi
 
 import oracle
 import torchmorph_gb300 as tm
+from torchmorph_gb300 import _C
 from tests.helpers import per_item, per_item_indices, rng
 
 pytestmark = pytest.mark.gpu
@@ -208,3 +209,29 @@ def test_edt_vector_path_and_offset_outputs(cuda):
     tm.euclidean_distance_transform(_t(x), distances=dbuf, indices=ibuf)
     np.testing.assert_array_equal(dbuf.cpu().numpy(), od.astype(np.float32))
     np.testing.assert_array_equal(ibuf.cpu().numpy(), oi)
+
+
+@pytest.mark.parametrize("metric", ["chessboard", "taxicab", "chamfer345"])
+@pytest.mark.parametrize("shape,p", [((2, 1, 20, 33, 128), 0.9), ((1, 2, 9, 40, 100), 0.85),
+                                     ((3, 1, 12, 16, 128), 0.999)])
+def test_chamfer_distances_bitmap_path_vs_raster(cuda, metric, shape, p):
+    """Distances-only calls on 3-D items with 97..128-voxel rows go through the bitmap
+    shell search; items it cannot finish (sparse backgrounds) fall back per item.  The
+    result must equal the raster passes (indices requested) and, for the scipy metrics,
+    scipy itself."""
+    r = rng(hash((metric, shape)) % 2**31)
+    x = r.random(shape) < p
+    if shape[0] == 3:
+        x[1] = True          # one item without background: -1 everywhere
+        x[2] = r.random(shape[2:]) < 0.9  # one dense item next to a sparse one
+    t = torch.from_numpy(x).cuda()
+    d_fast, _ = _C.cdt(t, metric, True, False)
+    d_ref, _ = _C.cdt(t, metric, True, True)
+    np.testing.assert_array_equal(d_fast.cpu().numpy(), d_ref.cpu().numpy())
+    d_o, _ = oracle.cdt(x, metric)
+    if metric == "chamfer345":  # the oracle counts thirds
+        d_o = np.where(d_o < 0, -1.0, d_o.astype(np.float32) / np.float32(3.0)).astype(np.float32)
+    np.testing.assert_array_equal(d_fast.cpu().numpy(), d_o)
+    if metric != "chamfer345" and shape[0] != 3:
+        exp = per_item(x, ndi.distance_transform_cdt, metric=metric).astype(np.float32)
+        np.testing.assert_array_equal(d_fast.cpu().numpy(), exp)

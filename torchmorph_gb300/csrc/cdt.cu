@@ -23,6 +23,7 @@
 #include <cstring>
 #include <vector>
 
+#include "edt_internal.cuh"
 #include "tm_common.cuh"
 
 namespace tmc {
@@ -111,11 +112,14 @@ __global__ void cdt_scatter_kernel(const int *__restrict__ off, int *__restrict_
     }
 }
 
+// todo (optional): 1 for the items the raster passes must compute; the
+// others were finished by the bitmap shell search and are left alone.
 template <typename In>
 __global__ void cdt_init_kernel(const In *__restrict__ in, int32_t *__restrict__ dt, int32_t *__restrict__ ft,
-                                int64_t numel, int64_t numel_item) {
+                                int64_t numel, int64_t numel_item, const int *__restrict__ todo) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < numel;
          i += (int64_t)gridDim.x * blockDim.x) {
+        if (todo && !todo[i / numel_item]) continue;
         dt[i] = in[i] != (In)0 ? -1 : 0;
         ft[i] = (int32_t)(i % numel_item);
     }
@@ -134,12 +138,13 @@ template <bool BACKWARD>
 __global__ void __launch_bounds__(kCdtThreads) cdt_pass_kernel(int32_t *__restrict__ dt, int32_t *__restrict__ ft,
                                                                const int *__restrict__ order,
                                                                const int *__restrict__ woff, CdtParams p,
-                                                               CdtOffsets offs) {
+                                                               CdtOffsets offs, const int *__restrict__ todo) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
     const int nd = p.ndim;
     const int sgn = BACKWARD ? -1 : 1;
     for (int64_t item = blockIdx.x; item < p.batch; item += gridDim.x) {
+        if (todo && !todo[item]) continue;  // uniform per block
         int32_t *D = dt + item * p.numel_item;
         int32_t *F = ft + item * p.numel_item;
         for (int step = 0; step < p.T; step++) {
@@ -233,9 +238,11 @@ __global__ void __launch_bounds__(kCdtThreads) cdt_pass_kernel(int32_t *__restri
 
 __global__ void cdt_finalize_kernel(const int32_t *__restrict__ dt, const int32_t *__restrict__ ft,
                                     float *__restrict__ dist, int32_t *__restrict__ indices, int64_t numel,
-                                    int64_t numel_item, int ndim, CdtParams p, float divisor) {
+                                    int64_t numel_item, int ndim, CdtParams p, float divisor,
+                                    const int *__restrict__ todo) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < numel;
          i += (int64_t)gridDim.x * blockDim.x) {
+        if (todo && !todo[i / numel_item]) continue;
         const int v = dt[i];
         if (dist) dist[i] = v < 0 ? -1.0f : (float)v / divisor;
         if (indices) {
@@ -281,7 +288,7 @@ CdtPlan plan_cdt(const Geometry &g) {
 
 template <typename In>
 int run_cdt(const In *in, const Geometry &g, int metric, float *dist, int32_t *indices, unsigned char *ws,
-            const CdtPlan &pl, cudaStream_t stream) {
+            const CdtPlan &pl, const int *todo, cudaStream_t stream) {
     const int nd = g.ndim;
     CdtParams p;
     std::memset(&p, 0, sizeof(p));
@@ -337,15 +344,15 @@ int run_cdt(const In *in, const Geometry &g, int metric, float *dist, int32_t *i
     cdt_scatter_kernel<<<rb, 256, 0, stream>>>(woff, cur, order, p);
     TM_LAUNCH_CHECK("cdt_scatter_kernel");
     unsigned eb = (unsigned)std::min<int64_t>(ceil_div(g.numel, 256), (int64_t)sms * 16);
-    cdt_init_kernel<In><<<eb, 256, 0, stream>>>(in, dt, ft, g.numel, g.numel_item);
+    cdt_init_kernel<In><<<eb, 256, 0, stream>>>(in, dt, ft, g.numel, g.numel_item, todo);
     TM_LAUNCH_CHECK("cdt_init_kernel");
     unsigned ib = (unsigned)std::min<int64_t>(g.batch, (int64_t)1 << 20);
-    cdt_pass_kernel<false><<<ib, kCdtThreads, 0, stream>>>(dt, ft, order, woff, p, local);
+    cdt_pass_kernel<false><<<ib, kCdtThreads, 0, stream>>>(dt, ft, order, woff, p, local, todo);
     TM_LAUNCH_CHECK("cdt_pass_kernel<forward>");
-    cdt_pass_kernel<true><<<ib, kCdtThreads, 0, stream>>>(dt, ft, order, woff, p, local);
+    cdt_pass_kernel<true><<<ib, kCdtThreads, 0, stream>>>(dt, ft, order, woff, p, local, todo);
     TM_LAUNCH_CHECK("cdt_pass_kernel<backward>");
     cdt_finalize_kernel<<<eb, 256, 0, stream>>>(dt, ft, dist, indices, g.numel, g.numel_item, nd, p,
-                                                metric == TM_CDT_CHAMFER345 ? 3.0f : 1.0f);
+                                                metric == TM_CDT_CHAMFER345 ? 3.0f : 1.0f, todo);
     TM_LAUNCH_CHECK("cdt_finalize_kernel");
     return TM_OK;
 }
@@ -353,10 +360,17 @@ int run_cdt(const In *in, const Geometry &g, int metric, float *dist, int32_t *i
 }  // namespace
 }  // namespace tmc
 
+// Distances without indices of 3-D items with 128-wide rows first go
+// through the bitmap shell search (edt_compact.cu); its workspace follows
+// the raster passes' one.
+static bool cdt_shell_shape(const tmc::Geometry &g) { return g.ndim == 3 && (g.shape[2] + 31) / 32 == 4 && g.shape[2] % 4 == 0; }
+
 extern "C" size_t tm_cdt_workspace_size(int64_t batch, int ndim, const int64_t *shape) {
     tmc::Geometry g;
     if (tmc::make_geometry(batch, ndim, shape, &g) != TM_OK) return 0;
-    return tmc::plan_cdt(g).total;
+    size_t n = tmc::plan_cdt(g).total;
+    if (cdt_shell_shape(g)) n += tmc::cdt_shell_workspace(g);
+    return n;
 }
 
 extern "C" int tm_cdt(const void *input, int in_dtype, int64_t batch, int ndim, const int64_t *shape, int metric,
@@ -374,10 +388,16 @@ extern "C" int tm_cdt(const void *input, int in_dtype, int64_t batch, int ndim, 
         return fail(TM_ERR_INVALID_ARGUMENT, "At least one of return_distances or return_indices must be True");
     if (g.numel_item >= ((int64_t)1 << 31)) return fail(TM_ERR_TOO_LARGE, "items of 2^31 or more voxels are not supported");
     CdtPlan pl = plan_cdt(g);
-    if (!workspace || workspace_bytes < pl.total)
-        return fail(TM_ERR_WORKSPACE, "workspace of %zu bytes required, got %zu", pl.total, workspace_bytes);
+    const size_t need = pl.total + (cdt_shell_shape(g) ? cdt_shell_workspace(g) : 0);
+    if (!workspace || workspace_bytes < need)
+        return fail(TM_ERR_WORKSPACE, "workspace of %zu bytes required, got %zu", need, workspace_bytes);
     unsigned char *ws = static_cast<unsigned char *>(workspace);
     cudaStream_t s = (cudaStream_t)stream;
-    if (in_dtype == TM_F32) return run_cdt<float>((const float *)input, g, metric, dist, indices, ws, pl, s);
-    return run_cdt<uint8_t>((const uint8_t *)input, g, metric, dist, indices, ws, pl, s);
+    int *todo = nullptr;
+    if (cdt_shell_shape(g) && cdt_shell_eligible(g, dist, indices)) {
+        st = cdt_shell_run(input, in_dtype, g, metric, dist, ws + pl.total, &todo, s);
+        if (st != TM_OK) return st;
+    }
+    if (in_dtype == TM_F32) return run_cdt<float>((const float *)input, g, metric, dist, indices, ws, pl, todo, s);
+    return run_cdt<uint8_t>((const uint8_t *)input, g, metric, dist, indices, ws, pl, todo, s);
 }

@@ -1220,16 +1220,21 @@ __global__ void __launch_bounds__(kShellThreads) edt_shell_ct_kernel(const uint3
     __shared__ int s_unresolved;
     const int L0 = p.L0, L1 = p.L1, W = p.L2;
     const int ybl = (L1 + kShellRows - 1) / kShellRows;
-    const int64_t item = blockIdx.x / ((int64_t)L0 * ybl);
-    const int rem = (int)(blockIdx.x - item * L0 * ybl);
-    const int z = rem / ybl, y0 = (rem % ybl) * kShellRows;
-    const int nrows = min(kShellRows, L1 - y0);
+    const int64_t nunits = p.batch * (int64_t)L0 * ybl;
     const int tid = threadIdx.x;
-    if (tid == 0) s_unresolved = 0;
     for (int t = tid; t < kShellN; t += kShellThreads) {
         const uint32_t c = c_shell[t];
         tab2[t] = make_int2((int)c, __float_as_int(__fsqrt_rn((float)(c >> 12))));
     }
+    // persistent: a CTA takes units blockIdx.x, +gridDim.x, ...; the stores of
+    // one unit drain while the next unit is staged and searched
+    for (int64_t unit = blockIdx.x; unit < nunits; unit += gridDim.x) {
+    const int64_t item = unit / ((int64_t)L0 * ybl);
+    const int rem = (int)(unit - item * L0 * ybl);
+    const int z = rem / ybl, y0 = (rem % ybl) * kShellRows;
+    const int nrows = min(kShellRows, L1 - y0);
+    __syncthreads();  // the previous unit's shared-memory reads are done
+    if (tid == 0) s_unresolved = 0;
     const uint32_t *ibm = bm + item * (int64_t)L0 * L1 * WW;
     for (int i = tid; i < (2 * kShellR + 1) * kRowsP; i += kShellThreads) {
         const int k = i / kRowsP, r = i - k * kRowsP;
@@ -1306,7 +1311,7 @@ __global__ void __launch_bounds__(kShellThreads) edt_shell_ct_kernel(const uint3
     __syncthreads();
     if (s_unresolved) {
         if (tid == 0) atomicExch(&todo[item], 1);
-        return;
+        continue;
     }
     const int64_t numel = p.numel;
     const int64_t rowbase = item * p.numel_item + ((int64_t)z * L1 + y0) * W;
@@ -1337,6 +1342,7 @@ __global__ void __launch_bounds__(kShellThreads) edt_shell_ct_kernel(const uint3
                 *reinterpret_cast<int4 *>(indices + 2 * numel + gi) = make_int4(i2[0], i2[1], i2[2], i2[3]);
             }
         }
+    }
     }
 }
 
@@ -1369,6 +1375,146 @@ int upload_shell_table() {
     }
     if (status == TM_OK) done[dev] = true;
     return status;
+}
+
+// ------------------------------------------------- chamfer, distances only
+// The chamfer distances of scipy's two-pass raster transform are the
+// minimum over background voxels b of a norm of (voxel - b) (monotone
+// paths stay inside the box): chessboard max|d|, taxicab sum|d|, 3-4-5
+// 3a + b + c for |d| sorted a >= b >= c (in thirds).  For distances only,
+// the offsets of the radius-4 cube with norm <= kCdtVmax(metric) are grouped
+// by norm; per 32-voxel word the union of a class's shifted background
+// masks resolves every voxel whose nearest background has that norm.
+// Unresolved voxels mark their item for the raster passes.
+__host__ __device__ constexpr int cdt_norm(int metric, int dz, int dy, int dx) {
+    int a = dz < 0 ? -dz : dz, b = dy < 0 ? -dy : dy, c = dx < 0 ? -dx : dx;
+    if (metric == 0) return a > b ? (a > c ? a : c) : (b > c ? b : c);  // chessboard
+    if (metric == 1) return a + b + c;                                   // taxicab
+    // 3-4-5: sort descending
+    if (a < b) { int t = a; a = b; b = t; }
+    if (b < c) { int t = b; b = c; c = t; }
+    if (a < b) { int t = a; a = b; b = t; }
+    return 3 * a + b + c;
+}
+
+__host__ __device__ constexpr int cdt_vmax(int metric) { return metric == 2 ? 12 : 4; }
+
+constexpr int kCdtShellMax = 729;
+
+struct CdtShellList {
+    int n;
+    int nclass;
+    int cls_value[64];
+    int cls_begin[65];
+    ShellOff o[kCdtShellMax];
+};
+
+__host__ __device__ constexpr CdtShellList make_cdt_list(int metric) {
+    CdtShellList l{};
+    const int vmax = cdt_vmax(metric);
+    int n = 0, nc = 0;
+    for (int v = 0; v <= vmax; v++) {
+        bool any = false;
+        for (int dz = -kShellR; dz <= kShellR; dz++)
+            for (int dy = -kShellR; dy <= kShellR; dy++)
+                for (int dx = -kShellR; dx <= kShellR; dx++)
+                    if (cdt_norm(metric, dz, dy, dx) == v) {
+                        if (!any) {
+                            l.cls_value[nc] = v;
+                            l.cls_begin[nc] = n;
+                            nc++;
+                            any = true;
+                        }
+                        l.o[n++] = ShellOff{dz, dy, dx, v};
+                    }
+    }
+    l.n = n;
+    l.nclass = nc;
+    l.cls_begin[nc] = n;
+    return l;
+}
+
+template <int WW, int MET>
+__global__ void __launch_bounds__(kShellThreads) cdt_shell_kernel(const uint32_t *__restrict__ bm,
+                                                                  float *__restrict__ dist, int *__restrict__ todo,
+                                                                  CompactParams p, float divisor) {
+    constexpr CdtShellList kL = make_cdt_list(MET);
+    constexpr int kPitch = WW + 2 * kShellPadW;
+    constexpr int kRowsP = kShellRows + 2 * kShellR;
+    constexpr int kPlaneP = kRowsP * kPitch;
+    __shared__ __align__(16) uint32_t bits[(2 * kShellR + 1) * kPlaneP];
+    __shared__ __align__(16) uint8_t res[kShellRows * WW * 32];
+    __shared__ int s_unresolved;
+    const int L0 = p.L0, L1 = p.L1, W = p.L2;
+    const int ybl = (L1 + kShellRows - 1) / kShellRows;
+    const int64_t item = blockIdx.x / ((int64_t)L0 * ybl);
+    const int rem = (int)(blockIdx.x - item * L0 * ybl);
+    const int z = rem / ybl, y0 = (rem % ybl) * kShellRows;
+    const int nrows = min(kShellRows, L1 - y0);
+    const int tid = threadIdx.x;
+    if (tid == 0) s_unresolved = 0;
+    const uint32_t *ibm = bm + item * (int64_t)L0 * L1 * WW;
+    for (int i = tid; i < (2 * kShellR + 1) * kRowsP; i += kShellThreads) {
+        const int k = i / kRowsP, r = i - k * kRowsP;
+        const int zz = z - kShellR + k, yy = y0 - kShellR + r;
+        uint32_t *dst = bits + k * kPlaneP + r * kPitch;
+        const bool in_item = (unsigned)zz < (unsigned)L0 && (unsigned)yy < (unsigned)L1;
+        const uint32_t *src = ibm + ((int64_t)zz * L1 + yy) * WW;
+        dst[0] = 0u;
+        dst[kShellPadW + WW] = 0u;
+#pragma unroll
+        for (int c = 0; c < WW; c++) dst[kShellPadW + c] = in_item ? src[c] : 0u;
+    }
+    __syncthreads();
+    for (int e = tid; e < nrows * WW; e += kShellThreads) {
+        const int r = e / WW, wi = e % WW;
+        const int nb = min(32, W - 32 * wi);
+        uint32_t U = nb == 32 ? 0xffffffffu : ((1u << nb) - 1u);
+        const uint32_t *here = bits + kShellR * kPlaneP + (kShellR + r) * kPitch + kShellPadW + wi;
+        uint8_t *out = res + r * W + 32 * wi;
+        // one straight-line pass over the offsets (norm order); at the end of
+        // each norm class the class's union resolves the voxels it covers
+        uint32_t H = 0;
+#pragma unroll
+        for (int t = 0; t < kL.n; t++) {
+            const int delta = kL.o[t].dz * kPlaneP + kL.o[t].dy * kPitch + (kL.o[t].dx >= 0 ? 0 : -1);
+            const int sh = kL.o[t].dx >= 0 ? kL.o[t].dx : 32 + kL.o[t].dx;
+            H |= __funnelshift_r(here[delta], here[delta + 1], sh);
+            if (t + 1 == kL.n || kL.o[t + 1].d2 != kL.o[t].d2) {
+                uint32_t hit = H & U;
+                U &= ~hit;
+                while (hit) {
+                    const int b = __ffs(hit) - 1;
+                    out[b] = (uint8_t)kL.o[t].d2;
+                    hit &= hit - 1;
+                }
+                H = 0;
+                if (U == 0u) break;
+            }
+        }
+        if (U) s_unresolved = 1;
+    }
+    __syncthreads();
+    if (s_unresolved) {
+        if (tid == 0) atomicExch(&todo[item], 1);
+        return;
+    }
+    const int64_t rowbase = item * p.numel_item + ((int64_t)z * L1 + y0) * W;
+    const float inv = 1.0f / divisor;
+    const int warp = tid >> 5, lane = tid & 31;
+    for (int r = warp; r < nrows; r += kShellThreads / 32) {
+        for (int x = 4 * lane; x < W; x += 128) {
+            const uint32_t v4 = *reinterpret_cast<const uint32_t *>(res + r * W + x);
+            float4 d;
+            // divisor 3 (3-4-5): correctly rounded v / 3 as the raster path computes it
+            d.x = divisor == 1.f ? (float)(v4 & 255u) : (float)(v4 & 255u) / divisor;
+            d.y = divisor == 1.f ? (float)((v4 >> 8) & 255u) : (float)((v4 >> 8) & 255u) / divisor;
+            d.z = divisor == 1.f ? (float)((v4 >> 16) & 255u) : (float)((v4 >> 16) & 255u) / divisor;
+            d.w = divisor == 1.f ? (float)(v4 >> 24) : (float)(v4 >> 24) / divisor;
+            (void)inv;
+            *reinterpret_cast<float4 *>(dist + rowbase + (int64_t)r * W + x) = d;
+        }
+    }
 }
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -1441,12 +1587,25 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
         const ShellSmem sm = shell_smem(p.L2);
         const int64_t sblocks = g.batch * (int64_t)p.L0 * ceil_div(p.L1, kShellRows);
         if (sblocks >= ((int64_t)1 << 31)) return fail(TM_ERR_TOO_LARGE, "too many blocks");
-        if (ww == 4) {
-            edt_shell_ct_kernel<4><<<(unsigned)sblocks, kShellThreads, 0, stream>>>(bm, dist, indices, sqdist, todo, p);
-        } else if (ww == 2) {
-            edt_shell_ct_kernel<2><<<(unsigned)sblocks, kShellThreads, 0, stream>>>(bm, dist, indices, sqdist, todo, p);
-        } else if (ww == 8) {
-            edt_shell_ct_kernel<8><<<(unsigned)sblocks, kShellThreads, 0, stream>>>(bm, dist, indices, sqdist, todo, p);
+        auto launch_ct = [&](auto kernel) -> int {
+            static thread_local int cached_dev = -1, cached_ctas = 0;
+            static thread_local const void *cached_fn = nullptr;
+            int dev = 0;
+            TM_CHECK_CUDA(cudaGetDevice(&dev));
+            if (cached_dev != dev || cached_fn != (const void *)kernel) {
+                int per_sm = 0;
+                TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kShellThreads, 0));
+                cached_ctas = (per_sm < 1 ? 1 : per_sm) * sm_count();
+                cached_dev = dev;
+                cached_fn = (const void *)kernel;
+            }
+            // about two units per CTA, so consecutive units of a CTA overlap
+            const int64_t grid = std::min<int64_t>(cached_ctas, (sblocks + 1) / 2);
+            kernel<<<(unsigned)grid, kShellThreads, 0, stream>>>(bm, dist, indices, sqdist, todo, p);
+            return TM_OK;
+        };
+        if (ww == 4) {  // rows of 97..128 voxels: straight-line search
+            if ((st = launch_ct(edt_shell_ct_kernel<4>)) != TM_OK) return st;
         } else {
             if (sm.total > 48 * 1024)
                 TM_CHECK_CUDA(cudaFuncSetAttribute(edt_shell_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1530,6 +1689,60 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
         st = vec ? launch2(edt_c2_kernel<false, true>, c1) : launch2(edt_c2_kernel<false, false>, c1);
     if (st != TM_OK) return st;
     TM_LAUNCH_CHECK("edt_c2_kernel");
+    return TM_OK;
+}
+
+
+bool cdt_shell_eligible(const Geometry &g, const float *dist, const int32_t *indices) {
+    if (g.ndim != 3 || indices || !dist) return false;
+    const int64_t L0 = g.shape[0], L1 = g.shape[1], L2 = g.shape[2];
+    const int ww = (int)((L2 + 31) / 32);
+    return (L2 % 4) == 0 && ((uintptr_t)dist & 15) == 0 && ww == 4 && L0 < 32768 && L1 < 32768 &&
+           g.numel_item < ((int64_t)1 << 31);
+}
+
+size_t cdt_shell_workspace(const Geometry &g) {
+    const int ww = (int)((g.shape[2] + 31) / 32);
+    return align256((size_t)g.batch * g.shape[0] * g.shape[1] * ww * 4) + align256((size_t)g.batch * 4);
+}
+
+int cdt_shell_run(const void *input, int in_dtype, const Geometry &g, int metric, float *dist, unsigned char *ws,
+                  int **todo_out, cudaStream_t stream) {
+    CompactParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.ndim = 3;
+    p.L0 = (int)g.shape[0];
+    p.L1 = (int)g.shape[1];
+    p.L2 = (int)g.shape[2];
+    p.batch = g.batch;
+    p.numel = g.numel;
+    p.numel_item = g.numel_item;
+    const int ww = (p.L2 + 31) / 32;
+    const int64_t nwords = g.batch * (int64_t)p.L0 * p.L1 * ww;
+    uint32_t *bm = reinterpret_cast<uint32_t *>(ws);
+    int *todo = reinterpret_cast<int *>(ws + align256((size_t)nwords * 4));
+    TM_CHECK_CUDA(cudaMemsetAsync(todo, 0, (size_t)g.batch * sizeof(int), stream));
+    const unsigned bblocks = (unsigned)std::min<int64_t>(ceil_div(nwords, 256), (int64_t)sm_count() * 16);
+    const bool vrow = (p.L2 % 32) == 0 && ((uintptr_t)input & 15) == 0;
+    if (in_dtype == TM_F32) {
+        const float *in = static_cast<const float *>(input);
+        if (vrow) edt_bitmap_kernel<float, true><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
+        else edt_bitmap_kernel<float, false><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
+    } else {
+        const uint8_t *in = static_cast<const uint8_t *>(input);
+        if (vrow) edt_bitmap_kernel<uint8_t, true><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
+        else edt_bitmap_kernel<uint8_t, false><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
+    }
+    TM_LAUNCH_CHECK("edt_bitmap_kernel");
+    const int64_t blocks = g.batch * (int64_t)p.L0 * ceil_div(p.L1, kShellRows);
+    if (blocks >= ((int64_t)1 << 31)) return fail(TM_ERR_TOO_LARGE, "too many blocks");
+    const float div = metric == TM_CDT_CHAMFER345 ? 3.0f : 1.0f;
+    auto go = [&](auto kernel) { kernel<<<(unsigned)blocks, kShellThreads, 0, stream>>>(bm, dist, todo, p, div); };
+    if (metric == TM_CDT_CHESSBOARD) go(cdt_shell_kernel<4, 0>);
+    else if (metric == TM_CDT_TAXICAB) go(cdt_shell_kernel<4, 1>);
+    else go(cdt_shell_kernel<4, 2>);
+    TM_LAUNCH_CHECK("cdt_shell_kernel");
+    *todo_out = todo;
     return TM_OK;
 }
 
