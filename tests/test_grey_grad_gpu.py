@@ -15,7 +15,11 @@ pytestmark = pytest.mark.gpu
 MODES = ["reflect", "constant", "nearest", "mirror", "wrap"]
 CASES = [((2, 1, 37, 53), (3, 3), (0, 0)), ((1, 2, 20, 9), (4, 5), (-1, 2)),
          ((1, 1, 11, 12, 13), (3, 3, 3), (0, 0, 0)), ((2, 1, 40), (7,), (-3,)),
-         ((1, 1, 3, 2), (5, 5), (0, 0)), ((1, 1, 64, 64), (15, 15), (0, 0))]
+         ((1, 1, 3, 2), (5, 5), (0, 0)), ((1, 1, 64, 64), (15, 15), (0, 0)),
+         # 2-D tiled kernels (128 x 32 tiles): interior and border tiles, a shifted
+         # origin, the widest tap extent they take (31) and a 2-D case they do not (33)
+         ((1, 2, 150, 420), (3, 3), (0, 0)), ((2, 1, 131, 300), (9, 7), (2, -1)),
+         ((1, 1, 100, 330), (1, 31), (0, 3)), ((1, 1, 70, 290), (33, 1), (0, 0))]
 
 
 def _element(ssize, seed, flat):

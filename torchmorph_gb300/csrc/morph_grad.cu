@@ -16,6 +16,7 @@
 // point; nearest: a run at the edges; constant: j itself -- constant-border
 // reads never route a gradient).  Interior voxels take a fast path over flat
 // offsets.  Sums run in tap order, then coordinate order.
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -109,16 +110,26 @@ __device__ __forceinline__ int pmod(int a, int m) {
 }
 
 // Coordinates y' in [lo, hi] (hi - lo + 1 == n) with map_coord(y') == c, as
-// up to two ranges r[0..1], r[2..3]; returns the number of ranges.
-__device__ __forceinline__ int preimage_ranges(int c, int n, int mode, int lo, int hi, int *r) {
-    int cnt = 0;
+// up to two ranges [a0, b0], [a1, b1] (an unused range has b < a).
+struct Ranges {
+    int a0, b0, a1, b1;
+    __device__ __forceinline__ bool empty() const { return b0 < a0; }
+    __device__ __forceinline__ int lo(int i) const { return i ? a1 : a0; }
+    __device__ __forceinline__ int hi(int i) const { return i ? b1 : b0; }
+};
+
+__device__ __forceinline__ Ranges preimage_ranges(int c, int n, int mode, int lo, int hi) {
+    Ranges r{0, -1, 0, -1};
     auto add = [&](int a, int b) {
         a = a > lo ? a : lo;
         b = b < hi ? b : hi;
-        if (a <= b) {
-            r[2 * cnt] = a;
-            r[2 * cnt + 1] = b;
-            cnt++;
+        if (a > b) return;
+        if (r.b0 < r.a0) {
+            r.a0 = a;
+            r.b0 = b;
+        } else {
+            r.a1 = a;
+            r.b1 = b;
         }
     };
     switch (mode) {
@@ -155,7 +166,75 @@ __device__ __forceinline__ int preimage_ranges(int c, int n, int mode, int lo, i
         add(c, c);
         break;
     }
-    return cnt;
+    return r;
+}
+
+// grad_in of voxel sp (coordinates c) of one item: gather over taps and
+// the coordinates' border preimages.
+__device__ __forceinline__ float grad_voxel(const float *__restrict__ g, const uint8_t *__restrict__ a, int64_t sp,
+                                            const int *c, const GradParams &p, const GradTaps &taps) {
+    // interior: every tap's output o = j - off is in the image, and no
+    // out-of-image coordinate a tap can reach maps onto j (mirror maps -h
+    // onto h, hence the extra voxel)
+    bool interior = true;
+    for (int d = 0; d < p.ndim; d++) interior &= c[d] > p.halo[d] && c[d] < p.shape[d] - 1 - p.halo[d];
+    float acc = 0.f;
+    if (interior) {
+        for (int t = 0; t < p.ntaps; t++) {
+            const int64_t o = sp - taps.flat[t];
+            if (a[o] == t) acc += g[o];
+        }
+        return acc;
+    }
+    for (int t = 0; t < p.ntaps; t++) {
+        Ranges rg[kGradMaxDims];
+        bool none = false;
+        for (int d = 0; d < kGradMaxDims; d++) {
+            if (d < p.ndim) {
+                const int off = taps.off[t][d];
+                rg[d] = preimage_ranges(c[d], p.shape[d], p.mode, off, off + p.shape[d] - 1);
+                none |= rg[d].empty();
+            } else {
+                rg[d] = Ranges{0, 0, 0, -1};
+            }
+        }
+        if (none) continue;
+        for (int i0 = 0; i0 < 2; i0++)
+            for (int y0 = rg[0].lo(i0); y0 <= rg[0].hi(i0); y0++)
+                for (int i1 = 0; i1 < 2; i1++)
+                    for (int y1 = rg[1].lo(i1); y1 <= rg[1].hi(i1); y1++)
+                        for (int i2 = 0; i2 < 2; i2++)
+                            for (int y2 = rg[2].lo(i2); y2 <= rg[2].hi(i2); y2++) {
+                                const int y[3] = {y0, y1, y2};
+                                int64_t o = 0;
+                                for (int d = 0; d < p.ndim; d++) o += (int64_t)(y[d] - taps.off[t][d]) * p.stride[d];
+                                if (a[o] == t) acc += g[o];
+                            }
+    }
+    return acc;
+}
+
+// grad_voxel for a 2-D item, pixel (y, x) within the halo of the border:
+// the same sums in the same order, ranges held in registers.
+__device__ __forceinline__ float grad_pixel2d(const float *__restrict__ g, const uint8_t *__restrict__ a, int y, int x,
+                                           const GradParams &p, const GradTaps &taps) {
+    const int H = p.shape[0], W = p.shape[1];
+    float acc = 0.f;
+    for (int t = 0; t < p.ntaps; t++) {
+        const int dy = taps.off[t][0], dx = taps.off[t][1];
+        const Ranges ry = preimage_ranges(y, H, p.mode, dy, dy + H - 1);
+        const Ranges rx = preimage_ranges(x, W, p.mode, dx, dx + W - 1);
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+            for (int yy = ry.lo(i); yy <= ry.hi(i); yy++)
+#pragma unroll
+                for (int k = 0; k < 2; k++)
+                    for (int xx = rx.lo(k); xx <= rx.hi(k); xx++) {
+                        const int64_t o = (int64_t)(yy - dy) * W + (xx - dx);
+                        if (a[o] == t) acc += g[o];
+                    }
+    }
+    return acc;
 }
 
 __global__ void __launch_bounds__(kGradThreads) morph_grad_kernel(const float *__restrict__ gout,
@@ -167,52 +246,278 @@ __global__ void __launch_bounds__(kGradThreads) morph_grad_kernel(const float *_
          idx += (int64_t)gridDim.x * blockDim.x) {
         const int64_t item = idx / p.numel_item;
         const int64_t sp = idx - item * p.numel_item;
-        const float *g = gout + item * p.numel_item;
-        const uint8_t *a = arg + item * p.numel_item;
         int c[kGradMaxDims];
         coords_of(sp, p, c);
-        // interior: every tap's output o = j - off is in the image, and no
-        // out-of-image coordinate a tap can reach maps onto j (mirror maps
-        // -h onto h, hence the extra voxel)
-        bool interior = true;
-        for (int d = 0; d < p.ndim; d++) interior &= c[d] > p.halo[d] && c[d] < p.shape[d] - 1 - p.halo[d];
-        float acc = 0.f;
-        if (interior) {
-            for (int t = 0; t < p.ntaps; t++) {
-                const int64_t o = sp - taps.flat[t];
-                if (a[o] == t) acc += g[o];
+        gin[idx] = grad_voxel(gout + item * p.numel_item, arg + item * p.numel_item, sp, c, p, taps);
+    }
+}
+
+// ------------------------------------------------------------- 2-D tiles
+// 2-D items: 128 x 32 tiles, 256 threads, one column and 16 rows per
+// thread.  The forward stages the input region the tile's taps read
+// (borders mapped as in the forward operator); the backward stages
+// (grad_out, argument) of the outputs its inputs can receive from.  Both run
+// the taps in the outer loop over 16 unrolled rows, reading shared memory at
+// a per-tap offset (computed on the host for the compile-time row pitch), so
+// the per-output results and their order of evaluation are those of the
+// per-voxel kernels above.  Backward pixels within the halo of the image
+// border take grad_voxel.
+constexpr int kT2W = 128, kT2H = 32, kT2Threads = 256, kT2Rows = 16;
+constexpr int kT2MaxTaps = 64;
+constexpr int kT2MaxExt = 30;  // tap offsets span at most 31 per axis
+
+struct Taps2D {
+    int n, min_dy, min_dx, ext_y, ext_x;  // offsets span [min, min + ext] per axis
+    int soff[kT2MaxTaps];                 // shared-memory offset of tap t for row 0, column 0
+    float val[kT2MaxTaps];
+};
+
+// Staging of a region of RH x RW elements (RW <= 160): warp w takes rows
+// w, w + 8, ...; each lane issues the loads of RB rows x 5 column chunks
+// before storing any of them, so a warp keeps up to 5 RB loads in flight
+// instead of one.
+constexpr int kT2ColChunks = 5;
+
+template <int RB, class Load, class Store>
+__device__ __forceinline__ void stage_region(int RH, int RW, Load load, Store store) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int kWarps = kT2Threads / 32;
+    for (int rb = warp; rb < RH; rb += kWarps * RB) {
+        decltype(load(0, 0)) v[RB][kT2ColChunks];
+#pragma unroll
+        for (int k = 0; k < RB; k++)
+#pragma unroll
+            for (int j = 0; j < kT2ColChunks; j++) {
+                const int r = rb + kWarps * k, cc = lane + 32 * j;
+                if (r < RH && cc < RW) v[k][j] = load(r, cc);
             }
-        } else {
-            for (int t = 0; t < p.ntaps; t++) {
-                int rng[kGradMaxDims][4], nr[kGradMaxDims];
-                bool none = false;
-                for (int d = 0; d < kGradMaxDims; d++) {
-                    if (d < p.ndim) {
-                        const int off = taps.off[t][d];
-                        nr[d] = preimage_ranges(c[d], p.shape[d], p.mode, off, off + p.shape[d] - 1, rng[d]);
-                        none |= nr[d] == 0;
-                    } else {
-                        nr[d] = 1;
-                        rng[d][0] = rng[d][1] = 0;
-                    }
+#pragma unroll
+        for (int k = 0; k < RB; k++)
+#pragma unroll
+            for (int j = 0; j < kT2ColChunks; j++) {
+                const int r = rb + kWarps * k, cc = lane + 32 * j;
+                if (r < RH && cc < RW) store(r, cc, v[k][j]);
+            }
+    }
+}
+
+template <bool MAX, int P>
+__global__ void __launch_bounds__(kT2Threads, 4) morph_arg2d_kernel(const float *__restrict__ in, float *__restrict__ out,
+                                                                 uint8_t *__restrict__ arg, GradParams p,
+                                                                 const __grid_constant__ Taps2D tp) {
+    using Op = MorphOp<float, MAX>;
+    extern __shared__ __align__(16) float stile[];
+    const int H = p.shape[0], W = p.shape[1];
+    const int RH = kT2H + tp.ext_y, RW = kT2W + tp.ext_x;
+    const int x0 = blockIdx.x * kT2W, y0 = blockIdx.y * kT2H;
+    const int gy0 = y0 + tp.min_dy, gx0 = x0 + tp.min_dx;
+    const bool inner = gy0 >= 0 && gx0 >= 0 && gy0 + RH <= H && gx0 + RW <= W;
+    const int c = threadIdx.x % kT2W, r0 = (threadIdx.x / kT2W) * kT2Rows;
+    const int x = x0 + c;
+    for (int64_t item = blockIdx.z; item < p.batch; item += gridDim.z) {
+        const float *src = in + item * p.numel_item;
+        const int mode = p.mode;
+        const float cval = p.cval;
+        auto put = [&](int r, int cc, float v) { stile[r * P + cc] = v; };
+        if (inner)
+            stage_region<2>(RH, RW, [&](int r, int cc) { return src[(int64_t)(gy0 + r) * W + gx0 + cc]; }, put);
+        else
+            stage_region<1>(
+                RH, RW,
+                [&](int r, int cc) {
+                    const int my = map_coord(gy0 + r, H, mode), mx = map_coord(gx0 + cc, W, mode);
+                    return (my < 0 || mx < 0) ? cval : src[(int64_t)my * W + mx];
+                },
+                put);
+        __syncthreads();
+        float best[kT2Rows];
+        int ba[kT2Rows];
+#pragma unroll
+        for (int i = 0; i < kT2Rows; i++) {
+            best[i] = Op::identity();
+            ba[i] = kNoTap;
+        }
+        const float *base = stile + r0 * P + c;
+        for (int t = 0; t < tp.n; t++) {
+            const float *q = base + tp.soff[t];
+            const float sv = tp.val[t];
+#pragma unroll
+            for (int i = 0; i < kT2Rows; i++) {
+                const float v = Op::apply(q[i * P], sv);
+                if (MAX ? v > best[i] : v < best[i]) {
+                    best[i] = v;
+                    ba[i] = t;
                 }
-                if (none) continue;
-                for (int r0 = 0; r0 < nr[0]; r0++)
-                    for (int y0 = rng[0][2 * r0]; y0 <= rng[0][2 * r0 + 1]; y0++)
-                        for (int r1 = 0; r1 < nr[1]; r1++)
-                            for (int y1 = rng[1][2 * r1]; y1 <= rng[1][2 * r1 + 1]; y1++)
-                                for (int r2 = 0; r2 < nr[2]; r2++)
-                                    for (int y2 = rng[2][2 * r2]; y2 <= rng[2][2 * r2 + 1]; y2++) {
-                                        const int y[3] = {y0, y1, y2};
-                                        int64_t o = 0;
-                                        for (int d = 0; d < p.ndim; d++)
-                                            o += (int64_t)(y[d] - taps.off[t][d]) * p.stride[d];
-                                        if (a[o] == t) acc += g[o];
-                                    }
             }
         }
-        gin[idx] = acc;
+        if (x < W) {
+#pragma unroll
+            for (int i = 0; i < kT2Rows; i++) {
+                const int y = y0 + r0 + i;
+                if (y < H) {
+                    const int64_t o = item * p.numel_item + (int64_t)y * W + x;
+                    out[o] = best[i];
+                    arg[o] = (uint8_t)ba[i];
+                }
+            }
+        }
+        __syncthreads();
     }
+}
+
+template <int P>
+__global__ void __launch_bounds__(kT2Threads, 3) morph_grad2d_kernel(const float *__restrict__ gout,
+                                                                  const uint8_t *__restrict__ arg,
+                                                                  float *__restrict__ gin, GradParams p,
+                                                                  const __grid_constant__ GradTaps taps,
+                                                                  const __grid_constant__ Taps2D tp) {
+    extern __shared__ __align__(16) uint2 sga[];  // (grad_out bits, argument) per staged output
+    const int H = p.shape[0], W = p.shape[1];
+    // outputs o = j - off with off in [min, min + ext] per axis
+    const int RH = kT2H + tp.ext_y, RW = kT2W + tp.ext_x;
+    const int x0 = blockIdx.x * kT2W, y0 = blockIdx.y * kT2H;
+    const int oy0 = y0 - tp.min_dy - tp.ext_y, ox0 = x0 - tp.min_dx - tp.ext_x;
+    // every input of an inner tile is an interior voxel of grad_voxel
+    const bool inner = y0 > p.halo[0] && y0 + kT2H - 1 < H - 1 - p.halo[0] && x0 > p.halo[1] &&
+                       x0 + kT2W - 1 < W - 1 - p.halo[1];
+    const int c = threadIdx.x % kT2W, r0 = (threadIdx.x / kT2W) * kT2Rows;
+    const int x = x0 + c;
+    // border pixels of an outer tile (within the halo of the image border)
+    // as lists of rows and columns, so that all threads share their gathers:
+    // (border rows x all columns) + (other rows x border columns)
+    __shared__ int s_brow[kT2H], s_orow[kT2H], s_bcol[kT2W];
+    __shared__ unsigned s_cmask[kT2W / 32];
+    __shared__ int s_nb[2];
+    const int ncols = min(kT2W, W - x0);
+    int n_brow = 0, n_orow = 0, n_bcol = 0;
+    if (!inner) {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const unsigned lt = (1u << lane) - 1u;
+        if (warp == 0) {
+            const int y = y0 + lane;
+            const bool in = y < H, br = in && (y <= p.halo[0] || y >= H - 1 - p.halo[0]);
+            const unsigned mb = __ballot_sync(~0u, br), mo = __ballot_sync(~0u, in && !br);
+            if (br) s_brow[__popc(mb & lt)] = lane;
+            if (in && !br) s_orow[__popc(mo & lt)] = lane;
+            if (lane == 0) {
+                s_nb[0] = __popc(mb);
+                s_nb[1] = __popc(mo);
+            }
+        }
+        if (warp < kT2W / 32) {
+            const int xc = x0 + warp * 32 + lane;
+            const bool bc = xc < W && (xc <= p.halo[1] || xc >= W - 1 - p.halo[1]);
+            s_cmask[warp] = __ballot_sync(~0u, bc);
+        }
+        __syncthreads();
+        if (warp < kT2W / 32) {
+            int before = 0;
+            for (int w = 0; w < warp; w++) before += __popc(s_cmask[w]);
+            if ((s_cmask[warp] >> lane) & 1u) s_bcol[before + __popc(s_cmask[warp] & lt)] = warp * 32 + lane;
+        }
+        n_brow = s_nb[0];
+        n_orow = s_nb[1];
+        for (int w = 0; w < kT2W / 32; w++) n_bcol += __popc(s_cmask[w]);
+        __syncthreads();
+    }
+    for (int64_t item = blockIdx.z; item < p.batch; item += gridDim.z) {
+        const float *g = gout + item * p.numel_item;
+        const uint8_t *a = arg + item * p.numel_item;
+        auto put = [&](int r, int cc, uint2 v) { sga[r * P + cc] = v; };
+        if (inner)
+            stage_region<2>(
+                RH, RW,
+                [&](int r, int cc) {
+                    const int64_t k = (int64_t)(oy0 + r) * W + ox0 + cc;
+                    return make_uint2(__float_as_uint(g[k]), a[k]);
+                },
+                put);
+        else
+            stage_region<1>(
+                RH, RW,
+                [&](int r, int cc) {
+                    const int oy = oy0 + r, ox = ox0 + cc;
+                    // outside the image: never a match
+                    if ((unsigned)oy >= (unsigned)H || (unsigned)ox >= (unsigned)W) return make_uint2(0u, kNoTap);
+                    const int64_t k = (int64_t)oy * W + ox;
+                    return make_uint2(__float_as_uint(g[k]), a[k]);
+                },
+                put);
+        __syncthreads();
+        float acc[kT2Rows];
+#pragma unroll
+        for (int i = 0; i < kT2Rows; i++) acc[i] = 0.f;
+        const uint2 *base = sga + r0 * P + c;
+        for (int t = 0; t < tp.n; t++) {
+            const uint2 *q = base + tp.soff[t];
+#pragma unroll
+            for (int i = 0; i < kT2Rows; i++) {
+                const uint2 v = q[i * P];
+                if (v.y == (unsigned)t) acc[i] += __uint_as_float(v.x);
+            }
+        }
+        float *dst = gin + item * p.numel_item;
+        if (x < W) {
+            const bool col_edge = !inner && (x <= p.halo[1] || x >= W - 1 - p.halo[1]);
+#pragma unroll
+            for (int i = 0; i < kT2Rows; i++) {
+                const int y = y0 + r0 + i;
+                if (y < H && !(col_edge || (!inner && (y <= p.halo[0] || y >= H - 1 - p.halo[0]))))
+                    dst[(int64_t)y * W + x] = acc[i];
+            }
+        }
+        if (!inner) {
+            const int n1 = n_brow * ncols, nb = n1 + n_orow * n_bcol;
+            for (int k = threadIdx.x; k < nb; k += kT2Threads) {
+                int y, xb;
+                if (k < n1) {
+                    y = y0 + s_brow[k / ncols];
+                    xb = x0 + k % ncols;
+                } else {
+                    const int k2 = k - n1;
+                    y = y0 + s_orow[k2 / n_bcol];
+                    xb = x0 + s_bcol[k2 % n_bcol];
+                }
+                dst[(int64_t)y * W + xb] = grad_pixel2d(g, a, y, xb, p, taps);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Row pitch (in staged elements) of the 2-D kernels for a tap extent.
+int pitch2d(int ext_x) { return ext_x <= 8 ? 136 : 160; }
+
+bool make_taps2d(const GradParams &p, const GradTaps &taps, bool backward, Taps2D *tp) {
+    if (p.ndim != 2 || p.ntaps > kT2MaxTaps) return false;
+    std::memset(tp, 0, sizeof(*tp));
+    int mny = 0, mxy = 0, mnx = 0, mxx = 0;
+    for (int t = 0; t < p.ntaps; t++) {
+        mny = std::min(mny, (int)taps.off[t][0]);
+        mxy = std::max(mxy, (int)taps.off[t][0]);
+        mnx = std::min(mnx, (int)taps.off[t][1]);
+        mxx = std::max(mxx, (int)taps.off[t][1]);
+    }
+    if (mxy - mny > kT2MaxExt || mxx - mnx > kT2MaxExt) return false;
+    tp->n = p.ntaps;
+    tp->min_dy = mny;
+    tp->min_dx = mnx;
+    tp->ext_y = mxy - mny;
+    tp->ext_x = mxx - mnx;
+    const int P = pitch2d(tp->ext_x);
+    for (int t = 0; t < p.ntaps; t++) {
+        const int dy = taps.off[t][0], dx = taps.off[t][1];
+        // forward: input j = o + off at staged (row + dy - min_dy, col + dx - min_dx);
+        // backward: output o = j - off at staged (row + ext_y + min_dy - dy, col + ext_x + min_dx - dx)
+        tp->soff[t] = backward ? (tp->ext_y + mny - dy) * P + (tp->ext_x + mnx - dx) : (dy - mny) * P + (dx - mnx);
+        tp->val[t] = taps.val[t];
+    }
+    return true;
+}
+
+dim3 grid2d(const GradParams &p) {
+    return dim3((unsigned)ceil_div(p.shape[1], kT2W), (unsigned)ceil_div(p.shape[0], kT2H),
+                (unsigned)std::min<int64_t>(p.batch, 65535));
 }
 
 // Host: tap table of the operator (same construction as the forward).
@@ -287,6 +592,17 @@ int run_arg(const float *in, float *out, uint8_t *arg, int64_t batch, int ndim, 
     GradTaps taps;
     int st = build_grad_taps(MAX, batch, ndim, shape, structure, footprint, sshape, origin, mode, cval, &p, &taps);
     if (st != TM_OK) return st;
+    Taps2D tp;
+    if (make_taps2d(p, taps, false, &tp)) {
+        const int P = pitch2d(tp.ext_x);
+        const size_t smem = (size_t)(kT2H + tp.ext_y) * P * sizeof(float);
+        auto kern = P == 136 ? morph_arg2d_kernel<MAX, 136> : morph_arg2d_kernel<MAX, 160>;
+        if (smem > 48 * 1024)
+            TM_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<grid2d(p), kT2Threads, smem, s>>>(in, out, arg, p, tp);
+        TM_LAUNCH_CHECK("morph_arg2d_kernel");
+        return TM_OK;
+    }
     morph_arg_kernel<MAX><<<grid_for(p.batch * p.numel_item), kGradThreads, 0, s>>>(in, out, arg, p, taps);
     TM_LAUNCH_CHECK("morph_arg_kernel");
     return TM_OK;
@@ -301,6 +617,17 @@ int run_grad(bool dilation, const float *gout, const uint8_t *arg, float *gin, i
     GradTaps taps;
     int st = build_grad_taps(dilation, batch, ndim, shape, nullptr, footprint, sshape, origin, mode, 0.f, &p, &taps);
     if (st != TM_OK) return st;
+    Taps2D tp;
+    if (make_taps2d(p, taps, true, &tp)) {
+        const int P = pitch2d(tp.ext_x);
+        const size_t smem = (size_t)(kT2H + tp.ext_y) * P * sizeof(uint2);
+        auto kern = P == 136 ? morph_grad2d_kernel<136> : morph_grad2d_kernel<160>;
+        if (smem > 48 * 1024)
+            TM_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<grid2d(p), kT2Threads, smem, s>>>(gout, arg, gin, p, taps, tp);
+        TM_LAUNCH_CHECK("morph_grad2d_kernel");
+        return TM_OK;
+    }
     morph_grad_kernel<<<grid_for(p.batch * p.numel_item), kGradThreads, 0, s>>>(gout, arg, gin, p, taps);
     TM_LAUNCH_CHECK("morph_grad_kernel");
     return TM_OK;
