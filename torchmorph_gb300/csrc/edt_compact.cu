@@ -1204,145 +1204,160 @@ __host__ __device__ constexpr ShellList make_shell_list() {
     return l;
 }
 
+// Shell search with the offset list unrolled at compile time, for rows of
+// WW = 4 words (97..128 voxels).  Each warp works alone on units of 8 rows
+// of one plane taken from a work queue: it stages the background words the
+// offsets reach (9 planes x 16 rows), searches one word per lane, and writes
+// the unit's outputs itself.  Warps synchronise only within themselves, so
+// on one SM some warps write while others stage or search.
+constexpr int kShellCtWarps = 4;
+constexpr int kShellCtThreads = 32 * kShellCtWarps;
+constexpr int kShellWarpRows = 8;                        // rows per warp unit (8 rows x 4 words = 32 lanes)
+constexpr int kSwPitch = 6;                              // staged row: 2 zero words, then the row's 4 words
+constexpr int kSwRowsP = kShellWarpRows + 2 * kShellR;   // 16 staged rows per plane
+constexpr int kSwPlaneP = kSwRowsP * kSwPitch;           // 96 words per staged plane
+constexpr int kSwStageRows = (2 * kShellR + 1) * kSwRowsP;  // 144
+constexpr int kSwWords = (2 * kShellR + 1) * kSwPlaneP + 2;  // + zero words read right of the last row
+
 template <int WW>
-__global__ void __launch_bounds__(kShellThreads) edt_shell_ct_kernel(const uint32_t *__restrict__ bm,
-                                                                     float *__restrict__ dist,
-                                                                     int32_t *__restrict__ indices,
-                                                                     int32_t *__restrict__ sqdist,
-                                                                     int *__restrict__ todo, CompactParams p) {
+__global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uint32_t *__restrict__ bm,
+                                                                       float *__restrict__ dist,
+                                                                       int32_t *__restrict__ indices,
+                                                                       int32_t *__restrict__ sqdist,
+                                                                       int *__restrict__ todo, CompactParams p) {
+    static_assert(WW == 4, "rows of four words (97..128 voxels)");
+    static_assert(kShellWarpRows * WW == 32, "one word per lane");
     constexpr ShellList kL = make_shell_list();
-    constexpr int kPitch = WW + 2 * kShellPadW;
-    constexpr int kRowsP = kShellRows + 2 * kShellR;
-    constexpr int kPlaneP = kRowsP * kPitch;
-    __shared__ __align__(16) uint32_t bits[(2 * kShellR + 1) * kPlaneP];
-    __shared__ __align__(16) uint16_t res[kShellRows * WW * 32];
+    constexpr int kStageIters = (kSwStageRows + 31) / 32;
+    __shared__ __align__(16) uint32_t bits_all[kShellCtWarps][kSwWords + 2];
+    __shared__ __align__(16) uint16_t res_all[kShellCtWarps][kShellWarpRows * 128];
     __shared__ int2 tab2[kShellN];  // (packed offset, distance as float bits)
-    __shared__ int s_unresolved;
     const int L0 = p.L0, L1 = p.L1, W = p.L2;
-    const int ybl = (L1 + kShellRows - 1) / kShellRows;
+    const int ybl = (L1 + kShellWarpRows - 1) / kShellWarpRows;
     const int64_t nunits = p.batch * (int64_t)L0 * ybl;
-    const int tid = threadIdx.x;
-    for (int t = tid; t < kShellN; t += kShellThreads) {
+    // 64-bit work counter after the per-item flags (8-byte aligned), zeroed with them
+    unsigned long long *queue = reinterpret_cast<unsigned long long *>(todo + ((p.batch + 1) & ~(int64_t)1));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t *bits = bits_all[warp];
+    uint16_t *res = res_all[warp];
+    for (int t = threadIdx.x; t < kShellN; t += kShellCtThreads) {
         const uint32_t c = c_shell[t];
         tab2[t] = make_int2((int)c, __float_as_int(__fsqrt_rn((float)(c >> 12))));
     }
-    // persistent: a CTA takes units blockIdx.x, +gridDim.x, ...; the stores of
-    // one unit drain while the next unit is staged and searched
-    for (int64_t unit = blockIdx.x; unit < nunits; unit += gridDim.x) {
-    const int64_t item = unit / ((int64_t)L0 * ybl);
-    const int rem = (int)(unit - item * L0 * ybl);
-    const int z = rem / ybl, y0 = (rem % ybl) * kShellRows;
-    const int nrows = min(kShellRows, L1 - y0);
-    __syncthreads();  // the previous unit's shared-memory reads are done
-    if (tid == 0) s_unresolved = 0;
-    const uint32_t *ibm = bm + item * (int64_t)L0 * L1 * WW;
-    for (int i = tid; i < (2 * kShellR + 1) * kRowsP; i += kShellThreads) {
-        const int k = i / kRowsP, r = i - k * kRowsP;
-        const int zz = z - kShellR + k, yy = y0 - kShellR + r;
-        uint32_t *dst = bits + k * kPlaneP + r * kPitch;
-        const bool in_item = (unsigned)zz < (unsigned)L0 && (unsigned)yy < (unsigned)L1;
-        const uint32_t *src = ibm + ((int64_t)zz * L1 + yy) * WW;
-        dst[0] = 0u;
-        dst[kShellPadW + WW] = 0u;
-        if constexpr ((WW & 3) == 0) {
-#pragma unroll
-            for (int c = 0; c < WW; c += 4) {
-                const uint4 v = in_item ? *reinterpret_cast<const uint4 *>(src + c) : make_uint4(0, 0, 0, 0);
-                dst[kShellPadW + c] = v.x;
-                dst[kShellPadW + c + 1] = v.y;
-                dst[kShellPadW + c + 2] = v.z;
-                dst[kShellPadW + c + 3] = v.w;
-            }
-        } else {
-#pragma unroll
-            for (int c = 0; c < WW; c++) dst[kShellPadW + c] = in_item ? src[c] : 0u;
-        }
-    }
+    if (lane < 2) bits[kSwWords - 2 + lane] = 0u;
     __syncthreads();
-    for (int e = tid; e < nrows * WW; e += kShellThreads) {
-        const int r = e / WW, wi = e % WW;
-        const int nb = min(32, W - 32 * wi);
-        uint32_t U = nb == 32 ? 0xffffffffu : ((1u << nb) - 1u);
-        const uint32_t *here = bits + kShellR * kPlaneP + (kShellR + r) * kPitch + kShellPadW + wi;
-        uint16_t *out = res + r * W + 32 * wi;
-        // batches of 8 offsets in list order: 16 independent loads, one
-        // branch on the union of the batch's hits; inside a hit batch the
-        // offsets are applied in order, so earlier ones keep priority
-        constexpr int kB = 8;
+    const int64_t numel = p.numel;
+    for (;;) {
+        int64_t unit = 0;
+        if (lane == 0) unit = (int64_t)atomicAdd(queue, 1ull);
+        unit = __shfl_sync(~0u, unit, 0);
+        if (unit >= nunits) break;
+        const int64_t item = unit / ((int64_t)L0 * ybl);
+        const int rem = (int)(unit - item * L0 * ybl);
+        const int z = rem / ybl, y0 = (rem % ybl) * kShellWarpRows;
+        const int nrows = min(kShellWarpRows, L1 - y0);
+        const uint32_t *ibm = bm + item * (int64_t)L0 * L1 * WW;
+        // stage: every load of the lane before any store
+        uint4 v[kStageIters];
 #pragma unroll
-        for (int t0 = 0; t0 < kShellN; t0 += kB) {
-            if (U == 0u) break;
-            uint32_t bg[kB];
-            uint32_t any = 0;
+        for (int j = 0; j < kStageIters; j++) {
+            const int i = lane + 32 * j;
+            const int kk = i / kSwRowsP, r = i - kk * kSwRowsP;
+            const int zz = z - kShellR + kk, yy = y0 - kShellR + r;
+            const bool ok = i < kSwStageRows && (unsigned)zz < (unsigned)L0 && (unsigned)yy < (unsigned)L1;
+            v[j] = ok ? *reinterpret_cast<const uint4 *>(ibm + ((int64_t)zz * L1 + yy) * WW) : make_uint4(0, 0, 0, 0);
+        }
 #pragma unroll
-            for (int i = 0; i < kB; i++) {
-                const int t = t0 + i < kShellN ? t0 + i : kShellN - 1;
-                const int delta = kL.o[t].dz * kPlaneP + kL.o[t].dy * kPitch + (kL.o[t].dx >= 0 ? 0 : -1);
-                const int sh = kL.o[t].dx >= 0 ? kL.o[t].dx : 32 + kL.o[t].dx;
-                bg[i] = t0 + i < kShellN ? __funnelshift_r(here[delta], here[delta + 1], sh) : 0u;
-                any |= bg[i];
+        for (int j = 0; j < kStageIters; j++) {
+            const int i = lane + 32 * j;
+            if (i < kSwStageRows) {
+                const int kk = i / kSwRowsP, r = i - kk * kSwRowsP;
+                uint2 *dst = reinterpret_cast<uint2 *>(bits + kk * kSwPlaneP + r * kSwPitch);
+                dst[0] = make_uint2(0u, 0u);
+                dst[1] = make_uint2(v[j].x, v[j].y);
+                dst[2] = make_uint2(v[j].z, v[j].w);
             }
-            uint32_t H = any & U;
-            if (H) {
-                U &= ~H;
+        }
+        __syncwarp();
+        // search: lane = word (row lane / 4, word lane % 4)
+        uint32_t U = 0u;
+        {
+            const int r = lane >> 2, wi = lane & 3;
+            const int nb = min(32, W - 32 * wi);
+            if (r < nrows) U = nb == 32 ? 0xffffffffu : ((1u << nb) - 1u);
+            const uint32_t *here = bits + kShellR * kSwPlaneP + (kShellR + r) * kSwPitch + 2 + wi;
+            uint16_t *out = res + r * 128 + 32 * wi;
+            // batches of 8 offsets in list order: 16 independent loads, one
+            // branch on the union of the batch's hits; inside a hit batch the
+            // offsets are applied in order, so earlier ones keep priority
+            constexpr int kB = 8;
+#pragma unroll
+            for (int t0 = 0; t0 < kShellN; t0 += kB) {
+                if (U == 0u) break;
+                uint32_t bg[kB];
+                uint32_t any = 0;
 #pragma unroll
                 for (int i = 0; i < kB; i++) {
-                    uint32_t hit = bg[i] & H;
-                    if (hit) {
-                        H &= ~hit;
-                        do {
-                            const int b = __ffs(hit) - 1;
-                            out[b] = (uint16_t)(t0 + i);
-                            hit &= hit - 1;
-                        } while (hit);
+                    const int t = t0 + i < kShellN ? t0 + i : kShellN - 1;
+                    const int delta = kL.o[t].dz * kSwPlaneP + kL.o[t].dy * kSwPitch + (kL.o[t].dx >= 0 ? 0 : -1);
+                    const int sh = kL.o[t].dx >= 0 ? kL.o[t].dx : 32 + kL.o[t].dx;
+                    bg[i] = t0 + i < kShellN ? __funnelshift_r(here[delta], here[delta + 1], sh) : 0u;
+                    any |= bg[i];
+                }
+                uint32_t H = any & U;
+                if (H) {
+                    U &= ~H;
+#pragma unroll
+                    for (int i = 0; i < kB; i++) {
+                        uint32_t hit = bg[i] & H;
+                        if (hit) {
+                            H &= ~hit;
+                            do {
+                                const int bb = __ffs(hit) - 1;
+                                out[bb] = (uint16_t)(t0 + i);
+                                hit &= hit - 1;
+                            } while (hit);
+                        }
                     }
                 }
             }
         }
-        if (U) {
-            s_unresolved = 1;
-            do {
-                const int b = __ffs(U) - 1;
-                out[b] = 0xFFFF;
-                U &= U - 1;
-            } while (U);
+        if (__any_sync(~0u, U != 0u)) {  // a voxel beyond the shell: the item takes the separable passes
+            if (lane == 0) atomicExch(&todo[item], 1);
+            continue;
         }
-    }
-    __syncthreads();
-    if (s_unresolved) {
-        if (tid == 0) atomicExch(&todo[item], 1);
-        continue;
-    }
-    const int64_t numel = p.numel;
-    const int64_t rowbase = item * p.numel_item + ((int64_t)z * L1 + y0) * W;
-    const int warp = tid >> 5, lane = tid & 31;
-    for (int r = warp; r < nrows; r += kShellThreads / 32) {
-        const uint16_t *rres = res + r * W;
-        for (int x = 4 * lane; x < W; x += 128) {
-            float dv[4];
-            int32_t i0[4], i1[4], i2[4], sq[4];
-            const uint2 rr = *reinterpret_cast<const uint2 *>(rres + x);  // 4 offset numbers
-            const int tt[4] = {(int)(rr.x & 0xffffu), (int)(rr.x >> 16), (int)(rr.y & 0xffffu), (int)(rr.y >> 16)};
+        __syncwarp();
+        // write: lane = 4 consecutive voxels of a row
+        const int64_t rowbase = item * p.numel_item + ((int64_t)z * L1 + y0) * W;
+        const int x = 4 * lane;
+        if (x < W) {
+            for (int r = 0; r < nrows; r++) {
+                float dv[4];
+                int32_t i0[4], i1[4], i2[4], sq[4];
+                const uint2 rr = *reinterpret_cast<const uint2 *>(res + r * 128 + x);  // 4 offset numbers
+                const int tt[4] = {(int)(rr.x & 0xffffu), (int)(rr.x >> 16), (int)(rr.y & 0xffffu),
+                                   (int)(rr.y >> 16)};
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const int2 e = tab2[tt[k]];
-                const uint32_t c = (uint32_t)e.x;
-                dv[k] = __int_as_float(e.y);
-                sq[k] = (int32_t)(c >> 12);
-                i0[k] = z + (int)(c & 15u) - 8;
-                i1[k] = y0 + r + (int)((c >> 4) & 15u) - 8;
-                i2[k] = x + k + (int)((c >> 8) & 15u) - 8;
-            }
-            const int64_t gi = rowbase + (int64_t)r * W + x;
-            if (dist) *reinterpret_cast<float4 *>(dist + gi) = make_float4(dv[0], dv[1], dv[2], dv[3]);
-            if (sqdist) *reinterpret_cast<int4 *>(sqdist + gi) = make_int4(sq[0], sq[1], sq[2], sq[3]);
-            if (indices) {
-                *reinterpret_cast<int4 *>(indices + gi) = make_int4(i0[0], i0[1], i0[2], i0[3]);
-                *reinterpret_cast<int4 *>(indices + numel + gi) = make_int4(i1[0], i1[1], i1[2], i1[3]);
-                *reinterpret_cast<int4 *>(indices + 2 * numel + gi) = make_int4(i2[0], i2[1], i2[2], i2[3]);
+                for (int q = 0; q < 4; q++) {
+                    const int2 e = tab2[tt[q]];
+                    const uint32_t c = (uint32_t)e.x;
+                    dv[q] = __int_as_float(e.y);
+                    sq[q] = (int32_t)(c >> 12);
+                    i0[q] = z + (int)(c & 15u) - 8;
+                    i1[q] = y0 + r + (int)((c >> 4) & 15u) - 8;
+                    i2[q] = x + q + (int)((c >> 8) & 15u) - 8;
+                }
+                const int64_t gi = rowbase + (int64_t)r * W + x;
+                if (dist) *reinterpret_cast<float4 *>(dist + gi) = make_float4(dv[0], dv[1], dv[2], dv[3]);
+                if (sqdist) *reinterpret_cast<int4 *>(sqdist + gi) = make_int4(sq[0], sq[1], sq[2], sq[3]);
+                if (indices) {
+                    *reinterpret_cast<int4 *>(indices + gi) = make_int4(i0[0], i0[1], i0[2], i0[3]);
+                    *reinterpret_cast<int4 *>(indices + numel + gi) = make_int4(i1[0], i1[1], i1[2], i1[3]);
+                    *reinterpret_cast<int4 *>(indices + 2 * numel + gi) = make_int4(i2[0], i2[1], i2[2], i2[3]);
+                }
             }
         }
-    }
+        __syncwarp();  // res and bits are free for the next unit
     }
 }
 
@@ -1571,7 +1586,8 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
         const int64_t nwords = g.batch * (int64_t)p.L0 * p.L1 * ww;
         uint32_t *bm = reinterpret_cast<uint32_t *>(c2);
         todo = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(c2) + align256((size_t)nwords * 4));
-        TM_CHECK_CUDA(cudaMemsetAsync(todo, 0, (size_t)g.batch * sizeof(int), stream));
+        // per-item flags, then (8-byte aligned) the shell kernel's work counter
+        TM_CHECK_CUDA(cudaMemsetAsync(todo, 0, (size_t)((g.batch + 1) & ~(int64_t)1) * sizeof(int) + 8, stream));
         const unsigned bblocks = (unsigned)std::min<int64_t>(ceil_div(nwords, 256), (int64_t)sm_count() * 16);
         const bool vrow = (p.L2 % 32) == 0 && ((uintptr_t)input & 15) == 0;
         if (in_dtype == TM_F32) {
@@ -1594,14 +1610,15 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
             TM_CHECK_CUDA(cudaGetDevice(&dev));
             if (cached_dev != dev || cached_fn != (const void *)kernel) {
                 int per_sm = 0;
-                TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kShellThreads, 0));
+                TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kShellCtThreads, 0));
                 cached_ctas = (per_sm < 1 ? 1 : per_sm) * sm_count();
                 cached_dev = dev;
                 cached_fn = (const void *)kernel;
             }
-            // about two units per CTA, so consecutive units of a CTA overlap
-            const int64_t grid = std::min<int64_t>(cached_ctas, (sblocks + 1) / 2);
-            kernel<<<(unsigned)grid, kShellThreads, 0, stream>>>(bm, dist, indices, sqdist, todo, p);
+            // persistent warps on a work queue of 8-row units
+            const int64_t wunits = g.batch * (int64_t)p.L0 * ceil_div(p.L1, kShellWarpRows);
+            const int64_t grid = std::min<int64_t>(cached_ctas, ceil_div(wunits, kShellCtWarps));
+            kernel<<<(unsigned)grid, kShellCtThreads, 0, stream>>>(bm, dist, indices, sqdist, todo, p);
             return TM_OK;
         };
         if (ww == 4) {  // rows of 97..128 voxels: straight-line search
