@@ -1230,7 +1230,8 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
     constexpr ShellList kL = make_shell_list();
     constexpr int kStageIters = (kSwStageRows + 31) / 32;
     __shared__ __align__(16) uint32_t bits_all[kShellCtWarps][kSwWords + 2];
-    __shared__ __align__(16) uint16_t res_all[kShellCtWarps][kShellWarpRows * 128];
+    // per word: bit-planes 0..8 of the resolving offset number (12 words, 16-byte aligned)
+    __shared__ __align__(16) uint32_t planes_all[kShellCtWarps][32 * 12];
     __shared__ int2 tab2[kShellN];  // (packed offset, distance as float bits)
     const int L0 = p.L0, L1 = p.L1, W = p.L2;
     const int ybl = (L1 + kShellWarpRows - 1) / kShellWarpRows;
@@ -1239,7 +1240,7 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
     unsigned long long *queue = reinterpret_cast<unsigned long long *>(todo + ((p.batch + 1) & ~(int64_t)1));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t *bits = bits_all[warp];
-    uint16_t *res = res_all[warp];
+    uint32_t *planes = planes_all[warp];
     for (int t = threadIdx.x; t < kShellN; t += kShellCtThreads) {
         const uint32_t c = c_shell[t];
         tab2[t] = make_int2((int)c, __float_as_int(__fsqrt_rn((float)(c >> 12))));
@@ -1279,17 +1280,18 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
             }
         }
         __syncwarp();
-        // search: lane = word (row lane / 4, word lane % 4)
+        // search: lane = word (row lane / 4, word lane % 4).  The offset number
+        // t = 8 * batch + i resolving each voxel is kept as bit-planes P[0..8]
+        // of the word: per batch, f_i = the voxels whose first background
+        // offset is the batch's i-th (earlier offsets keep priority), then
+        // planes 0-2 take the bits of i and planes 3-8 the batch number.
         uint32_t U = 0u;
         {
             const int r = lane >> 2, wi = lane & 3;
             const int nb = min(32, W - 32 * wi);
             if (r < nrows) U = nb == 32 ? 0xffffffffu : ((1u << nb) - 1u);
-            const uint32_t *here = bits + kShellR * kSwPlaneP + (kShellR + r) * kSwPitch + 2 + wi;
-            uint16_t *out = res + r * 128 + 32 * wi;
-            // batches of 8 offsets in list order: 16 independent loads, one
-            // branch on the union of the batch's hits; inside a hit batch the
-            // offsets are applied in order, so earlier ones keep priority
+            const volatile uint32_t *vhere = bits + kShellR * kSwPlaneP + (kShellR + r) * kSwPitch + 2 + wi;
+            uint32_t P[9] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
             constexpr int kB = 8;
 #pragma unroll
             for (int t0 = 0; t0 < kShellN; t0 += kB) {
@@ -1301,26 +1303,30 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
                     const int t = t0 + i < kShellN ? t0 + i : kShellN - 1;
                     const int delta = kL.o[t].dz * kSwPlaneP + kL.o[t].dy * kSwPitch + (kL.o[t].dx >= 0 ? 0 : -1);
                     const int sh = kL.o[t].dx >= 0 ? kL.o[t].dx : 32 + kL.o[t].dx;
-                    bg[i] = t0 + i < kShellN ? __funnelshift_r(here[delta], here[delta + 1], sh) : 0u;
+                    // volatile: each batch's loads stay behind its exit test
+                    bg[i] = t0 + i < kShellN ? __funnelshift_r(vhere[delta], vhere[delta + 1], sh) : 0u;
                     any |= bg[i];
                 }
-                uint32_t H = any & U;
-                if (H) {
-                    U &= ~H;
+                const uint32_t H = any & U;  // resolved in this batch
+                U &= ~H;
+                uint32_t rem = H, f[kB];
 #pragma unroll
-                    for (int i = 0; i < kB; i++) {
-                        uint32_t hit = bg[i] & H;
-                        if (hit) {
-                            H &= ~hit;
-                            do {
-                                const int bb = __ffs(hit) - 1;
-                                out[bb] = (uint16_t)(t0 + i);
-                                hit &= hit - 1;
-                            } while (hit);
-                        }
-                    }
+                for (int i = 0; i < kB; i++) {
+                    f[i] = bg[i] & rem;
+                    rem &= ~bg[i];
                 }
+                P[0] |= f[1] | f[3] | f[5] | f[7];
+                P[1] |= f[2] | f[3] | f[6] | f[7];
+                P[2] |= f[4] | f[5] | f[6] | f[7];
+                const int bi = t0 / kB;  // a constant once the loop is unrolled
+#pragma unroll
+                for (int j = 0; j < 6; j++)
+                    if ((bi >> j) & 1) P[3 + j] |= H;
             }
+            uint4 *pw = reinterpret_cast<uint4 *>(planes + lane * 12);
+            pw[0] = make_uint4(P[0], P[1], P[2], P[3]);
+            pw[1] = make_uint4(P[4], P[5], P[6], P[7]);
+            pw[2] = make_uint4(P[8], 0u, 0u, 0u);
         }
         if (__any_sync(~0u, U != 0u)) {  // a voxel beyond the shell: the item takes the separable passes
             if (lane == 0) atomicExch(&todo[item], 1);
@@ -1331,12 +1337,23 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
         const int64_t rowbase = item * p.numel_item + ((int64_t)z * L1 + y0) * W;
         const int x = 4 * lane;
         if (x < W) {
+            const int b = x & 31;
             for (int r = 0; r < nrows; r++) {
                 float dv[4];
                 int32_t i0[4], i1[4], i2[4], sq[4];
-                const uint2 rr = *reinterpret_cast<const uint2 *>(res + r * 128 + x);  // 4 offset numbers
-                const int tt[4] = {(int)(rr.x & 0xffffu), (int)(rr.x >> 16), (int)(rr.y & 0xffffu),
-                                   (int)(rr.y >> 16)};
+                // offset numbers of voxels x..x+3 from the word's bit-planes:
+                // a plane's nibble spread to one bit per byte, bytes = t & 255
+                const uint4 *pw = reinterpret_cast<const uint4 *>(planes + (r * 4 + (x >> 5)) * 12);
+                const uint4 qa = pw[0], qb = pw[1];
+                const uint32_t p8 = planes[(r * 4 + (x >> 5)) * 12 + 8];
+                const uint32_t pl[8] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y, qb.z, qb.w};
+                uint32_t acc = 0u;
+#pragma unroll
+                for (int j = 0; j < 8; j++) acc += ((((pl[j] >> b) & 15u) * 0x00204081u) & 0x01010101u) << j;
+                const uint32_t hi = (((p8 >> b) & 15u) * 0x00204081u) & 0x01010101u;
+                int tt[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) tt[q] = (int)(((acc >> (8 * q)) & 255u) | (((hi >> (8 * q)) & 1u) << 8));
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
                     const int2 e = tab2[tt[q]];
