@@ -115,6 +115,7 @@ __global__ void __launch_bounds__(kCols *kSegs) edt_c0_smem_kernel(const In *__r
                                                                    int16_t *__restrict__ c1, CompactParams p,
                                                                    const int *__restrict__ todo) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    pdl_wait();  // launched after the shell search: its flags are complete
     const int L = p.L0;
     const int64_t inner = p.numel_item / L;
     if (todo && !todo[blockIdx.x / ((inner + kCols - 1) / kCols)]) return;  // item finished by the shell pass
@@ -704,6 +705,7 @@ __global__ void __launch_bounds__(kC12Threads) edt_c12_kernel(const int16_t *__r
                                                               int16_t *__restrict__ gstack, CompactParams p,
                                                               const int *__restrict__ todo) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    pdl_wait();  // launched after pass 0: its features are complete
     const int L0 = p.L0, L1 = p.L1, W = p.L2;
     if (todo && !todo[blockIdx.x / L0]) return;  // item finished by the shell pass
     const C12Smem sm = c12_smem(L1, W);
@@ -1241,12 +1243,14 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t *bits = bits_all[warp];
     uint32_t *planes = planes_all[warp];
+    pdl_trigger();  // the fallback passes may be scheduled as this grid's CTAs retire
     for (int t = threadIdx.x; t < kShellN; t += kShellCtThreads) {
         const uint32_t c = c_shell[t];
         tab2[t] = make_int2((int)c, __float_as_int(__fsqrt_rn((float)(c >> 12))));
     }
     if (lane < 2) bits[kSwWords - 2 + lane] = 0u;
     __syncthreads();
+    pdl_wait();  // the background bitmap and the zeroed flags / counter are complete
     const int64_t numel = p.numel;
     for (;;) {
         int64_t unit = 0;
@@ -1635,7 +1639,8 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
             // persistent warps on a work queue of 8-row units
             const int64_t wunits = g.batch * (int64_t)p.L0 * ceil_div(p.L1, kShellWarpRows);
             const int64_t grid = std::min<int64_t>(cached_ctas, ceil_div(wunits, kShellCtWarps));
-            kernel<<<(unsigned)grid, kShellCtThreads, 0, stream>>>(bm, dist, indices, sqdist, todo, p);
+            TM_CHECK_CUDA(launch_pdl(kernel, dim3((unsigned)grid), dim3(kShellCtThreads), 0, stream, bm, dist,
+                                     indices, sqdist, todo, p));
             return TM_OK;
         };
         if (ww == 4) {  // rows of 97..128 voxels: straight-line search
@@ -1661,12 +1666,22 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
             TM_CHECK_CUDA(cudaFuncSetAttribute(edt_c0_smem_kernel<uint8_t>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         }
-        if (in_dtype == TM_F32)
-            edt_c0_smem_kernel<float><<<(unsigned)blocks, kCols * kSegs, smem, stream>>>(
-                static_cast<const float *>(input), c1, p, todo);
-        else
-            edt_c0_smem_kernel<uint8_t><<<(unsigned)blocks, kCols * kSegs, smem, stream>>>(
-                static_cast<const uint8_t *>(input), c1, p, todo);
+        // after the shell search, overlap this launch with its last CTAs
+        if (in_dtype == TM_F32) {
+            const float *in = static_cast<const float *>(input);
+            if (todo)
+                TM_CHECK_CUDA(launch_pdl(edt_c0_smem_kernel<float>, dim3((unsigned)blocks), dim3(kCols * kSegs), smem,
+                                         stream, in, c1, p, (const int *)todo));
+            else
+                edt_c0_smem_kernel<float><<<(unsigned)blocks, kCols * kSegs, smem, stream>>>(in, c1, p, todo);
+        } else {
+            const uint8_t *in = static_cast<const uint8_t *>(input);
+            if (todo)
+                TM_CHECK_CUDA(launch_pdl(edt_c0_smem_kernel<uint8_t>, dim3((unsigned)blocks), dim3(kCols * kSegs),
+                                         smem, stream, in, c1, p, (const int *)todo));
+            else
+                edt_c0_smem_kernel<uint8_t><<<(unsigned)blocks, kCols * kSegs, smem, stream>>>(in, c1, p, todo);
+        }
         TM_LAUNCH_CHECK("edt_c0_smem_kernel");
     } else {
         const int64_t nlines0 = g.batch * inner0;
@@ -1685,7 +1700,9 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
         if (smem > 48 * 1024)
             TM_CHECK_CUDA(cudaFuncSetAttribute(edt_c12_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)smem));
-        edt_c12_kernel<<<(unsigned)blocks, kC12Threads, smem, stream>>>(c1, dist, indices, sqdist, stack1, p, todo);
+        // launched after pass 0 (whose kernel runs normally when there is no shell search)
+        TM_CHECK_CUDA(launch_pdl(edt_c12_kernel, dim3((unsigned)blocks), dim3(kC12Threads), smem, stream,
+                                 (const int16_t *)c1, dist, indices, sqdist, stack1, p, (const int *)todo));
         TM_LAUNCH_CHECK("edt_c12_kernel");
         return TM_OK;
     }

@@ -76,6 +76,31 @@ __host__ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) 
     return (hi + ((n - hi) >> 1)) >> (f.shift - 1);
 }
 
+// Programmatic dependent launch: the kernel may be scheduled while the
+// previous kernel of the stream is still finishing.  A kernel launched this
+// way calls pdl_wait() before it touches anything the previous kernel writes
+// or reads; pdl_wait() then returns once that kernel has completed and its
+// writes are visible (it is a no-op in a kernel launched normally).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Lets the next kernel of the stream (if launched with launch_pdl) be scheduled now.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 }  // namespace tmc
 
 #define TM_CHECK_CUDA(call)                                    \
