@@ -995,7 +995,11 @@ __device__ __forceinline__ uint32_t zero_bytes4(uint32_t v) {
 
 template <typename In, bool VEC>
 __global__ void __launch_bounds__(256) edt_bitmap_kernel(const In *__restrict__ in, uint32_t *__restrict__ bm,
-                                                         CompactParams p, int ww, int64_t nwords) {
+                                                         CompactParams p, int ww, int64_t nwords,
+                                                         int *__restrict__ clear, int nclear) {
+    // the shell pass's per-item flags and work counter start at zero
+    if (blockIdx.x == 0)
+        for (int i = threadIdx.x; i < nclear; i += blockDim.x) clear[i] = 0;
     for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += (int64_t)gridDim.x * blockDim.x) {
         const int64_t row = w / ww;
         const int wi = (int)(w - row * ww);
@@ -1607,18 +1611,20 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
         const int64_t nwords = g.batch * (int64_t)p.L0 * p.L1 * ww;
         uint32_t *bm = reinterpret_cast<uint32_t *>(c2);
         todo = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(c2) + align256((size_t)nwords * 4));
-        // per-item flags, then (8-byte aligned) the shell kernel's work counter
-        TM_CHECK_CUDA(cudaMemsetAsync(todo, 0, (size_t)((g.batch + 1) & ~(int64_t)1) * sizeof(int) + 8, stream));
+        // per-item flags, then (8-byte aligned) the shell kernel's 64-bit work
+        // counter: zeroed by the bitmap kernel
+        const int nclear = (int)((g.batch + 1) & ~(int64_t)1) + 2;
+        if (g.batch > ((int64_t)1 << 30)) return fail(TM_ERR_TOO_LARGE, "batch too large");
         const unsigned bblocks = (unsigned)std::min<int64_t>(ceil_div(nwords, 256), (int64_t)sm_count() * 16);
         const bool vrow = (p.L2 % 32) == 0 && ((uintptr_t)input & 15) == 0;
         if (in_dtype == TM_F32) {
             const float *in = static_cast<const float *>(input);
-            if (vrow) edt_bitmap_kernel<float, true><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
-            else edt_bitmap_kernel<float, false><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
+            if (vrow) edt_bitmap_kernel<float, true><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords, todo, nclear);
+            else edt_bitmap_kernel<float, false><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords, todo, nclear);
         } else {
             const uint8_t *in = static_cast<const uint8_t *>(input);
-            if (vrow) edt_bitmap_kernel<uint8_t, true><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
-            else edt_bitmap_kernel<uint8_t, false><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
+            if (vrow) edt_bitmap_kernel<uint8_t, true><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords, todo, nclear);
+            else edt_bitmap_kernel<uint8_t, false><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords, todo, nclear);
         }
         TM_LAUNCH_CHECK("edt_bitmap_kernel");
         const ShellSmem sm = shell_smem(p.L2);
@@ -1772,17 +1778,18 @@ int cdt_shell_run(const void *input, int in_dtype, const Geometry &g, int metric
     const int64_t nwords = g.batch * (int64_t)p.L0 * p.L1 * ww;
     uint32_t *bm = reinterpret_cast<uint32_t *>(ws);
     int *todo = reinterpret_cast<int *>(ws + align256((size_t)nwords * 4));
-    TM_CHECK_CUDA(cudaMemsetAsync(todo, 0, (size_t)g.batch * sizeof(int), stream));
+    if (g.batch > ((int64_t)1 << 30)) return fail(TM_ERR_TOO_LARGE, "batch too large");
+    const int nclear = (int)g.batch;  // per-item flags, zeroed by the bitmap kernel
     const unsigned bblocks = (unsigned)std::min<int64_t>(ceil_div(nwords, 256), (int64_t)sm_count() * 16);
     const bool vrow = (p.L2 % 32) == 0 && ((uintptr_t)input & 15) == 0;
     if (in_dtype == TM_F32) {
         const float *in = static_cast<const float *>(input);
-        if (vrow) edt_bitmap_kernel<float, true><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
-        else edt_bitmap_kernel<float, false><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
+        if (vrow) edt_bitmap_kernel<float, true><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords, todo, nclear);
+        else edt_bitmap_kernel<float, false><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords, todo, nclear);
     } else {
         const uint8_t *in = static_cast<const uint8_t *>(input);
-        if (vrow) edt_bitmap_kernel<uint8_t, true><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
-        else edt_bitmap_kernel<uint8_t, false><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords);
+        if (vrow) edt_bitmap_kernel<uint8_t, true><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords, todo, nclear);
+        else edt_bitmap_kernel<uint8_t, false><<<bblocks, 256, 0, stream>>>(in, bm, p, ww, nwords, todo, nclear);
     }
     TM_LAUNCH_CHECK("edt_bitmap_kernel");
     const int64_t blocks = g.batch * (int64_t)p.L0 * ceil_div(p.L1, kShellRows);
