@@ -211,6 +211,31 @@ def test_edt_vector_path_and_offset_outputs(cuda):
     np.testing.assert_array_equal(ibuf.cpu().numpy(), oi)
 
 
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_edt_shell_patch_and_overflow(cuda, seed):
+    """3-D items with 97..128-voxel rows take the bitmap shell search (|d|^2 <= 16); voxels
+    it leaves are patched one by one, and items with more of them than the patch list
+    holds (or without background) take the separable passes.  Item 0: a 9^3 foreground
+    block (centre at |d|^2 = 25); item 1: a radius-12 foreground ball (~2000 listed
+    voxels); item 2: all foreground (overflows the list); item 3: plain Bernoulli(0.9)."""
+    r = rng(100 + seed)
+    shape = (4, 1, 40, 50, 128)
+    x = r.random(shape) < 0.9
+    x[0, 0, 10:19, 20:29, 60:69] = True
+    zz, yy, xx = np.meshgrid(np.arange(40), np.arange(50), np.arange(128), indexing="ij")
+    x[1, 0] |= (zz - 20) ** 2 + (yy - 25) ** 2 + (xx - 64) ** 2 <= 144
+    x[2] = True
+    sq, od, oi = oracle.edt(x)
+    d, idx = tm.euclidean_distance_transform(_t(x), return_indices=True)
+    np.testing.assert_array_equal(d.cpu().numpy(), od.astype(np.float32))
+    np.testing.assert_array_equal(idx.cpu().numpy(), oi)
+    s = tm.euclidean_distance_transform_squared(_t(x))
+    np.testing.assert_array_equal(s.cpu().numpy(), sq.astype(np.int32))
+    ed, ei = per_item_indices(x[[0, 1, 3]], ndi.distance_transform_edt)
+    np.testing.assert_array_equal(d.cpu().numpy()[[0, 1, 3]], ed.astype(np.float32))
+    np.testing.assert_array_equal(idx.cpu().numpy()[:, [0, 1, 3]], ei)
+
+
 @pytest.mark.parametrize("metric", ["chessboard", "taxicab", "chamfer345"])
 @pytest.mark.parametrize("shape,p", [((2, 1, 20, 33, 128), 0.9), ((1, 2, 9, 40, 100), 0.85),
                                      ((3, 1, 12, 16, 128), 0.999)])

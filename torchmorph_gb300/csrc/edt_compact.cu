@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(kCols *kSegs) edt_c0_smem_kernel(const In *__r
                                                                    int16_t *__restrict__ c1, CompactParams p,
                                                                    const int *__restrict__ todo) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    pdl_wait();  // launched after the shell search: its flags are complete
+    pdl_wait();  // launched after the shell search and its patch pass: the flags are complete
     const int L = p.L0;
     const int64_t inner = p.numel_item / L;
     if (todo && !todo[blockIdx.x / ((inner + kCols - 1) / kCols)]) return;  // item finished by the shell pass
@@ -1230,7 +1230,9 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
                                                                        float *__restrict__ dist,
                                                                        int32_t *__restrict__ indices,
                                                                        int32_t *__restrict__ sqdist,
-                                                                       int *__restrict__ todo, CompactParams p) {
+                                                                       int *__restrict__ todo, CompactParams p,
+                                                                       unsigned long long *__restrict__ ulist,
+                                                                       unsigned ucap) {
     static_assert(WW == 4, "rows of four words (97..128 voxels)");
     static_assert(kShellWarpRows * WW == 32, "one word per lane");
     constexpr ShellList kL = make_shell_list();
@@ -1244,6 +1246,7 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
     const int64_t nunits = p.batch * (int64_t)L0 * ybl;
     // 64-bit work counter after the per-item flags (8-byte aligned), zeroed with them
     unsigned long long *queue = reinterpret_cast<unsigned long long *>(todo + ((p.batch + 1) & ~(int64_t)1));
+    unsigned *ucount = reinterpret_cast<unsigned *>(queue + 1);  // entries of the unresolved-voxel list
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t *bits = bits_all[warp];
     uint32_t *planes = planes_all[warp];
@@ -1336,9 +1339,20 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
             pw[1] = make_uint4(P[4], P[5], P[6], P[7]);
             pw[2] = make_uint4(P[8], 0u, 0u, 0u);
         }
-        if (__any_sync(~0u, U != 0u)) {  // a voxel beyond the shell: the item takes the separable passes
-            if (lane == 0) atomicExch(&todo[item], 1);
-            continue;
+        if (U) {
+            // voxels beyond the shell (|d|^2 > 16): listed for the patch pass,
+            // which overwrites what is written for them below; when the list
+            // is full the item takes the separable passes instead
+            // (every slot below the capacity is written by the lane that took it,
+            // so the patch pass reads only written entries)
+            const unsigned nu = __popc(U);
+            const unsigned at = atomicAdd(ucount, nu);
+            if (at + nu > ucap || at + nu < at) atomicExch(&todo[item], 1);
+            const int r = lane >> 2, wi = lane & 3;
+            unsigned k = at;
+            for (uint32_t m = U; m && k < ucap; m &= m - 1)
+                ulist[k++] = ((unsigned long long)item << 24) | ((unsigned long long)z << 16) |
+                             ((unsigned long long)(y0 + r) << 8) | (unsigned long long)(32 * wi + __ffs(m) - 1);
         }
         __syncwarp();
         // write: lane = 4 consecutive voxels of a row
@@ -1383,6 +1397,110 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
             }
         }
         __syncwarp();  // res and bits are free for the next unit
+    }
+}
+
+// Patch pass for the voxels the shell search left (no background with
+// |d|^2 <= 16; near the item's faces the shell is cut off): one warp per
+// listed voxel searches the cube of Chebyshev radius R on the background
+// bitmap, R = 6, 13, 27, ... until the best squared distance is below
+// (R + 1)^2 (nothing outside the cube can be nearer or tie) or the cube
+// covers the item.  Per row (dz, dy) only the nearest background bit on
+// each side of x can be the row's best.  Among equal squared distances the
+// smallest axis-2 coordinate wins, then axis 1, then axis 0 -- the order of
+// the shell list (|d|^2, dx, dy, dz), which is the separable passes' tie
+// rule (each pass keeps the lower coordinate).  An item without background
+// is flagged for the separable passes.
+constexpr int kPatchThreads = 256;
+constexpr unsigned kPatchCap = 4096;  // listed voxels per call at most (more: the separable passes are cheaper)
+
+__global__ void __launch_bounds__(kPatchThreads) edt_patch_kernel(const uint32_t *__restrict__ bm,
+                                                                  float *__restrict__ dist,
+                                                                  int32_t *__restrict__ indices,
+                                                                  int32_t *__restrict__ sqdist, int *__restrict__ todo,
+                                                                  CompactParams p,
+                                                                  const unsigned long long *__restrict__ ulist,
+                                                                  unsigned ucap) {
+    pdl_wait();  // the shell search (and its list) is complete
+    constexpr int WW = 4;
+    const unsigned long long *queue =
+        reinterpret_cast<const unsigned long long *>(todo + ((p.batch + 1) & ~(int64_t)1));
+    const unsigned nlist = min(*reinterpret_cast<const unsigned *>(queue + 1), ucap);
+    const int L0 = p.L0, L1 = p.L1, W = p.L2;
+    const int lane = threadIdx.x & 31;
+    const unsigned gw = (blockIdx.x * kPatchThreads + threadIdx.x) >> 5, nw = (gridDim.x * kPatchThreads) >> 5;
+    for (unsigned e = gw; e < nlist; e += nw) {
+        const unsigned long long v = ulist[e];
+        const int64_t item = (int64_t)(v >> 24);
+        const int z = (int)((v >> 16) & 255u), y = (int)((v >> 8) & 255u), x = (int)(v & 255u);
+        if (item >= p.batch || z >= L0 || y >= L1 || x >= W) continue;  // not an entry of this call
+        if (todo[item]) continue;  // the separable passes redo the item
+        const uint32_t *ibm = bm + item * (int64_t)L0 * L1 * WW;
+        unsigned long long best = ~0ull;  // (d2 << 24) | (x' << 16) | (y' << 8) | z'
+        for (int R = 6;; R = 2 * R + 1) {
+            const int side = 2 * R + 1;
+            const int xl = max(0, x - R), xr = min(W - 1, x + R);
+            for (int k = lane; k < side * side; k += 32) {
+                const int dz = k / side - R, dy = k % side - R;
+                const int zz = z + dz, yy = y + dy;
+                if ((unsigned)zz >= (unsigned)L0 || (unsigned)yy >= (unsigned)L1) continue;
+                const unsigned rowd2 = (unsigned)(dz * dz + dy * dy);
+                if (((unsigned long long)rowd2 << 24) >= best) continue;
+                const uint32_t *row = ibm + ((int64_t)zz * L1 + yy) * WW;
+                // nearest background at x' <= x
+                for (int w = x >> 5; w >= (xl >> 5); w--) {
+                    uint32_t m = row[w];
+                    if (w == (x >> 5)) m &= (x & 31) == 31 ? 0xffffffffu : ((2u << (x & 31)) - 1u);
+                    if (w == (xl >> 5)) m &= ~((1u << (xl & 31)) - 1u);
+                    if (m) {
+                        const int xp = 32 * w + 31 - __clz(m);
+                        const unsigned d2 = rowd2 + (unsigned)((x - xp) * (x - xp));
+                        const unsigned long long key = ((unsigned long long)d2 << 24) | ((unsigned)xp << 16) |
+                                                       ((unsigned)yy << 8) | (unsigned)zz;
+                        best = key < best ? key : best;
+                        break;
+                    }
+                }
+                // nearest background at x' > x
+                if (x < xr)
+                    for (int w = (x + 1) >> 5; w <= (xr >> 5); w++) {
+                        uint32_t m = row[w];
+                        if (w == ((x + 1) >> 5)) m &= ~((1u << ((x + 1) & 31)) - 1u);
+                        if (w == (xr >> 5)) m &= (xr & 31) == 31 ? 0xffffffffu : ((2u << (xr & 31)) - 1u);
+                        if (m) {
+                            const int xp = 32 * w + __ffs(m) - 1;
+                            const unsigned d2 = rowd2 + (unsigned)((xp - x) * (xp - x));
+                            const unsigned long long key = ((unsigned long long)d2 << 24) | ((unsigned)xp << 16) |
+                                                           ((unsigned)yy << 8) | (unsigned)zz;
+                            best = key < best ? key : best;
+                            break;
+                        }
+                    }
+            }
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                const unsigned long long other = __shfl_xor_sync(~0u, best, o);
+                best = other < best ? other : best;
+            }
+            const bool covers = z - R <= 0 && z + R >= L0 - 1 && y - R <= 0 && y + R >= L1 - 1 && x - R <= 0 &&
+                                x + R >= W - 1;
+            if ((best >> 24) < (unsigned long long)(R + 1) * (R + 1) || covers) break;
+        }
+        if (lane != 0) continue;
+        if (best == ~0ull) {  // no background in the item
+            atomicExch(&todo[item], 1);
+            continue;
+        }
+        const unsigned d2 = (unsigned)(best >> 24);
+        const int xp = (int)((best >> 16) & 255u), yp = (int)((best >> 8) & 255u), zp = (int)(best & 255u);
+        const int64_t gi = item * p.numel_item + ((int64_t)z * L1 + y) * W + x;
+        if (dist) dist[gi] = __fsqrt_rn((float)d2);
+        if (sqdist) sqdist[gi] = (int32_t)d2;
+        if (indices) {
+            indices[gi] = zp;
+            indices[p.numel + gi] = yp;
+            indices[2 * p.numel + gi] = xp;
+        }
     }
 }
 
@@ -1612,8 +1730,15 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
         uint32_t *bm = reinterpret_cast<uint32_t *>(c2);
         todo = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(c2) + align256((size_t)nwords * 4));
         // per-item flags, then (8-byte aligned) the shell kernel's 64-bit work
-        // counter: zeroed by the bitmap kernel
-        const int nclear = (int)((g.batch + 1) & ~(int64_t)1) + 2;
+        // counter and the length of its unresolved-voxel list: zeroed by the
+        // bitmap kernel.  The list follows, in the rest of the region.
+        const int nclear = (int)((g.batch + 1) & ~(int64_t)1) + 4;
+        const size_t list_off = align256((size_t)nwords * 4) + align256((size_t)nclear * 4);
+        const size_t region = align256(n * 4);
+        unsigned long long *ulist =
+            reinterpret_cast<unsigned long long *>(reinterpret_cast<unsigned char *>(c2) + list_off);
+        const unsigned ucap =
+            list_off < region ? (unsigned)std::min<size_t>(kPatchCap, (region - list_off) / 8) : 0u;
         if (g.batch > ((int64_t)1 << 30)) return fail(TM_ERR_TOO_LARGE, "batch too large");
         const unsigned bblocks = (unsigned)std::min<int64_t>(ceil_div(nwords, 256), (int64_t)sm_count() * 16);
         const bool vrow = (p.L2 % 32) == 0 && ((uintptr_t)input & 15) == 0;
@@ -1646,7 +1771,12 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
             const int64_t wunits = g.batch * (int64_t)p.L0 * ceil_div(p.L1, kShellWarpRows);
             const int64_t grid = std::min<int64_t>(cached_ctas, ceil_div(wunits, kShellCtWarps));
             TM_CHECK_CUDA(launch_pdl(kernel, dim3((unsigned)grid), dim3(kShellCtThreads), 0, stream, bm, dist,
-                                     indices, sqdist, todo, p));
+                                     indices, sqdist, todo, p, ulist, ucap));
+            TM_LAUNCH_CHECK("edt_shell_ct_kernel");
+            TM_CHECK_CUDA(launch_pdl(edt_patch_kernel, dim3((unsigned)sm_count()), dim3(kPatchThreads), 0, stream,
+                                     (const uint32_t *)bm, dist, indices, sqdist, todo, p,
+                                     (const unsigned long long *)ulist, ucap));
+            TM_LAUNCH_CHECK("edt_patch_kernel");
             return TM_OK;
         };
         if (ww == 4) {  // rows of 97..128 voxels: straight-line search
@@ -1672,7 +1802,7 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
             TM_CHECK_CUDA(cudaFuncSetAttribute(edt_c0_smem_kernel<uint8_t>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         }
-        // after the shell search, overlap this launch with its last CTAs
+        // after the shell search and its patch pass, overlap this launch with their last CTAs
         if (in_dtype == TM_F32) {
             const float *in = static_cast<const float *>(input);
             if (todo)
