@@ -111,21 +111,18 @@ __device__ __forceinline__ bool widen(int q, int L, GF G, uint32_t &best, int &b
 // per column, each sweeping a quarter of the column; the quarters exchange
 // their first/last background position through shared memory.
 template <typename In>
-__global__ void __launch_bounds__(kCols *kSegs) edt_c0_smem_kernel(const In *__restrict__ in,
-                                                                   int16_t *__restrict__ c1, CompactParams p,
-                                                                   const int *__restrict__ todo) {
+__device__ __forceinline__ void edt_c0_smem_block(const int64_t blk, const In *__restrict__ in,
+                                                  int16_t *__restrict__ c1, const CompactParams &p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    pdl_wait();  // launched after the shell search and its patch pass: the flags are complete
     const int L = p.L0;
     const int64_t inner = p.numel_item / L;
-    if (todo && !todo[blockIdx.x / ((inner + kCols - 1) / kCols)]) return;  // item finished by the shell pass
     uint8_t *fg = smem_raw;                                              // [L][kCols]
     int16_t *prev = reinterpret_cast<int16_t *>(smem_raw + L * kCols);   // [L][kCols]
     int16_t *seg_last = prev + L * kCols;                                // [kSegs][kCols]
     int16_t *seg_first = seg_last + kSegs * kCols;                       // [kSegs][kCols]
     const int64_t cblocks = (inner + kCols - 1) / kCols;
-    const int64_t item = blockIdx.x / cblocks;
-    const int64_t c0 = (blockIdx.x - item * cblocks) * kCols;
+    const int64_t item = blk / cblocks;
+    const int64_t c0 = (blk - item * cblocks) * kCols;
     const int64_t base = item * p.numel_item + c0;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // stage: 16 warps take rows w, w+16, ...; lane covers columns 4*lane .. 4*lane+3
@@ -177,6 +174,22 @@ __global__ void __launch_bounds__(kCols *kSegs) edt_c0_smem_kernel(const In *__r
         if (pv == y) next = y;
         const int f = (pv >= 0 && (next < 0 || y - pv <= next - y)) ? pv : next;
         *out = (int16_t)f;
+    }
+}
+
+// Grid-stride over column blocks (one resident wave when per-item flags are
+// given, as for the fused passes).
+template <typename In>
+__global__ void __launch_bounds__(kCols *kSegs) edt_c0_smem_kernel(const In *__restrict__ in,
+                                                                   int16_t *__restrict__ c1, CompactParams p,
+                                                                   const int *__restrict__ todo) {
+    pdl_wait();  // launched after the shell search: its flags are complete
+    const int64_t cblocks = (p.numel_item / p.L0 + kCols - 1) / kCols;
+    const int64_t nblk = p.batch * cblocks;
+    for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+        if (todo && !todo[blk / cblocks]) continue;  // item finished by the shell pass
+        edt_c0_smem_block<In>(blk, in, c1, p);
+        __syncthreads();  // the next block reuses shared memory
     }
 }
 
@@ -699,15 +712,13 @@ __host__ __device__ inline C12Smem c12_smem(int L1, int L2) {
     return m;
 }
 
-__global__ void __launch_bounds__(kC12Threads) edt_c12_kernel(const int16_t *__restrict__ c1, float *__restrict__ dist,
-                                                              int32_t *__restrict__ indices,
-                                                              int32_t *__restrict__ sqdist,
-                                                              int16_t *__restrict__ gstack, CompactParams p,
-                                                              const int *__restrict__ todo) {
+// One plane (block number blk = item * L0 + z) of the fused passes 1 + 2.
+__device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *__restrict__ c1,
+                                              float *__restrict__ dist, int32_t *__restrict__ indices,
+                                              int32_t *__restrict__ sqdist, int16_t *__restrict__ gstack,
+                                              const CompactParams &p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    pdl_wait();  // launched after pass 0: its features are complete
     const int L0 = p.L0, L1 = p.L1, W = p.L2;
-    if (todo && !todo[blockIdx.x / L0]) return;  // item finished by the shell pass
     const C12Smem sm = c12_smem(L1, W);
     float *tab = reinterpret_cast<float *>(smem_raw + sm.tab);
     uint8_t *f0s = smem_raw + sm.f0s + kC12PadTop * W;  // row y at f0s + y * W, y in -4 .. L1+11
@@ -715,8 +726,8 @@ __global__ void __launch_bounds__(kC12Threads) edt_c12_kernel(const int16_t *__r
     int16_t *stk_all = reinterpret_cast<int16_t *>(smem_raw + sm.stk);
     int *colflag = reinterpret_cast<int *>(smem_raw + sm.flag);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int64_t item = blockIdx.x / L0;
-    const int z = (int)(blockIdx.x - item * L0);
+    const int64_t item = blk / L0;
+    const int z = (int)(blk - item * L0);
     const int64_t plane = item * p.numel_item + (int64_t)z * L1 * W;
     const int rowp = sm.rowp;
     for (int i = tid; i < kSqrtTab; i += kC12Threads) tab[i] = __fsqrt_rn((float)i);
@@ -967,6 +978,23 @@ __global__ void __launch_bounds__(kC12Threads) edt_c12_kernel(const int16_t *__r
     }
 }
 
+// Grid-stride over planes: with per-item flags (after the shell search) the
+// grid is one resident wave, so items the search finished cost one flag
+// read per plane.
+__global__ void __launch_bounds__(kC12Threads, 3) edt_c12_kernel(const int16_t *__restrict__ c1, float *__restrict__ dist,
+                                                              int32_t *__restrict__ indices,
+                                                              int32_t *__restrict__ sqdist,
+                                                              int16_t *__restrict__ gstack, CompactParams p,
+                                                              const int *__restrict__ todo) {
+    pdl_wait();  // launched after pass 0: its features are complete
+    const int64_t nblk = p.batch * (int64_t)p.L0;
+    for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+        if (todo && !todo[blk / p.L0]) continue;  // item finished by the shell pass
+        edt_c12_block(blk, c1, dist, indices, sqdist, gstack, p);
+        __syncthreads();  // the next plane reuses shared memory
+    }
+}
+
 // -------------------------------------------------------- shell search
 // 3-D items whose voxels all have a background voxel within squared distance
 // kShellD2 (dense backgrounds, e.g. 10 %): the answer is the first background
@@ -1210,6 +1238,70 @@ __host__ __device__ constexpr ShellList make_shell_list() {
     return l;
 }
 
+// Nearest background of voxel (z, y, x) of one item beyond the radius-4
+// shell (none with |d|^2 <= 16; near the item's faces the shell is cut
+// off).  All 32 lanes of the warp search the cube of Chebyshev radius R on
+// the background bitmap, R = 6, 13, 27, ... until the best squared distance
+// is below (R + 1)^2 (nothing outside the cube can be nearer or tie) or the
+// cube covers the item.  Per row (dz, dy) only the nearest background bit on
+// each side of x can be the row's best.  Among equal squared distances the
+// smallest axis-2 coordinate wins, then axis 1, then axis 0 -- the order of
+// the shell list (|d|^2, dx, dy, dz), which is the separable passes' tie
+// rule (each pass keeps the lower coordinate).  Returns
+// (d2 << 24) | (x' << 16) | (y' << 8) | z', or ~0 if the item has no background.
+__device__ unsigned long long far_search(const uint32_t *__restrict__ ibm, int z, int y, int x, int L0, int L1, int W,
+                                         int lane) {
+    constexpr int WW = 4;
+    unsigned long long best = ~0ull;
+    for (int R = 6;; R = 2 * R + 1) {
+        const int side = 2 * R + 1;
+        const int xl = max(0, x - R), xr = min(W - 1, x + R);
+        for (int k = lane; k < side * side; k += 32) {
+            const int dz = k / side - R, dy = k % side - R;
+            const int zz = z + dz, yy = y + dy;
+            if ((unsigned)zz >= (unsigned)L0 || (unsigned)yy >= (unsigned)L1) continue;
+            const unsigned rowd2 = (unsigned)(dz * dz + dy * dy);
+            if (((unsigned long long)rowd2 << 24) >= best) continue;
+            const uint32_t *row = ibm + ((int64_t)zz * L1 + yy) * WW;
+            for (int w = x >> 5; w >= (xl >> 5); w--) {  // nearest background at x' <= x
+                uint32_t m = row[w];
+                if (w == (x >> 5)) m &= (x & 31) == 31 ? 0xffffffffu : ((2u << (x & 31)) - 1u);
+                if (w == (xl >> 5)) m &= ~((1u << (xl & 31)) - 1u);
+                if (m) {
+                    const int xp = 32 * w + 31 - __clz(m);
+                    const unsigned d2 = rowd2 + (unsigned)((x - xp) * (x - xp));
+                    const unsigned long long key =
+                        ((unsigned long long)d2 << 24) | ((unsigned)xp << 16) | ((unsigned)yy << 8) | (unsigned)zz;
+                    best = key < best ? key : best;
+                    break;
+                }
+            }
+            if (x < xr)
+                for (int w = (x + 1) >> 5; w <= (xr >> 5); w++) {  // nearest background at x' > x
+                    uint32_t m = row[w];
+                    if (w == ((x + 1) >> 5)) m &= ~((1u << ((x + 1) & 31)) - 1u);
+                    if (w == (xr >> 5)) m &= (xr & 31) == 31 ? 0xffffffffu : ((2u << (xr & 31)) - 1u);
+                    if (m) {
+                        const int xp = 32 * w + __ffs(m) - 1;
+                        const unsigned d2 = rowd2 + (unsigned)((xp - x) * (xp - x));
+                        const unsigned long long key =
+                            ((unsigned long long)d2 << 24) | ((unsigned)xp << 16) | ((unsigned)yy << 8) | (unsigned)zz;
+                        best = key < best ? key : best;
+                        break;
+                    }
+                }
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            const unsigned long long other = __shfl_xor_sync(~0u, best, o);
+            best = other < best ? other : best;
+        }
+        const bool covers =
+            z - R <= 0 && z + R >= L0 - 1 && y - R <= 0 && y + R >= L1 - 1 && x - R <= 0 && x + R >= W - 1;
+        if ((best >> 24) < (unsigned long long)(R + 1) * (R + 1) || covers) return best;
+    }
+}
+
 // Shell search with the offset list unrolled at compile time, for rows of
 // WW = 4 words (97..128 voxels).  Each warp works alone on units of 8 rows
 // of one plane taken from a work queue: it stages the background words the
@@ -1217,6 +1309,7 @@ __host__ __device__ constexpr ShellList make_shell_list() {
 // the unit's outputs itself.  Warps synchronise only within themselves, so
 // on one SM some warps write while others stage or search.
 constexpr int kShellCtWarps = 4;
+constexpr unsigned kFarPerUnit = 32;  // voxels beyond the shell searched per 8-row unit at most
 constexpr int kShellCtThreads = 32 * kShellCtWarps;
 constexpr int kShellWarpRows = 8;                        // rows per warp unit (8 rows x 4 words = 32 lanes)
 constexpr int kSwPitch = 6;                              // staged row: 2 zero words, then the row's 4 words
@@ -1230,9 +1323,7 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
                                                                        float *__restrict__ dist,
                                                                        int32_t *__restrict__ indices,
                                                                        int32_t *__restrict__ sqdist,
-                                                                       int *__restrict__ todo, CompactParams p,
-                                                                       unsigned long long *__restrict__ ulist,
-                                                                       unsigned ucap) {
+                                                                       int *__restrict__ todo, CompactParams p) {
     static_assert(WW == 4, "rows of four words (97..128 voxels)");
     static_assert(kShellWarpRows * WW == 32, "one word per lane");
     constexpr ShellList kL = make_shell_list();
@@ -1246,7 +1337,6 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
     const int64_t nunits = p.batch * (int64_t)L0 * ybl;
     // 64-bit work counter after the per-item flags (8-byte aligned), zeroed with them
     unsigned long long *queue = reinterpret_cast<unsigned long long *>(todo + ((p.batch + 1) & ~(int64_t)1));
-    unsigned *ucount = reinterpret_cast<unsigned *>(queue + 1);  // entries of the unresolved-voxel list
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t *bits = bits_all[warp];
     uint32_t *planes = planes_all[warp];
@@ -1339,20 +1429,10 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
             pw[1] = make_uint4(P[4], P[5], P[6], P[7]);
             pw[2] = make_uint4(P[8], 0u, 0u, 0u);
         }
-        if (U) {
-            // voxels beyond the shell (|d|^2 > 16): listed for the patch pass,
-            // which overwrites what is written for them below; when the list
-            // is full the item takes the separable passes instead
-            // (every slot below the capacity is written by the lane that took it,
-            // so the patch pass reads only written entries)
-            const unsigned nu = __popc(U);
-            const unsigned at = atomicAdd(ucount, nu);
-            if (at + nu > ucap || at + nu < at) atomicExch(&todo[item], 1);
-            const int r = lane >> 2, wi = lane & 3;
-            unsigned k = at;
-            for (uint32_t m = U; m && k < ucap; m &= m - 1)
-                ulist[k++] = ((unsigned long long)item << 24) | ((unsigned long long)z << 16) |
-                             ((unsigned long long)(y0 + r) << 8) | (unsigned long long)(32 * wi + __ffs(m) - 1);
+        const unsigned nfar = __reduce_add_sync(~0u, (unsigned)__popc(U));  // voxels beyond the shell
+        if (nfar > kFarPerUnit) {  // many: the item takes the separable passes
+            if (lane == 0) atomicExch(&todo[item], 1);
+            continue;
         }
         __syncwarp();
         // write: lane = 4 consecutive voxels of a row
@@ -1396,111 +1476,33 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
                 }
             }
         }
-        __syncwarp();  // res and bits are free for the next unit
-    }
-}
-
-// Patch pass for the voxels the shell search left (no background with
-// |d|^2 <= 16; near the item's faces the shell is cut off): one warp per
-// listed voxel searches the cube of Chebyshev radius R on the background
-// bitmap, R = 6, 13, 27, ... until the best squared distance is below
-// (R + 1)^2 (nothing outside the cube can be nearer or tie) or the cube
-// covers the item.  Per row (dz, dy) only the nearest background bit on
-// each side of x can be the row's best.  Among equal squared distances the
-// smallest axis-2 coordinate wins, then axis 1, then axis 0 -- the order of
-// the shell list (|d|^2, dx, dy, dz), which is the separable passes' tie
-// rule (each pass keeps the lower coordinate).  An item without background
-// is flagged for the separable passes.
-constexpr int kPatchThreads = 256;
-constexpr unsigned kPatchCap = 4096;  // listed voxels per call at most (more: the separable passes are cheaper)
-
-__global__ void __launch_bounds__(kPatchThreads) edt_patch_kernel(const uint32_t *__restrict__ bm,
-                                                                  float *__restrict__ dist,
-                                                                  int32_t *__restrict__ indices,
-                                                                  int32_t *__restrict__ sqdist, int *__restrict__ todo,
-                                                                  CompactParams p,
-                                                                  const unsigned long long *__restrict__ ulist,
-                                                                  unsigned ucap) {
-    pdl_wait();  // the shell search (and its list) is complete
-    constexpr int WW = 4;
-    const unsigned long long *queue =
-        reinterpret_cast<const unsigned long long *>(todo + ((p.batch + 1) & ~(int64_t)1));
-    const unsigned nlist = min(*reinterpret_cast<const unsigned *>(queue + 1), ucap);
-    const int L0 = p.L0, L1 = p.L1, W = p.L2;
-    const int lane = threadIdx.x & 31;
-    const unsigned gw = (blockIdx.x * kPatchThreads + threadIdx.x) >> 5, nw = (gridDim.x * kPatchThreads) >> 5;
-    for (unsigned e = gw; e < nlist; e += nw) {
-        const unsigned long long v = ulist[e];
-        const int64_t item = (int64_t)(v >> 24);
-        const int z = (int)((v >> 16) & 255u), y = (int)((v >> 8) & 255u), x = (int)(v & 255u);
-        if (item >= p.batch || z >= L0 || y >= L1 || x >= W) continue;  // not an entry of this call
-        if (todo[item]) continue;  // the separable passes redo the item
-        const uint32_t *ibm = bm + item * (int64_t)L0 * L1 * WW;
-        unsigned long long best = ~0ull;  // (d2 << 24) | (x' << 16) | (y' << 8) | z'
-        for (int R = 6;; R = 2 * R + 1) {
-            const int side = 2 * R + 1;
-            const int xl = max(0, x - R), xr = min(W - 1, x + R);
-            for (int k = lane; k < side * side; k += 32) {
-                const int dz = k / side - R, dy = k % side - R;
-                const int zz = z + dz, yy = y + dy;
-                if ((unsigned)zz >= (unsigned)L0 || (unsigned)yy >= (unsigned)L1) continue;
-                const unsigned rowd2 = (unsigned)(dz * dz + dy * dy);
-                if (((unsigned long long)rowd2 << 24) >= best) continue;
-                const uint32_t *row = ibm + ((int64_t)zz * L1 + yy) * WW;
-                // nearest background at x' <= x
-                for (int w = x >> 5; w >= (xl >> 5); w--) {
-                    uint32_t m = row[w];
-                    if (w == (x >> 5)) m &= (x & 31) == 31 ? 0xffffffffu : ((2u << (x & 31)) - 1u);
-                    if (w == (xl >> 5)) m &= ~((1u << (xl & 31)) - 1u);
-                    if (m) {
-                        const int xp = 32 * w + 31 - __clz(m);
-                        const unsigned d2 = rowd2 + (unsigned)((x - xp) * (x - xp));
-                        const unsigned long long key = ((unsigned long long)d2 << 24) | ((unsigned)xp << 16) |
-                                                       ((unsigned)yy << 8) | (unsigned)zz;
-                        best = key < best ? key : best;
-                        break;
+        if (nfar) {
+            // the few voxels beyond the shell: searched by the whole warp, written
+            // after the unit's stores above (ordered by the warp barrier)
+            __syncwarp();
+            for (unsigned has = __ballot_sync(~0u, U != 0u); has; has &= has - 1) {
+                const int src = __ffs(has) - 1;
+                for (uint32_t m = __shfl_sync(~0u, U, src); m; m &= m - 1) {
+                    const int yv = y0 + (src >> 2), xv = 32 * (src & 3) + __ffs(m) - 1;
+                    const unsigned long long best = far_search(ibm, z, yv, xv, L0, L1, W, lane);
+                    if (lane != 0) continue;
+                    if (best == ~0ull) {  // no background in the item
+                        atomicExch(&todo[item], 1);
+                        continue;
+                    }
+                    const unsigned d2 = (unsigned)(best >> 24);
+                    const int64_t gi = rowbase + (int64_t)(yv - y0) * W + xv;
+                    if (dist) dist[gi] = __fsqrt_rn((float)d2);
+                    if (sqdist) sqdist[gi] = (int32_t)d2;
+                    if (indices) {
+                        indices[gi] = (int32_t)(best & 255u);
+                        indices[numel + gi] = (int32_t)((best >> 8) & 255u);
+                        indices[2 * numel + gi] = (int32_t)((best >> 16) & 255u);
                     }
                 }
-                // nearest background at x' > x
-                if (x < xr)
-                    for (int w = (x + 1) >> 5; w <= (xr >> 5); w++) {
-                        uint32_t m = row[w];
-                        if (w == ((x + 1) >> 5)) m &= ~((1u << ((x + 1) & 31)) - 1u);
-                        if (w == (xr >> 5)) m &= (xr & 31) == 31 ? 0xffffffffu : ((2u << (xr & 31)) - 1u);
-                        if (m) {
-                            const int xp = 32 * w + __ffs(m) - 1;
-                            const unsigned d2 = rowd2 + (unsigned)((xp - x) * (xp - x));
-                            const unsigned long long key = ((unsigned long long)d2 << 24) | ((unsigned)xp << 16) |
-                                                           ((unsigned)yy << 8) | (unsigned)zz;
-                            best = key < best ? key : best;
-                            break;
-                        }
-                    }
             }
-#pragma unroll
-            for (int o = 16; o; o >>= 1) {
-                const unsigned long long other = __shfl_xor_sync(~0u, best, o);
-                best = other < best ? other : best;
-            }
-            const bool covers = z - R <= 0 && z + R >= L0 - 1 && y - R <= 0 && y + R >= L1 - 1 && x - R <= 0 &&
-                                x + R >= W - 1;
-            if ((best >> 24) < (unsigned long long)(R + 1) * (R + 1) || covers) break;
         }
-        if (lane != 0) continue;
-        if (best == ~0ull) {  // no background in the item
-            atomicExch(&todo[item], 1);
-            continue;
-        }
-        const unsigned d2 = (unsigned)(best >> 24);
-        const int xp = (int)((best >> 16) & 255u), yp = (int)((best >> 8) & 255u), zp = (int)(best & 255u);
-        const int64_t gi = item * p.numel_item + ((int64_t)z * L1 + y) * W + x;
-        if (dist) dist[gi] = __fsqrt_rn((float)d2);
-        if (sqdist) sqdist[gi] = (int32_t)d2;
-        if (indices) {
-            indices[gi] = zp;
-            indices[p.numel + gi] = yp;
-            indices[2 * p.numel + gi] = xp;
-        }
+        __syncwarp();  // res and bits are free for the next unit
     }
 }
 
@@ -1693,6 +1695,15 @@ bool edt_compact_eligible(const Geometry &g, bool unit) {
     return true;
 }
 
+// CTAs of one kernel resident at once on the device (one wave), at least one.
+template <typename K>
+int64_t wave_ctas(K kernel, int threads, size_t smem) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return (int64_t)per_sm * sm_count();
+}
+
 size_t edt_compact_workspace(const Geometry &g) {
     const size_t n = (size_t)g.numel;
     size_t s = align256(n * 2);                               // f0 per voxel
@@ -1730,15 +1741,8 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
         uint32_t *bm = reinterpret_cast<uint32_t *>(c2);
         todo = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(c2) + align256((size_t)nwords * 4));
         // per-item flags, then (8-byte aligned) the shell kernel's 64-bit work
-        // counter and the length of its unresolved-voxel list: zeroed by the
-        // bitmap kernel.  The list follows, in the rest of the region.
-        const int nclear = (int)((g.batch + 1) & ~(int64_t)1) + 4;
-        const size_t list_off = align256((size_t)nwords * 4) + align256((size_t)nclear * 4);
-        const size_t region = align256(n * 4);
-        unsigned long long *ulist =
-            reinterpret_cast<unsigned long long *>(reinterpret_cast<unsigned char *>(c2) + list_off);
-        const unsigned ucap =
-            list_off < region ? (unsigned)std::min<size_t>(kPatchCap, (region - list_off) / 8) : 0u;
+        // counter: zeroed by the bitmap kernel
+        const int nclear = (int)((g.batch + 1) & ~(int64_t)1) + 2;
         if (g.batch > ((int64_t)1 << 30)) return fail(TM_ERR_TOO_LARGE, "batch too large");
         const unsigned bblocks = (unsigned)std::min<int64_t>(ceil_div(nwords, 256), (int64_t)sm_count() * 16);
         const bool vrow = (p.L2 % 32) == 0 && ((uintptr_t)input & 15) == 0;
@@ -1771,12 +1775,7 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
             const int64_t wunits = g.batch * (int64_t)p.L0 * ceil_div(p.L1, kShellWarpRows);
             const int64_t grid = std::min<int64_t>(cached_ctas, ceil_div(wunits, kShellCtWarps));
             TM_CHECK_CUDA(launch_pdl(kernel, dim3((unsigned)grid), dim3(kShellCtThreads), 0, stream, bm, dist,
-                                     indices, sqdist, todo, p, ulist, ucap));
-            TM_LAUNCH_CHECK("edt_shell_ct_kernel");
-            TM_CHECK_CUDA(launch_pdl(edt_patch_kernel, dim3((unsigned)sm_count()), dim3(kPatchThreads), 0, stream,
-                                     (const uint32_t *)bm, dist, indices, sqdist, todo, p,
-                                     (const unsigned long long *)ulist, ucap));
-            TM_LAUNCH_CHECK("edt_patch_kernel");
+                                     indices, sqdist, todo, p));
             return TM_OK;
         };
         if (ww == 4) {  // rows of 97..128 voxels: straight-line search
@@ -1802,21 +1801,27 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
             TM_CHECK_CUDA(cudaFuncSetAttribute(edt_c0_smem_kernel<uint8_t>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         }
-        // after the shell search and its patch pass, overlap this launch with their last CTAs
+        // after the shell search: overlap this launch with its last CTAs, one
+        // resident wave striding over the column blocks
         if (in_dtype == TM_F32) {
             const float *in = static_cast<const float *>(input);
-            if (todo)
-                TM_CHECK_CUDA(launch_pdl(edt_c0_smem_kernel<float>, dim3((unsigned)blocks), dim3(kCols * kSegs), smem,
+            if (todo) {
+                const int64_t grid = std::min<int64_t>(blocks, wave_ctas(edt_c0_smem_kernel<float>, kCols * kSegs, smem));
+                TM_CHECK_CUDA(launch_pdl(edt_c0_smem_kernel<float>, dim3((unsigned)grid), dim3(kCols * kSegs), smem,
                                          stream, in, c1, p, (const int *)todo));
-            else
+            } else {
                 edt_c0_smem_kernel<float><<<(unsigned)blocks, kCols * kSegs, smem, stream>>>(in, c1, p, todo);
+            }
         } else {
             const uint8_t *in = static_cast<const uint8_t *>(input);
-            if (todo)
-                TM_CHECK_CUDA(launch_pdl(edt_c0_smem_kernel<uint8_t>, dim3((unsigned)blocks), dim3(kCols * kSegs),
+            if (todo) {
+                const int64_t grid =
+                    std::min<int64_t>(blocks, wave_ctas(edt_c0_smem_kernel<uint8_t>, kCols * kSegs, smem));
+                TM_CHECK_CUDA(launch_pdl(edt_c0_smem_kernel<uint8_t>, dim3((unsigned)grid), dim3(kCols * kSegs),
                                          smem, stream, in, c1, p, (const int *)todo));
-            else
+            } else {
                 edt_c0_smem_kernel<uint8_t><<<(unsigned)blocks, kCols * kSegs, smem, stream>>>(in, c1, p, todo);
+            }
         }
         TM_LAUNCH_CHECK("edt_c0_smem_kernel");
     } else {
@@ -1837,7 +1842,8 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
             TM_CHECK_CUDA(cudaFuncSetAttribute(edt_c12_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)smem));
         // launched after pass 0 (whose kernel runs normally when there is no shell search)
-        TM_CHECK_CUDA(launch_pdl(edt_c12_kernel, dim3((unsigned)blocks), dim3(kC12Threads), smem, stream,
+        const int64_t grid = todo ? std::min<int64_t>(blocks, wave_ctas(edt_c12_kernel, kC12Threads, smem)) : blocks;
+        TM_CHECK_CUDA(launch_pdl(edt_c12_kernel, dim3((unsigned)grid), dim3(kC12Threads), smem, stream,
                                  (const int16_t *)c1, dist, indices, sqdist, stack1, p, (const int *)todo));
         TM_LAUNCH_CHECK("edt_c12_kernel");
         return TM_OK;
