@@ -82,26 +82,55 @@ __device__ __forceinline__ void next_tile(PlanHeader *hdr, const RaggedItem *ite
 }
 
 // Stage rows [gy0, gy0 + RH) x columns [gx0, gx0 + RW) of one image into
-// shared memory (row stride ld), mapping out-of-image coordinates.
+// shared memory (row stride ld), mapping out-of-image coordinates.  Warp w
+// takes rows w, w + 8, ...; a lane issues the loads of 2 rows x up to 5
+// column chunks before it stores any, so a warp keeps many loads in flight
+// (tiles inside the image; border tiles map every coordinate, one row at a
+// time).
 template <typename T>
 __device__ __forceinline__ void stage_tile(const T *src, int H, int W, int gy0, int gx0, int RH, int RW, int ld,
                                            int mode, T cval, T *tile) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nwarps = kFlatThreads / 32;
+    constexpr int nwarps = kFlatThreads / 32, RB = 2, NC = 5;
     const bool interior = gy0 >= 0 && gx0 >= 0 && gy0 + RH <= H && gx0 + RW <= W;
-    for (int r = warp; r < RH; r += nwarps) {
-        const int gy = gy0 + r;
-        const int my = interior ? gy : map_coord(gy, H, mode);
-        for (int c = lane; c < RW; c += 32) {
-            const int gx = gx0 + c;
-            T v;
-            if (interior) {
-                v = src[(int64_t)gy * W + gx];
-            } else {
-                const int mx = map_coord(gx, W, mode);
-                v = (my < 0 || mx < 0) ? cval : src[(int64_t)my * W + mx];
+    if (interior) {
+        for (int rb = warp; rb < RH; rb += nwarps * RB)
+            for (int cb = 0; cb < RW; cb += 32 * NC) {
+                T v[RB][NC];
+#pragma unroll
+                for (int k = 0; k < RB; k++)
+#pragma unroll
+                    for (int j = 0; j < NC; j++) {
+                        const int r = rb + nwarps * k, c = cb + lane + 32 * j;
+                        if (r < RH && c < RW) v[k][j] = src[(int64_t)(gy0 + r) * W + gx0 + c];
+                    }
+#pragma unroll
+                for (int k = 0; k < RB; k++)
+#pragma unroll
+                    for (int j = 0; j < NC; j++) {
+                        const int r = rb + nwarps * k, c = cb + lane + 32 * j;
+                        if (r < RH && c < RW) tile[r * ld + c] = v[k][j];
+                    }
             }
-            tile[r * ld + c] = v;
+        return;
+    }
+    for (int r = warp; r < RH; r += nwarps) {
+        const int my = map_coord(gy0 + r, H, mode);
+        for (int cb = 0; cb < RW; cb += 32 * NC) {
+            T v[NC];
+#pragma unroll
+            for (int j = 0; j < NC; j++) {
+                const int c = cb + lane + 32 * j;
+                if (c < RW) {
+                    const int mx = map_coord(gx0 + c, W, mode);
+                    v[j] = (my < 0 || mx < 0) ? cval : src[(int64_t)my * W + mx];
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < NC; j++) {
+                const int c = cb + lane + 32 * j;
+                if (c < RW) tile[r * ld + c] = v[j];
+            }
         }
     }
 }
@@ -142,7 +171,12 @@ __global__ void __launch_bounds__(kFlatThreads) ragged_flat_kernel(const T *__re
     }
 }
 
-template <typename T, bool MAX>
+// Tap loop over a staged tile.  With a compile-time row pitch P (taps
+// spanning at most 33 rows and P - 128 + 1 columns) a thread owns one column
+// and 16 rows, runs the taps in the outer loop at one shared-memory offset
+// each, and keeps the 16 results in registers; P = 0 is the general case
+// (one output at a time).  Per output the taps combine in the same order.
+template <typename T, bool MAX, int P>
 __global__ void __launch_bounds__(kFlatThreads) ragged_taps_kernel(const T *__restrict__ in, T *__restrict__ out,
                                                                    PlanHeader *hdr, const RaggedItem *__restrict__ items,
                                                                    const __grid_constant__ RaggedTaps taps, int mode,
@@ -151,6 +185,7 @@ __global__ void __launch_bounds__(kFlatThreads) ragged_taps_kernel(const T *__re
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_slot[2];
     const int RH = kTileH + taps.ext_y, RW = kTileW + taps.ext_x;
+    const int ld = P ? P : RW;
     T *tile = reinterpret_cast<T *>(smem_raw);
     for (;;) {
         next_tile(hdr, items, s_slot);
@@ -160,18 +195,41 @@ __global__ void __launch_bounds__(kFlatThreads) ragged_taps_kernel(const T *__re
         const int local = t - it.tile_begin;
         const int ty = local / it.tiles_x, tx = local - ty * it.tiles_x;
         const int x0 = tx * kTileW, y0 = ty * kTileH;
-        stage_tile<T>(in + it.off, it.H, it.W, y0 + taps.min_y, x0 + taps.min_x, RH, RW, RW, mode, (T)cval, tile);
+        stage_tile<T>(in + it.off, it.H, it.W, y0 + taps.min_y, x0 + taps.min_x, RH, RW, ld, mode, (T)cval, tile);
         __syncthreads();
         T *dst = out + it.off;
-        for (int e = threadIdx.x; e < kTileH * kTileW; e += kFlatThreads) {
-            const int r = e / kTileW, c = e % kTileW;
-            const int gy = y0 + r, gx = x0 + c;
-            if (gy >= it.H || gx >= it.W) continue;
-            T acc = Op::identity();
-            for (int k = 0; k < taps.n; k++)
-                acc = Op::combine(acc, Op::apply(tile[(r + taps.dy[k] - taps.min_y) * RW + c + taps.dx[k] - taps.min_x],
-                                                 taps.val[k]));
-            dst[(int64_t)gy * it.W + gx] = acc;
+        if constexpr (P != 0) {
+            constexpr int kRows = kTileH * kTileW / kFlatThreads;  // 16
+            const int c = threadIdx.x % kTileW, r0 = (threadIdx.x / kTileW) * kRows;
+            T acc[kRows];
+#pragma unroll
+            for (int i = 0; i < kRows; i++) acc[i] = Op::identity();
+            const T *base = tile + r0 * P + c;
+            for (int k = 0; k < taps.n; k++) {
+                const T *q = base + (taps.dy[k] - taps.min_y) * P + (taps.dx[k] - taps.min_x);
+                const float sv = taps.val[k];
+#pragma unroll
+                for (int i = 0; i < kRows; i++) acc[i] = Op::combine(acc[i], Op::apply(q[i * P], sv));
+            }
+            const int gx = x0 + c;
+            if (gx < it.W) {
+#pragma unroll
+                for (int i = 0; i < kRows; i++) {
+                    const int gy = y0 + r0 + i;
+                    if (gy < it.H) dst[(int64_t)gy * it.W + gx] = acc[i];
+                }
+            }
+        } else {
+            for (int e = threadIdx.x; e < kTileH * kTileW; e += kFlatThreads) {
+                const int r = e / kTileW, c = e % kTileW;
+                const int gy = y0 + r, gx = x0 + c;
+                if (gy >= it.H || gx >= it.W) continue;
+                T acc = Op::identity();
+                for (int k = 0; k < taps.n; k++)
+                    acc = Op::combine(acc, Op::apply(tile[(r + taps.dy[k] - taps.min_y) * RW + c + taps.dx[k] - taps.min_x],
+                                                     taps.val[k]));
+                dst[(int64_t)gy * it.W + gx] = acc;
+            }
         }
         __syncthreads();
     }
@@ -295,8 +353,12 @@ int run_ragged(const T *in, T *out, const void *plan, size_t plan_bytes, int64_t
     taps.min_x = min_x;
     taps.ext_y = max_y - min_y;
     taps.ext_x = max_x - min_x;
-    const size_t smem = (size_t)(kTileH + taps.ext_y) * (kTileW + taps.ext_x) * sizeof(T);
-    auto kernel = ragged_taps_kernel<T, MAX>;
+    // compile-time pitch for taps spanning up to 33 rows and 9 or 33 columns
+    const int P = taps.ext_y > 32 ? 0 : taps.ext_x <= 8 ? 136 : taps.ext_x <= 32 ? 160 : 0;
+    const size_t smem = (size_t)(kTileH + taps.ext_y) * (P ? P : kTileW + taps.ext_x) * sizeof(T);
+    auto kernel = P == 136 ? ragged_taps_kernel<T, MAX, 136>
+                  : P == 160 ? ragged_taps_kernel<T, MAX, 160>
+                             : ragged_taps_kernel<T, MAX, 0>;
     int grid = 0;
     int st = persistent_grid(kernel, smem, &grid);
     if (st != TM_OK) return st;
