@@ -237,6 +237,29 @@ def test_edt_shell_patch_and_overflow(cuda, seed):
 
 
 @pytest.mark.parametrize("metric", ["chessboard", "taxicab", "chamfer345"])
+def test_chamfer_far_voxels(cuda, metric):
+    """Voxels whose nearest background lies beyond the radius-4 shell's classes are
+    searched on the bitmap (the 9^3 block's centre; taxicab and 3-4-5 voxels at
+    Bernoulli(0.9)); a unit with many of them (the ball, the all-foreground item) sends
+    its item to the raster passes.  Fast path == raster passes == oracle."""
+    r = rng(7)
+    shape = (4, 1, 40, 50, 128)
+    x = r.random(shape) < 0.9
+    x[0, 0, 10:19, 20:29, 60:69] = True
+    zz, yy, xx = np.meshgrid(np.arange(40), np.arange(50), np.arange(128), indexing="ij")
+    x[1, 0] |= (zz - 20) ** 2 + (yy - 25) ** 2 + (xx - 64) ** 2 <= 144
+    x[2] = True
+    t = torch.from_numpy(x).cuda()
+    d_fast, _ = _C.cdt(t, metric, True, False)
+    d_ref, _ = _C.cdt(t, metric, True, True)
+    np.testing.assert_array_equal(d_fast.cpu().numpy(), d_ref.cpu().numpy())
+    d_o, _ = oracle.cdt(x, metric)
+    if metric == "chamfer345":  # the oracle counts thirds
+        d_o = np.where(d_o < 0, -1.0, d_o.astype(np.float32) / np.float32(3.0)).astype(np.float32)
+    np.testing.assert_array_equal(d_fast.cpu().numpy(), d_o)
+
+
+@pytest.mark.parametrize("metric", ["chessboard", "taxicab", "chamfer345"])
 @pytest.mark.parametrize("shape,p", [((2, 1, 20, 33, 128), 0.9), ((1, 2, 9, 40, 100), 0.85),
                                      ((3, 1, 12, 16, 128), 0.999)])
 def test_chamfer_distances_bitmap_path_vs_raster(cuda, metric, shape, p):

@@ -1544,8 +1544,10 @@ int upload_shell_table() {
 // 3a + b + c for |d| sorted a >= b >= c (in thirds).  For distances only,
 // the offsets of the radius-4 cube with norm <= kCdtVmax(metric) are grouped
 // by norm; per 32-voxel word the union of a class's shifted background
-// masks resolves every voxel whose nearest background has that norm.
-// Unresolved voxels mark their item for the raster passes.
+// masks resolves every voxel whose nearest background has that norm.  The
+// few voxels left (nearest background beyond the class bound) are searched
+// on the bitmap; a unit with many of them marks its item for the raster
+// passes.
 __host__ __device__ constexpr int cdt_norm(int metric, int dz, int dy, int dx) {
     int a = dz < 0 ? -dz : dz, b = dy < 0 ? -dy : dy, c = dx < 0 ? -dx : dx;
     if (metric == 0) return a > b ? (a > c ? a : c) : (b > c ? b : c);  // chessboard
@@ -1594,6 +1596,57 @@ __host__ __device__ constexpr CdtShellList make_cdt_list(int metric) {
     return l;
 }
 
+// Smallest chamfer norm from voxel (z, y, x) of one item to a background
+// voxel beyond the shell, by the whole warp on the bitmap: cubes of
+// Chebyshev radius R = 6, 13, 27, ... until the best norm is at most the
+// smallest norm outside the cube (R + 1, or 3 (R + 1) for 3-4-5) or the cube
+// covers the item.  Each norm grows with |dx| for fixed (dz, dy), so per row
+// the nearest background bit on either side of x is the row's best.
+// Returns -1 if the item has no background.
+template <int MET>
+__device__ int far_norm_search(const uint32_t *__restrict__ ibm, int z, int y, int x, int L0, int L1, int W,
+                               int lane) {
+    constexpr int WW = 4;
+    int best = 0x7fffffff;
+    for (int R = 6;; R = 2 * R + 1) {
+        const int side = 2 * R + 1;
+        const int xl = max(0, x - R), xr = min(W - 1, x + R);
+        for (int k = lane; k < side * side; k += 32) {
+            const int dz = k / side - R, dy = k % side - R;
+            const int zz = z + dz, yy = y + dy;
+            if ((unsigned)zz >= (unsigned)L0 || (unsigned)yy >= (unsigned)L1) continue;
+            if (cdt_norm(MET, dz, dy, 0) >= best) continue;
+            const uint32_t *row = ibm + ((int64_t)zz * L1 + yy) * WW;
+            for (int w = x >> 5; w >= (xl >> 5); w--) {  // nearest background at x' <= x
+                uint32_t m = row[w];
+                if (w == (x >> 5)) m &= (x & 31) == 31 ? 0xffffffffu : ((2u << (x & 31)) - 1u);
+                if (w == (xl >> 5)) m &= ~((1u << (xl & 31)) - 1u);
+                if (m) {
+                    best = min(best, cdt_norm(MET, dz, dy, x - (32 * w + 31 - __clz(m))));
+                    break;
+                }
+            }
+            if (x < xr)
+                for (int w = (x + 1) >> 5; w <= (xr >> 5); w++) {  // nearest background at x' > x
+                    uint32_t m = row[w];
+                    if (w == ((x + 1) >> 5)) m &= ~((1u << ((x + 1) & 31)) - 1u);
+                    if (w == (xr >> 5)) m &= (xr & 31) == 31 ? 0xffffffffu : ((2u << (xr & 31)) - 1u);
+                    if (m) {
+                        best = min(best, cdt_norm(MET, dz, dy, 32 * w + __ffs(m) - 1 - x));
+                        break;
+                    }
+                }
+        }
+        best = __reduce_min_sync(~0u, best);
+        const int outside = MET == 2 ? 3 * (R + 1) : R + 1;
+        const bool covers =
+            z - R <= 0 && z + R >= L0 - 1 && y - R <= 0 && y + R >= L1 - 1 && x - R <= 0 && x + R >= W - 1;
+        if (best <= outside || covers) return best == 0x7fffffff ? -1 : best;
+    }
+}
+
+constexpr int kCdtFarPerUnit = 64;  // voxels beyond the shell searched per 32-row unit at most
+
 template <int WW, int MET>
 __global__ void __launch_bounds__(kShellThreads) cdt_shell_kernel(const uint32_t *__restrict__ bm,
                                                                   float *__restrict__ dist, int *__restrict__ todo,
@@ -1604,7 +1657,7 @@ __global__ void __launch_bounds__(kShellThreads) cdt_shell_kernel(const uint32_t
     constexpr int kPlaneP = kRowsP * kPitch;
     __shared__ __align__(16) uint32_t bits[(2 * kShellR + 1) * kPlaneP];
     __shared__ __align__(16) uint8_t res[kShellRows * WW * 32];
-    __shared__ int s_unresolved;
+    __shared__ int s_nfar;
     const int L0 = p.L0, L1 = p.L1, W = p.L2;
     const int ybl = (L1 + kShellRows - 1) / kShellRows;
     const int64_t item = blockIdx.x / ((int64_t)L0 * ybl);
@@ -1612,7 +1665,7 @@ __global__ void __launch_bounds__(kShellThreads) cdt_shell_kernel(const uint32_t
     const int z = rem / ybl, y0 = (rem % ybl) * kShellRows;
     const int nrows = min(kShellRows, L1 - y0);
     const int tid = threadIdx.x;
-    if (tid == 0) s_unresolved = 0;
+    if (tid == 0) s_nfar = 0;
     const uint32_t *ibm = bm + item * (int64_t)L0 * L1 * WW;
     for (int i = tid; i < (2 * kShellR + 1) * kRowsP; i += kShellThreads) {
         const int k = i / kRowsP, r = i - k * kRowsP;
@@ -1626,6 +1679,8 @@ __global__ void __launch_bounds__(kShellThreads) cdt_shell_kernel(const uint32_t
         for (int c = 0; c < WW; c++) dst[kShellPadW + c] = in_item ? src[c] : 0u;
     }
     __syncthreads();
+    static_assert(kShellRows * WW <= kShellThreads, "one word per thread");
+    uint32_t Ufar = 0;  // voxels of this thread's word beyond the shell
     for (int e = tid; e < nrows * WW; e += kShellThreads) {
         const int r = e / WW, wi = e % WW;
         const int nb = min(32, W - 32 * wi);
@@ -1652,10 +1707,12 @@ __global__ void __launch_bounds__(kShellThreads) cdt_shell_kernel(const uint32_t
                 if (U == 0u) break;
             }
         }
-        if (U) s_unresolved = 1;
+        if (U) atomicAdd(&s_nfar, __popc(U));
+        Ufar = U;
     }
     __syncthreads();
-    if (s_unresolved) {
+    const int nfar = s_nfar;
+    if (nfar > kCdtFarPerUnit) {  // many voxels beyond the shell: the item takes the raster passes
         if (tid == 0) atomicExch(&todo[item], 1);
         return;
     }
@@ -1673,6 +1730,21 @@ __global__ void __launch_bounds__(kShellThreads) cdt_shell_kernel(const uint32_t
             d.w = divisor == 1.f ? (float)(v4 >> 24) : (float)(v4 >> 24) / divisor;
             (void)inv;
             *reinterpret_cast<float4 *>(dist + rowbase + (int64_t)r * W + x) = d;
+        }
+    }
+    if (nfar == 0) return;
+    // the few voxels beyond the shell: each warp searches its own threads'
+    // voxels and overwrites what was written for them above (block barrier)
+    __syncthreads();
+    for (unsigned has = __ballot_sync(~0u, Ufar != 0u); has; has &= has - 1) {
+        const int src = __ffs(has) - 1;
+        const int e = warp * 32 + src, r = e / WW, wi = e % WW;
+        for (uint32_t m = __shfl_sync(~0u, Ufar, src); m; m &= m - 1) {
+            const int xv = 32 * wi + __ffs(m) - 1;
+            const int best = far_norm_search<MET>(ibm, z, y0 + r, xv, L0, L1, W, lane);
+            if (lane != 0) continue;
+            if (best < 0) atomicExch(&todo[item], 1);  // no background: the raster passes give -1
+            else dist[rowbase + (int64_t)r * W + xv] = divisor == 1.f ? (float)best : (float)best / divisor;
         }
     }
 }
