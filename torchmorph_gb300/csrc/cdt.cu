@@ -63,13 +63,18 @@ __device__ __forceinline__ int tau_of_row(uint32_t r, const CdtParams &p) {
     return tau;
 }
 
-__global__ void cdt_count_kernel(int *__restrict__ cnt, CdtParams p) {
+__global__ void cdt_count_kernel(int *__restrict__ cnt, CdtParams p, const int *__restrict__ any) {
+    pdl_wait();
+    if (any && !*any) return;  // the shell search finished every item
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < p.rows; r += gridDim.x * blockDim.x)
         atomicAdd(&cnt[tau_of_row((uint32_t)r, p)], 1);
 }
 
 // Exclusive scan of T counters (single CTA); off[T] = total.
-__global__ void cdt_scan_kernel(const int *__restrict__ cnt, int *__restrict__ off, int T) {
+__global__ void cdt_scan_kernel(const int *__restrict__ cnt, int *__restrict__ off, int T,
+                                const int *__restrict__ any) {
+    pdl_wait();
+    if (any && !*any) return;
     __shared__ int carry;
     __shared__ int warp_sums[32];
     if (threadIdx.x == 0) carry = 0;
@@ -104,7 +109,9 @@ __global__ void cdt_scan_kernel(const int *__restrict__ cnt, int *__restrict__ o
 }
 
 __global__ void cdt_scatter_kernel(const int *__restrict__ off, int *__restrict__ cursor,
-                                   int *__restrict__ order, CdtParams p) {
+                                   int *__restrict__ order, CdtParams p, const int *__restrict__ any) {
+    pdl_wait();
+    if (any && !*any) return;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < p.rows; r += gridDim.x * blockDim.x) {
         int t = tau_of_row((uint32_t)r, p);
         int pos = atomicAdd(&cursor[t], 1);
@@ -116,7 +123,10 @@ __global__ void cdt_scatter_kernel(const int *__restrict__ off, int *__restrict_
 // others were finished by the bitmap shell search and are left alone.
 template <typename In>
 __global__ void cdt_init_kernel(const In *__restrict__ in, int32_t *__restrict__ dt, int32_t *__restrict__ ft,
-                                int64_t numel, int64_t numel_item, const int *__restrict__ todo) {
+                                int64_t numel, int64_t numel_item, const int *__restrict__ todo,
+                                const int *__restrict__ any) {
+    pdl_wait();
+    if (any && !*any) return;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < numel;
          i += (int64_t)gridDim.x * blockDim.x) {
         if (todo && !todo[i / numel_item]) continue;
@@ -138,7 +148,10 @@ template <bool BACKWARD>
 __global__ void __launch_bounds__(kCdtThreads) cdt_pass_kernel(int32_t *__restrict__ dt, int32_t *__restrict__ ft,
                                                                const int *__restrict__ order,
                                                                const int *__restrict__ woff, CdtParams p,
-                                                               CdtOffsets offs, const int *__restrict__ todo) {
+                                                               CdtOffsets offs, const int *__restrict__ todo,
+                                                               const int *__restrict__ any) {
+    pdl_wait();
+    if (any && !*any) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
     const int nd = p.ndim;
@@ -239,7 +252,9 @@ __global__ void __launch_bounds__(kCdtThreads) cdt_pass_kernel(int32_t *__restri
 __global__ void cdt_finalize_kernel(const int32_t *__restrict__ dt, const int32_t *__restrict__ ft,
                                     float *__restrict__ dist, int32_t *__restrict__ indices, int64_t numel,
                                     int64_t numel_item, int ndim, CdtParams p, float divisor,
-                                    const int *__restrict__ todo) {
+                                    const int *__restrict__ todo, const int *__restrict__ any) {
+    pdl_wait();
+    if (any && !*any) return;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < numel;
          i += (int64_t)gridDim.x * blockDim.x) {
         if (todo && !todo[i / numel_item]) continue;
@@ -286,9 +301,16 @@ CdtPlan plan_cdt(const Geometry &g) {
     return pl;
 }
 
+// Zero the wavefront counters of the raster passes (before their launches).
+cudaError_t clear_cdt_counters(unsigned char *ws, const CdtPlan &pl, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(ws + pl.cnt_off, 0, (size_t)pl.T * 4, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ws + pl.cur_off, 0, (size_t)pl.T * 4, stream);
+    return e;
+}
+
 template <typename In>
 int run_cdt(const In *in, const Geometry &g, int metric, float *dist, int32_t *indices, unsigned char *ws,
-            const CdtPlan &pl, const int *todo, cudaStream_t stream) {
+            const CdtPlan &pl, const int *todo, bool counters_cleared, cudaStream_t stream) {
     const int nd = g.ndim;
     CdtParams p;
     std::memset(&p, 0, sizeof(p));
@@ -334,25 +356,29 @@ int run_cdt(const In *in, const Geometry &g, int metric, float *dist, int32_t *i
     int *cnt = reinterpret_cast<int *>(ws + pl.cnt_off);
     int *cur = reinterpret_cast<int *>(ws + pl.cur_off);
     const int sms = sm_count();
-    TM_CHECK_CUDA(cudaMemsetAsync(cnt, 0, (size_t)pl.T * 4, stream));
-    TM_CHECK_CUDA(cudaMemsetAsync(cur, 0, (size_t)pl.T * 4, stream));
+    if (!counters_cleared) TM_CHECK_CUDA(clear_cdt_counters(ws, pl, stream));
+    // after the shell search (todo given): every kernel is launched as a
+    // programmatic dependent of the previous one and returns at once when no
+    // item was marked (the flag after the per-item flags)
+    const int *any = todo ? todo + g.batch : nullptr;
+    auto go = [&](auto kernel, unsigned grid, unsigned block, auto... args) -> cudaError_t {
+        if (todo) return launch_pdl(kernel, dim3(grid), dim3(block), 0, stream, args...);
+        kernel<<<grid, block, 0, stream>>>(args...);
+        return cudaGetLastError();
+    };
     unsigned rb = (unsigned)std::min<int64_t>(ceil_div(pl.rows, 256), sms * 4);
-    cdt_count_kernel<<<rb, 256, 0, stream>>>(cnt, p);
-    TM_LAUNCH_CHECK("cdt_count_kernel");
-    cdt_scan_kernel<<<1, 1024, 0, stream>>>(cnt, woff, pl.T);
-    TM_LAUNCH_CHECK("cdt_scan_kernel");
-    cdt_scatter_kernel<<<rb, 256, 0, stream>>>(woff, cur, order, p);
-    TM_LAUNCH_CHECK("cdt_scatter_kernel");
+    TM_CHECK_CUDA(go(cdt_count_kernel, rb, 256, cnt, p, any));
+    TM_CHECK_CUDA(go(cdt_scan_kernel, 1, 1024, (const int *)cnt, woff, pl.T, any));
+    TM_CHECK_CUDA(go(cdt_scatter_kernel, rb, 256, (const int *)woff, cur, order, p, any));
     unsigned eb = (unsigned)std::min<int64_t>(ceil_div(g.numel, 256), (int64_t)sms * 16);
-    cdt_init_kernel<In><<<eb, 256, 0, stream>>>(in, dt, ft, g.numel, g.numel_item, todo);
-    TM_LAUNCH_CHECK("cdt_init_kernel");
+    TM_CHECK_CUDA(go(cdt_init_kernel<In>, eb, 256, in, dt, ft, g.numel, g.numel_item, todo, any));
     unsigned ib = (unsigned)std::min<int64_t>(g.batch, (int64_t)1 << 20);
-    cdt_pass_kernel<false><<<ib, kCdtThreads, 0, stream>>>(dt, ft, order, woff, p, local, todo);
-    TM_LAUNCH_CHECK("cdt_pass_kernel<forward>");
-    cdt_pass_kernel<true><<<ib, kCdtThreads, 0, stream>>>(dt, ft, order, woff, p, local, todo);
-    TM_LAUNCH_CHECK("cdt_pass_kernel<backward>");
-    cdt_finalize_kernel<<<eb, 256, 0, stream>>>(dt, ft, dist, indices, g.numel, g.numel_item, nd, p,
-                                                metric == TM_CDT_CHAMFER345 ? 3.0f : 1.0f, todo);
+    TM_CHECK_CUDA(go(cdt_pass_kernel<false>, ib, kCdtThreads, dt, ft, (const int *)order, (const int *)woff, p, local,
+                     todo, any));
+    TM_CHECK_CUDA(go(cdt_pass_kernel<true>, ib, kCdtThreads, dt, ft, (const int *)order, (const int *)woff, p, local,
+                     todo, any));
+    TM_CHECK_CUDA(go(cdt_finalize_kernel, eb, 256, (const int32_t *)dt, (const int32_t *)ft, dist, indices, g.numel,
+                     g.numel_item, nd, p, metric == TM_CDT_CHAMFER345 ? 3.0f : 1.0f, todo, any));
     TM_LAUNCH_CHECK("cdt_finalize_kernel");
     return TM_OK;
 }
@@ -394,10 +420,15 @@ extern "C" int tm_cdt(const void *input, int in_dtype, int64_t batch, int ndim, 
     unsigned char *ws = static_cast<unsigned char *>(workspace);
     cudaStream_t s = (cudaStream_t)stream;
     int *todo = nullptr;
+    bool cleared = false;
     if (cdt_shell_shape(g) && cdt_shell_eligible(g, dist, indices)) {
+        // counters first, so that nothing but kernels follows the shell search
+        TM_CHECK_CUDA(clear_cdt_counters(ws, pl, s));
+        cleared = true;
         st = cdt_shell_run(input, in_dtype, g, metric, dist, ws + pl.total, &todo, s);
         if (st != TM_OK) return st;
     }
-    if (in_dtype == TM_F32) return run_cdt<float>((const float *)input, g, metric, dist, indices, ws, pl, todo, s);
-    return run_cdt<uint8_t>((const uint8_t *)input, g, metric, dist, indices, ws, pl, todo, s);
+    if (in_dtype == TM_F32)
+        return run_cdt<float>((const float *)input, g, metric, dist, indices, ws, pl, todo, cleared, s);
+    return run_cdt<uint8_t>((const uint8_t *)input, g, metric, dist, indices, ws, pl, todo, cleared, s);
 }

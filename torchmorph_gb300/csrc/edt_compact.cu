@@ -1665,6 +1665,8 @@ __global__ void __launch_bounds__(kShellThreads) cdt_shell_kernel(const uint32_t
     const int z = rem / ybl, y0 = (rem % ybl) * kShellRows;
     const int nrows = min(kShellRows, L1 - y0);
     const int tid = threadIdx.x;
+    pdl_trigger();  // the raster kernels may be scheduled as this grid's CTAs retire
+    pdl_wait();     // the bitmap and the zeroed flags are complete
     if (tid == 0) s_nfar = 0;
     const uint32_t *ibm = bm + item * (int64_t)L0 * L1 * WW;
     for (int i = tid; i < (2 * kShellR + 1) * kRowsP; i += kShellThreads) {
@@ -1713,7 +1715,10 @@ __global__ void __launch_bounds__(kShellThreads) cdt_shell_kernel(const uint32_t
     __syncthreads();
     const int nfar = s_nfar;
     if (nfar > kCdtFarPerUnit) {  // many voxels beyond the shell: the item takes the raster passes
-        if (tid == 0) atomicExch(&todo[item], 1);
+        if (tid == 0) {
+            atomicExch(&todo[item], 1);
+            atomicExch(&todo[p.batch], 1);  // some item is marked
+        }
         return;
     }
     const int64_t rowbase = item * p.numel_item + ((int64_t)z * L1 + y0) * W;
@@ -1743,8 +1748,10 @@ __global__ void __launch_bounds__(kShellThreads) cdt_shell_kernel(const uint32_t
             const int xv = 32 * wi + __ffs(m) - 1;
             const int best = far_norm_search<MET>(ibm, z, y0 + r, xv, L0, L1, W, lane);
             if (lane != 0) continue;
-            if (best < 0) atomicExch(&todo[item], 1);  // no background: the raster passes give -1
-            else dist[rowbase + (int64_t)r * W + xv] = divisor == 1.f ? (float)best : (float)best / divisor;
+            if (best < 0) {  // no background: the raster passes give -1
+                atomicExch(&todo[item], 1);
+                atomicExch(&todo[p.batch], 1);
+            } else dist[rowbase + (int64_t)r * W + xv] = divisor == 1.f ? (float)best : (float)best / divisor;
         }
     }
 }
@@ -1968,7 +1975,7 @@ bool cdt_shell_eligible(const Geometry &g, const float *dist, const int32_t *ind
 
 size_t cdt_shell_workspace(const Geometry &g) {
     const int ww = (int)((g.shape[2] + 31) / 32);
-    return align256((size_t)g.batch * g.shape[0] * g.shape[1] * ww * 4) + align256((size_t)g.batch * 4);
+    return align256((size_t)g.batch * g.shape[0] * g.shape[1] * ww * 4) + align256((size_t)(g.batch + 1) * 4);
 }
 
 int cdt_shell_run(const void *input, int in_dtype, const Geometry &g, int metric, float *dist, unsigned char *ws,
@@ -1987,7 +1994,7 @@ int cdt_shell_run(const void *input, int in_dtype, const Geometry &g, int metric
     uint32_t *bm = reinterpret_cast<uint32_t *>(ws);
     int *todo = reinterpret_cast<int *>(ws + align256((size_t)nwords * 4));
     if (g.batch > ((int64_t)1 << 30)) return fail(TM_ERR_TOO_LARGE, "batch too large");
-    const int nclear = (int)g.batch;  // per-item flags, zeroed by the bitmap kernel
+    const int nclear = (int)g.batch + 1;  // per-item flags and the "any item marked" flag, zeroed by the bitmap kernel
     const unsigned bblocks = (unsigned)std::min<int64_t>(ceil_div(nwords, 256), (int64_t)sm_count() * 16);
     const bool vrow = (p.L2 % 32) == 0 && ((uintptr_t)input & 15) == 0;
     if (in_dtype == TM_F32) {
@@ -2003,10 +2010,13 @@ int cdt_shell_run(const void *input, int in_dtype, const Geometry &g, int metric
     const int64_t blocks = g.batch * (int64_t)p.L0 * ceil_div(p.L1, kShellRows);
     if (blocks >= ((int64_t)1 << 31)) return fail(TM_ERR_TOO_LARGE, "too many blocks");
     const float div = metric == TM_CDT_CHAMFER345 ? 3.0f : 1.0f;
-    auto go = [&](auto kernel) { kernel<<<(unsigned)blocks, kShellThreads, 0, stream>>>(bm, dist, todo, p, div); };
-    if (metric == TM_CDT_CHESSBOARD) go(cdt_shell_kernel<4, 0>);
-    else if (metric == TM_CDT_TAXICAB) go(cdt_shell_kernel<4, 1>);
-    else go(cdt_shell_kernel<4, 2>);
+    auto go = [&](auto kernel) {
+        return launch_pdl(kernel, dim3((unsigned)blocks), dim3(kShellThreads), 0, stream, (const uint32_t *)bm, dist,
+                          todo, p, div);
+    };
+    if (metric == TM_CDT_CHESSBOARD) TM_CHECK_CUDA(go(cdt_shell_kernel<4, 0>));
+    else if (metric == TM_CDT_TAXICAB) TM_CHECK_CUDA(go(cdt_shell_kernel<4, 1>));
+    else TM_CHECK_CUDA(go(cdt_shell_kernel<4, 2>));
     TM_LAUNCH_CHECK("cdt_shell_kernel");
     *todo_out = todo;
     return TM_OK;
