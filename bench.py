@@ -421,6 +421,30 @@ def ragged_lines(dev, stream, steps, warmup):
         "gpu_launches_per_step": 5}}
 
 
+def pointcloud_profile_case(dev):
+    """Small point-cloud case for profiler captures: 64 problems, n and m log-uniform in
+    [64, 512], the bench's mixture points, eps 0.05, 200 iterations without a stopping
+    test, solved twice (the second solve is the captured one)."""
+    import torch
+
+    from torchmorph_gb300 import PointCloudSinkhorn, pack_clouds
+
+    rng = np.random.default_rng(0)
+    xs, ys = [], []
+    for _ in range(64):
+        n, m = (int(v) for v in np.exp(rng.uniform(np.log(64), np.log(512), 2)))
+        means = rng.uniform(-1, 1, (4, 3))
+        xs.append((means[rng.integers(0, 4, n)] + 0.2 * rng.standard_normal((n, 3))).astype(np.float32))
+        ys.append((means[rng.integers(0, 4, m)] + 0.2 * rng.standard_normal((m, 3))).astype(np.float32))
+    x, nx = pack_clouds([torch.from_numpy(v).to(dev) for v in xs])
+    y, ny = pack_clouds([torch.from_numpy(v).to(dev) for v in ys])
+    solver = PointCloudSinkhorn(epsilon=0.05, max_iter=200, threshold=0.0)
+    for _ in range(2):
+        solver.solve(x, y, nx, ny)
+    torch.cuda.synchronize()
+    return {"case": "pointcloud-profile", "problems": 64, "iterations": 200}
+
+
 def pointcloud_problems(seed=0, count=512):
     """512 OT problems, n and m iid log-uniform integers in [64, 2048], points from a
     4-component Gaussian mixture in R^3 (means U[-1, 1]^3, sigma 0.2), uniform weights."""
@@ -715,8 +739,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--case", choices=["all", "sinkhorn", "ragged", "pointcloud"], default="all",
-                    help="only the shared-cost Sinkhorn or the ragged-batch lines (one JSON object)")
+    ap.add_argument("--case", choices=["all", "sinkhorn", "ragged", "pointcloud", "pointcloud-profile"],
+                    default="all",
+                    help="only the shared-cost Sinkhorn, ragged-batch or point-cloud lines (one JSON object); "
+                         "pointcloud-profile: the small fixed-iteration case used for ncu captures")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.case != "all" and args.impl == "ours":
@@ -728,6 +754,8 @@ def main():
             print(json.dumps(sinkhorn_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline)))
         elif args.case == "pointcloud":
             print(json.dumps(pointcloud_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline)))
+        elif args.case == "pointcloud-profile":
+            print(json.dumps(pointcloud_profile_case(dev)))
         else:
             print(json.dumps(ragged_lines(dev, stream, max(args.steps, 10), args.warmup)))
         return
