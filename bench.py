@@ -283,14 +283,13 @@ def load_traffic(kind):
         return json.load(f).get(kind)
 
 
-def secondary(args, dev, stream, hbm_peak):
-    """Grey/binary dilation, chamfer and Sinkhorn lines (rank 0 only)."""
+def grey_lines(args, dev, stream, hbm_peak):
+    """Flat 3x3 grey dilation (reflect) of float32 U[0, 1): 8 x 256^2 (L2 resident) and
+    8 x 4096^2 (HBM resident, two rotating inputs), 8 algorithmic B/voxel."""
     import torch
 
-    import torchmorph_gb300 as tm
     from torchmorph_gb300 import _C
 
-    out = {}
     g = torch.Generator(device="cpu").manual_seed(0)
     st3 = torch.zeros((3, 3), dtype=torch.float32)
     fp0 = torch.empty(0, dtype=torch.bool)
@@ -312,8 +311,19 @@ def secondary(args, dev, stream, hbm_peak):
                 "achieved_GBps": round(8 * nv / per / 1e9, 1),
                 "frac_of_hbm": round(8 * nv / per / 1e9 / hbm_peak, 4)}
 
-    out["grey_dilation_3x3_8x256x256"] = grey_line((8, 1, 256, 256), 8)
-    out["grey_dilation_3x3_8x4096x4096_hbm"] = grey_line((8, 1, 4096, 4096), 2)
+    return {"grey_dilation_3x3_8x256x256": grey_line((8, 1, 256, 256), 8),
+            "grey_dilation_3x3_8x4096x4096_hbm": grey_line((8, 1, 4096, 4096), 2)}
+
+
+def secondary(args, dev, stream, hbm_peak):
+    """Grey/binary dilation, chamfer and Sinkhorn lines (rank 0 only)."""
+    import torch
+
+    import torchmorph_gb300 as tm
+    from torchmorph_gb300 import _C
+
+    out = grey_lines(args, dev, stream, hbm_peak)
+    g = torch.Generator(device="cpu").manual_seed(1)
 
     xb = (torch.rand((8, 1, 256, 256), generator=g) > 0.5).to(dev)
     box = torch.ones((3, 3), dtype=torch.bool)
@@ -739,7 +749,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--case", choices=["all", "sinkhorn", "ragged", "pointcloud", "pointcloud-profile"],
+    ap.add_argument("--case", choices=["all", "grey", "sinkhorn", "ragged", "pointcloud", "pointcloud-profile"],
                     default="all",
                     help="only the shared-cost Sinkhorn, ragged-batch or point-cloud lines (one JSON object); "
                          "pointcloud-profile: the small fixed-iteration case used for ncu captures")
@@ -750,7 +760,9 @@ def main():
 
         dev = torch.device("cuda", 0)
         stream = torch.cuda.current_stream(dev)
-        if args.case == "sinkhorn":
+        if args.case == "grey":
+            print(json.dumps(grey_lines(args, dev, stream, peaks()[0])))
+        elif args.case == "sinkhorn":
             print(json.dumps(sinkhorn_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline)))
         elif args.case == "pointcloud":
             print(json.dumps(pointcloud_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline)))
