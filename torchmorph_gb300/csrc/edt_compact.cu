@@ -1722,7 +1722,6 @@ __global__ void __launch_bounds__(kShellThreads) cdt_shell_kernel(const uint32_t
         return;
     }
     const int64_t rowbase = item * p.numel_item + ((int64_t)z * L1 + y0) * W;
-    const float inv = 1.0f / divisor;
     const int warp = tid >> 5, lane = tid & 31;
     for (int r = warp; r < nrows; r += kShellThreads / 32) {
         for (int x = 4 * lane; x < W; x += 128) {
@@ -1733,7 +1732,6 @@ __global__ void __launch_bounds__(kShellThreads) cdt_shell_kernel(const uint32_t
             d.y = divisor == 1.f ? (float)((v4 >> 8) & 255u) : (float)((v4 >> 8) & 255u) / divisor;
             d.z = divisor == 1.f ? (float)((v4 >> 16) & 255u) : (float)((v4 >> 16) & 255u) / divisor;
             d.w = divisor == 1.f ? (float)(v4 >> 24) : (float)(v4 >> 24) / divisor;
-            (void)inv;
             *reinterpret_cast<float4 *>(dist + rowbase + (int64_t)r * W + x) = d;
         }
     }
