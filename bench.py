@@ -311,8 +311,24 @@ def grey_lines(args, dev, stream, hbm_peak):
                 "achieved_GBps": round(8 * nv / per / 1e9, 1),
                 "frac_of_hbm": round(8 * nv / per / 1e9 / hbm_peak, 4)}
 
-    return {"grey_dilation_3x3_8x256x256": grey_line((8, 1, 256, 256), 8),
-            "grey_dilation_3x3_8x4096x4096_hbm": grey_line((8, 1, 4096, 4096), 2)}
+    out = {"grey_dilation_3x3_8x256x256": grey_line((8, 1, 256, 256), 8),
+           "grey_dilation_3x3_8x4096x4096_hbm": grey_line((8, 1, 4096, 4096), 2)}
+
+    # morphological gradient 3x3 on the HBM-resident shape: one pass (8 B/voxel) vs the
+    # reference's composition of the two operators and a subtraction (28 B/voxel moved)
+    import torchmorph_gb300 as tm
+
+    xs = [torch.rand((8, 1, 4096, 4096), generator=g).to(dev) for _ in range(2)]
+    steps = max(args.steps, 10)
+    t1 = time_device(lambda x: tm.morphological_gradient(x, size=3), xs, steps, args.warmup, stream) / steps
+    t2 = time_device(lambda x: _C.grey_dilation_cuda(x, st3, fp0, [0, 0], 1, 0.0)
+                     - _C.grey_erosion_cuda(x, st3, fp0, [0, 0], 1, 0.0), xs, steps, args.warmup, stream) / steps
+    nv = xs[0].numel()
+    out["grey_gradient_3x3_8x4096x4096_one_pass"] = {
+        "us_per_call": round(t1 * 1e6, 1), "Gvoxel/s": round(nv / t1 / 1e9, 3),
+        "frac_of_hbm": round(8 * nv / t1 / 1e9 / hbm_peak, 4),
+        "two_operators_us": round(t2 * 1e6, 1), "speedup_vs_two_operators": round(t2 / t1, 2)}
+    return out
 
 
 def secondary(args, dev, stream, hbm_peak):

@@ -122,6 +122,20 @@ int tm_grey_dilation_backward(const float *grad_out, const uint8_t *arg, float *
                               const uint8_t *footprint, const int64_t *sshape,
                               const int64_t *origin, int mode, tm_stream_t stream);
 
+/* One-pass grey composites of 2-D items (same arguments as tm_grey_dilation):
+ * out = dilation - erosion (morphological_gradient,
+ * torchmorph/morphology/grey.py:200-221) and out = (dilation + erosion) - 2 in
+ * (morphological_laplace, grey.py:268-289), each value rounded as the
+ * reference's elementwise float32 ops round it.  Elements of up to 64 active
+ * taps whose offsets span at most 31 per axis; anything else returns
+ * TM_ERR_UNSUPPORTED (the caller then composes the two operators). */
+int tm_grey_gradient(const float *in, float *out, int64_t batch, int ndim, const int64_t *shape,
+                     const float *structure, const uint8_t *footprint, const int64_t *sshape,
+                     const int64_t *origin, int mode, float cval, tm_stream_t stream);
+int tm_grey_laplace(const float *in, float *out, int64_t batch, int ndim, const int64_t *shape,
+                    const float *structure, const uint8_t *footprint, const int64_t *sshape,
+                    const int64_t *origin, int mode, float cval, tm_stream_t stream);
+
 /* ---------------------------------------------------------------- binary --
  * Replaces binary_erosion_cuda / binary_dilation_cuda
  * (torchmorph/csrc/torchmorph.cpp:21-33, torchmorph/csrc/binary_kernel.cu:252-272).

@@ -104,6 +104,25 @@ def test_propagation_fill_holes_hit_or_miss(cuda):
     np.testing.assert_array_equal(got.cpu().numpy(), per_item(hit, ndi.binary_hit_or_miss))
 
 
+def test_until_stable_needs_many_iterations(cuda):
+    """Iterate-until-stable runs its iterations in chunks with device-side change flags;
+    a seed propagating through a 90 x 90 maze-like mask takes a few hundred iterations,
+    i.e. several chunks.  Results equal scipy's fixed points."""
+    r = rng(5)
+    mask = r.random((2, 1, 90, 90)) < 0.75
+    mask[:, :, ::6, :] = True  # corridors so that long paths exist
+    seed = np.zeros_like(mask)
+    seed[:, :, 0, 0] = True
+    got = tm.binary_propagation(_t(seed), mask=_t(mask))
+    exp = np.stack([ndi.binary_propagation(seed[b, 0], mask=mask[b, 0]) for b in range(2)])[:, None]
+    np.testing.assert_array_equal(got.cpu().numpy(), exp)
+    holes = r.random((2, 1, 90, 90)) < 0.55
+    got = tm.binary_fill_holes(_t(holes))
+    np.testing.assert_array_equal(got.cpu().numpy(), per_item(holes, ndi.binary_fill_holes))
+    got = tm.binary_erosion(_t(holes), iterations=-1)
+    np.testing.assert_array_equal(got.cpu().numpy(), per_item(holes, ndi.binary_erosion, iterations=-1))
+
+
 @pytest.mark.parametrize("nd", [1, 8])
 def test_dimension_range(cuda, nd):
     x = np.zeros((1, 1) + (2,) * nd, bool)

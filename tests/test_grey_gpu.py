@@ -210,3 +210,41 @@ def test_binary_box_tma_tiles_vs_oracle(cuda, dilation):
     exp = oracle.binary(x, st, dilation=dilation)
     np.testing.assert_array_equal(got.cpu().numpy(), exp)
     assert _device_error() == 0
+
+
+ELEMENTS = {
+    "box3": dict(size=3),
+    "box3x5": dict(size=(3, 5)),
+    "even4_origin": dict(size=(4, 4), origin=(-1, 1)),
+    "nonflat": dict(structure=torch.tensor(rng(31).random((3, 3)) * 0.2, dtype=torch.float32)),
+    "footprint": dict(footprint=torch.tensor((rng(32).random((5, 5)) < 0.6) | np.eye(5, dtype=bool))),
+    "wide31": dict(size=(1, 31)),
+    "too_many_taps": dict(size=(9, 9)),  # 81 taps: composed from the two operators
+}
+
+
+@pytest.mark.parametrize("kind", ["gradient", "laplace"])
+@pytest.mark.parametrize("mode", ["reflect", "constant", "nearest", "mirror", "wrap"])
+@pytest.mark.parametrize("elem", list(ELEMENTS))
+def test_one_pass_composites_equal_two_operators(cuda, kind, mode, elem):
+    """2-D gradient / laplace in one pass (elements of up to 64 taps spanning up to 31)
+    equal the reference's formulas on the two operators bit for bit: d - e and
+    (d + e) - 2 x in float32; flat gradients also equal scipy."""
+    kw = dict(ELEMENTS[elem], mode=mode, cval=0.3)
+    x = rng(hash((kind, mode, elem)) % 2**31).random((2, 2, 150, 300)).astype(np.float32)
+    xt = torch.from_numpy(x).cuda()
+    got = getattr(tm, f"morphological_{kind}")(xt, **kw)
+    d, e = tm.grey_dilation(xt, **kw), tm.grey_erosion(xt, **kw)
+    exp = d - e if kind == "gradient" else d + e - 2 * xt
+    assert torch.equal(got, exp)
+    if kind == "gradient" and "size" in ELEMENTS[elem]:
+        sk = {k: v for k, v in kw.items()}
+        np.testing.assert_array_equal(got.cpu().numpy(), per_item(x, ndi.morphological_gradient, **sk))
+
+
+def test_one_pass_composites_leave_3d_to_the_operators(cuda):
+    x = torch.from_numpy(rng(33).random((1, 1, 20, 30, 40)).astype(np.float32)).cuda()
+    for kind in ("gradient", "laplace"):
+        got = getattr(tm, f"morphological_{kind}")(x, size=3)
+        d, e = tm.grey_dilation(x, size=3), tm.grey_erosion(x, size=3)
+        assert torch.equal(got, d - e if kind == "gradient" else d + e - 2 * x)

@@ -83,6 +83,35 @@ def grey_dilation_cuda(input, structure, footprint, origin, mode, cval):
     return _grey("tm_grey_dilation", input, structure, footprint, origin, mode, cval)
 
 
+_TM_ERR_UNSUPPORTED = 2
+
+
+def grey_composite(kind, input, structure, footprint, origin, mode, cval):
+    """One-pass morphological gradient ("gradient") or laplace ("laplace") of a 2-D batch
+    (tm_grey_gradient / tm_grey_laplace); None when the element is outside the one-pass
+    kernel's limits, so that the caller composes the two operators instead."""
+    _require(input.is_cuda and input.is_contiguous() and input.dtype == torch.float32,
+             "input must be a contiguous float32 CUDA tensor")
+    nd = structure.dim()
+    _require(len(origin) == nd and input.dim() == nd + 2, "structure/origin/input dimensions disagree")
+    if nd != 2:
+        return None
+    use_fp = footprint.numel() != 0
+    batch, shape = _batch_shape(input)
+    out = torch.empty_like(input)
+    name = "tm_grey_gradient" if kind == "gradient" else "tm_grey_laplace"
+    lib = _lib.load()
+    with torch.cuda.device(input.device):
+        st = getattr(lib, name)(
+            _lib.ptr(input), _lib.ptr(out), batch, nd, _lib.i64_array(shape), _host_f32(structure),
+            _host_u8(footprint) if use_fp else None, _lib.i64_array(structure.shape),
+            _lib.i64_array(origin), int(mode), float(cval), _lib.stream_of(input.device))
+    if st == _TM_ERR_UNSUPPORTED:
+        return None
+    _lib.check(st, name)
+    return out
+
+
 def _grey_arg(fn_name, input, structure, footprint, origin, mode, cval):
     """(output, argument) of the forward with the first extremum tap recorded per output."""
     _require(input.is_cuda and input.is_contiguous() and input.dtype == torch.float32,

@@ -70,6 +70,10 @@ SIGNATURES = {
                                      I64P, c_int, c_float, c_void]),
     "tm_grey_erosion_backward": (c_int, [c_void, c_void, c_void, c_i64, c_int, I64P, U8P, I64P, I64P,
                                          c_int, c_void]),
+    "tm_grey_gradient": (c_int, [c_void, c_void, c_i64, c_int, I64P, F32P, U8P, I64P, I64P, c_int, c_float,
+                                 c_void]),
+    "tm_grey_laplace": (c_int, [c_void, c_void, c_i64, c_int, I64P, F32P, U8P, I64P, I64P, c_int, c_float,
+                                c_void]),
     "tm_grey_dilation_backward": (c_int, [c_void, c_void, c_void, c_i64, c_int, I64P, U8P, I64P, I64P,
                                           c_int, c_void]),
     "tm_pointcloud_sinkhorn_workspace_size": (c_size, [c_i64, I64P, I64P, c_i64]),

@@ -515,6 +515,90 @@ bool make_taps2d(const GradParams &p, const GradTaps &taps, bool backward, Taps2
     return true;
 }
 
+// ------------------------------------------ fused 2-D composites, one pass
+// morphological_gradient = dilation - erosion and morphological_laplace =
+// (dilation + erosion) - 2 x of 2-D items (torchmorph/morphology/grey.py:
+// 200-221, 268-289) in one read of the input and one write: the union of
+// the dilation's and the erosion's tap regions is staged once; each tap list
+// runs in raster order with a strict comparison (the first extremum wins,
+// as in the forward-with-argument kernel, whose values equal the plain
+// operators' bit for bit), and the combination is rounded like the
+// reference's elementwise ops (no contraction).
+struct Taps2DPair {
+    int nd, ne, min_dy, min_dx, ext_y, ext_x, center;
+    int soff_d[kT2MaxTaps], soff_e[kT2MaxTaps];
+    float val_d[kT2MaxTaps], val_e[kT2MaxTaps];
+};
+
+template <int OP, int P>  // OP 0: gradient, 1: laplace
+__global__ void __launch_bounds__(kT2Threads, 3) grey_composite2d_kernel(const float *__restrict__ in,
+                                                                         float *__restrict__ out, GradParams p,
+                                                                         const __grid_constant__ Taps2DPair tp) {
+    extern __shared__ __align__(16) float stile[];
+    const int H = p.shape[0], W = p.shape[1];
+    const int RH = kT2H + tp.ext_y, RW = kT2W + tp.ext_x;
+    const int x0 = blockIdx.x * kT2W, y0 = blockIdx.y * kT2H;
+    const int gy0 = y0 + tp.min_dy, gx0 = x0 + tp.min_dx;
+    const bool inner = gy0 >= 0 && gx0 >= 0 && gy0 + RH <= H && gx0 + RW <= W;
+    const int c = threadIdx.x % kT2W, r0 = (threadIdx.x / kT2W) * kT2Rows;
+    const int x = x0 + c;
+    for (int64_t item = blockIdx.z; item < p.batch; item += gridDim.z) {
+        const float *src = in + item * p.numel_item;
+        const int mode = p.mode;
+        const float cval = p.cval;
+        auto put = [&](int r, int cc, float v) { stile[r * P + cc] = v; };
+        if (inner)
+            stage_region<2>(RH, RW, [&](int r, int cc) { return src[(int64_t)(gy0 + r) * W + gx0 + cc]; }, put);
+        else
+            stage_region<1>(
+                RH, RW,
+                [&](int r, int cc) {
+                    const int my = map_coord(gy0 + r, H, mode), mx = map_coord(gx0 + cc, W, mode);
+                    return (my < 0 || mx < 0) ? cval : src[(int64_t)my * W + mx];
+                },
+                put);
+        __syncthreads();
+        float dmax[kT2Rows], emin[kT2Rows];
+#pragma unroll
+        for (int i = 0; i < kT2Rows; i++) {
+            dmax[i] = -INFINITY;
+            emin[i] = INFINITY;
+        }
+        const float *base = stile + r0 * P + c;
+        for (int t = 0; t < tp.nd; t++) {
+            const float *q = base + tp.soff_d[t];
+            const float sv = tp.val_d[t];
+#pragma unroll
+            for (int i = 0; i < kT2Rows; i++) {
+                const float v = q[i * P] + sv;
+                if (v > dmax[i]) dmax[i] = v;
+            }
+        }
+        for (int t = 0; t < tp.ne; t++) {
+            const float *q = base + tp.soff_e[t];
+            const float sv = tp.val_e[t];
+#pragma unroll
+            for (int i = 0; i < kT2Rows; i++) {
+                const float v = q[i * P] - sv;
+                if (v < emin[i]) emin[i] = v;
+            }
+        }
+        if (x < W) {
+#pragma unroll
+            for (int i = 0; i < kT2Rows; i++) {
+                const int y = y0 + r0 + i;
+                if (y < H) {
+                    float r;
+                    if (OP == 0) r = __fsub_rn(dmax[i], emin[i]);
+                    else r = __fsub_rn(__fadd_rn(dmax[i], emin[i]), __fmul_rn(2.f, base[tp.center + i * P]));
+                    out[item * p.numel_item + (int64_t)y * W + x] = r;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 dim3 grid2d(const GradParams &p) {
     return dim3((unsigned)ceil_div(p.shape[1], kT2W), (unsigned)ceil_div(p.shape[0], kT2H),
                 (unsigned)std::min<int64_t>(p.batch, 65535));
@@ -633,6 +717,59 @@ int run_grad(bool dilation, const float *gout, const uint8_t *arg, float *gin, i
     return TM_OK;
 }
 
+int run_composite(int op, const float *in, float *out, int64_t batch, int ndim, const int64_t *shape,
+                  const float *structure, const uint8_t *footprint, const int64_t *sshape, const int64_t *origin,
+                  int mode, float cval, cudaStream_t s) {
+    if (!in || !out) return fail(TM_ERR_INVALID_ARGUMENT, "NULL input or output");
+    if (in == out) return fail(TM_ERR_INVALID_ARGUMENT, "output must not alias the input");
+    if (ndim != 2) return fail(TM_ERR_UNSUPPORTED, "the one-pass composites take 2-D items");
+    GradParams pd, pe;
+    GradTaps td, te;
+    int st = build_grad_taps(true, batch, ndim, shape, structure, footprint, sshape, origin, mode, cval, &pd, &td);
+    if (st != TM_OK) return st;
+    st = build_grad_taps(false, batch, ndim, shape, structure, footprint, sshape, origin, mode, cval, &pe, &te);
+    if (st != TM_OK) return st;
+    if (pd.ntaps > kT2MaxTaps) return fail(TM_ERR_UNSUPPORTED, "the one-pass composites take up to %d taps", kT2MaxTaps);
+    int mny = 0, mxy = 0, mnx = 0, mxx = 0;  // union of both tap regions (and the voxel itself)
+    for (int t = 0; t < pd.ntaps; t++)
+        for (const GradTaps *tt : {&td, &te}) {
+            mny = std::min(mny, (int)tt->off[t][0]);
+            mxy = std::max(mxy, (int)tt->off[t][0]);
+            mnx = std::min(mnx, (int)tt->off[t][1]);
+            mxx = std::max(mxx, (int)tt->off[t][1]);
+        }
+    if (mxy - mny > kT2MaxExt || mxx - mnx > kT2MaxExt)
+        return fail(TM_ERR_UNSUPPORTED, "the one-pass composites take tap offsets spanning up to %d", kT2MaxExt + 1);
+    Taps2DPair *tp = new Taps2DPair;
+    std::memset(tp, 0, sizeof(*tp));
+    tp->nd = pd.ntaps;
+    tp->ne = pe.ntaps;
+    tp->min_dy = mny;
+    tp->min_dx = mnx;
+    tp->ext_y = mxy - mny;
+    tp->ext_x = mxx - mnx;
+    const int P = pitch2d(tp->ext_x);
+    tp->center = (0 - mny) * P + (0 - mnx);
+    for (int t = 0; t < pd.ntaps; t++) {
+        tp->soff_d[t] = (td.off[t][0] - mny) * P + (td.off[t][1] - mnx);
+        tp->val_d[t] = td.val[t];
+        tp->soff_e[t] = (te.off[t][0] - mny) * P + (te.off[t][1] - mnx);
+        tp->val_e[t] = te.val[t];
+    }
+    const size_t smem = (size_t)(kT2H + tp->ext_y) * P * sizeof(float);
+    auto kern = op == 0 ? (P == 136 ? grey_composite2d_kernel<0, 136> : grey_composite2d_kernel<0, 160>)
+                        : (P == 136 ? grey_composite2d_kernel<1, 136> : grey_composite2d_kernel<1, 160>);
+    cudaError_t e = cudaSuccess;
+    if (smem > 48 * 1024) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) {
+        kern<<<grid2d(pd), kT2Threads, smem, s>>>(in, out, pd, *tp);
+        e = cudaGetLastError();
+    }
+    delete tp;
+    TM_CHECK_CUDA(e);
+    return TM_OK;
+}
+
 }  // namespace
 }  // namespace tmc
 
@@ -665,4 +802,18 @@ extern "C" int tm_grey_dilation_backward(const float *grad_out, const uint8_t *a
                                          tm_stream_t stream) {
     return tmc::run_grad(true, grad_out, arg, grad_in, batch, ndim, shape, footprint, sshape, origin, mode,
                          (cudaStream_t)stream);
+}
+
+extern "C" int tm_grey_gradient(const float *in, float *out, int64_t batch, int ndim, const int64_t *shape,
+                                const float *structure, const uint8_t *footprint, const int64_t *sshape,
+                                const int64_t *origin, int mode, float cval, tm_stream_t stream) {
+    return tmc::run_composite(0, in, out, batch, ndim, shape, structure, footprint, sshape, origin, mode, cval,
+                              (cudaStream_t)stream);
+}
+
+extern "C" int tm_grey_laplace(const float *in, float *out, int64_t batch, int ndim, const int64_t *shape,
+                               const float *structure, const uint8_t *footprint, const int64_t *sshape,
+                               const int64_t *origin, int mode, float cval, tm_stream_t stream) {
+    return tmc::run_composite(1, in, out, batch, ndim, shape, structure, footprint, sshape, origin, mode, cval,
+                              (cudaStream_t)stream);
 }

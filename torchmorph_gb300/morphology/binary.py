@@ -49,14 +49,24 @@ def _binary_morphology(input, structure, iterations, mask, output, border_value,
         return _binary_morphology_cuda_step(v, structure, border_value, origin, mode=mode)
 
     if until_stable:
-        prev = None
+        # Iterate to the fixed point without a host sync per iteration: run
+        # chunks of 1, 2, 4, ... 32 iterations, each recording on the device
+        # whether it changed anything, and read the flags once per chunk.
+        # Once an iteration changes nothing every later one returns the same
+        # volume, so a chunk with an unchanged iteration ends at the fixed
+        # point (at most 31 iterations beyond it are computed).
+        chunk = 1
         while True:
-            x = step(x)
-            if mask_b is not None:
-                x = torch.where(mask_b, x, original)
-            if prev is not None and torch.equal(x, prev):
+            changed = torch.empty(chunk, dtype=torch.bool, device=x.device)
+            for j in range(chunk):
+                nxt = step(x)
+                if mask_b is not None:
+                    nxt = torch.where(mask_b, nxt, original)
+                changed[j] = torch.ne(nxt, x).any()
+                x = nxt
+            if not bool(changed.all()):
                 break
-            prev = x
+            chunk = min(2 * chunk, 32)
     else:
         for _ in range(iterations):
             x = step(x)

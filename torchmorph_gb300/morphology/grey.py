@@ -166,11 +166,21 @@ def _finish(result, output):
     return result
 
 
+def _one_pass(kind, input, size, footprint, structure, mode, cval, origin):
+    """The one-pass 2-D composite kernel's result, or None outside its limits."""
+    struct, fp, o, m = _prepare(input, size, footprint, structure, mode, origin)
+    return _C.grey_composite(kind, input.detach().contiguous().float(), struct, fp, o, m, cval)
+
+
 def morphological_gradient(input, size=None, footprint=None, structure=None, output=None,
                            mode="reflect", cval=0.0, origin=0, *, differentiable=False) -> Tensor:
-    """Dilation minus erosion."""
+    """Dilation minus erosion (2-D items with elements of up to 64 taps: one pass)."""
     validate_bcs_input(input)
     validate_output(input, output)
+    if not (differentiable and input.requires_grad and torch.is_grad_enabled()):
+        res = _one_pass("gradient", input, size, footprint, structure, mode, cval, origin)
+        if res is not None:
+            return _finish(res, output)
     kw = _element_kwargs(size, footprint, structure, mode, cval, origin)
     return _finish(grey_dilation(input, differentiable=differentiable, **kw)
                    - grey_erosion(input, differentiable=differentiable, **kw), output)
@@ -196,9 +206,13 @@ def black_tophat(input, size=None, footprint=None, structure=None, output=None, 
 
 def morphological_laplace(input, size=None, footprint=None, structure=None, output=None,
                           mode="reflect", cval=0.0, origin=0) -> Tensor:
-    """Dilation plus erosion minus twice the input."""
+    """Dilation plus erosion minus twice the input (2-D items with elements of up to 64 taps:
+    one pass)."""
     validate_bcs_input(input)
     validate_output(input, output)
+    res = _one_pass("laplace", input, size, footprint, structure, mode, cval, origin)
+    if res is not None:
+        return _finish(res, output)
     kw = _element_kwargs(size, footprint, structure, mode, cval, origin)
     res = grey_dilation(input, **kw) + grey_erosion(input, **kw) - 2 * input.detach().float()
     return _finish(res, output)
