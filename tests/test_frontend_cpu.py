@@ -84,6 +84,46 @@ def test_sinkhorn_cpu_path_matches_oracle():
         np.testing.assert_allclose(solver(src, tgt).numpy(), dist, rtol=1e-10)
 
 
+def test_sinkhorn_one_solve_per_problem(monkeypatch):
+    """forward, plan, potentials and solve on the same (unmodified) inputs run one solve;
+    changed inputs, in-place edits or parameters solve again; results equal a fresh
+    solver's, gradients still reach the inputs."""
+    import torchmorph_gb300.optimal_transport as ot
+
+    calls = []
+    real = ot._scaling_iterations
+
+    def counting(*args, **kw):
+        calls.append(1)
+        return real(*args, **kw)
+
+    monkeypatch.setattr(ot, "_scaling_iterations", counting)
+    g = torch.Generator().manual_seed(43)
+    src = (torch.rand((3, 6), generator=g, dtype=torch.float64) + 0.1).requires_grad_(True)
+    tgt = torch.rand((3, 6), generator=g, dtype=torch.float64) + 0.1
+    solver = tm.SinkhornSolver(epsilon=1.5, max_iter=200)
+    dist = solver(src, tgt)
+    plan = solver.plan(src, tgt)
+    f, h = solver.potentials(src, tgt)
+    res = solver.solve(src, tgt)
+    assert len(calls) == 1
+    fresh = tm.SinkhornSolver(epsilon=1.5, max_iter=200)
+    assert torch.equal(plan, fresh.plan(src, tgt))
+    assert torch.equal(f, fresh.potentials(src, tgt)[0]) and torch.equal(dist.detach(), res["distance"])
+    dist.sum().backward()
+    assert src.grad is not None and torch.isfinite(src.grad).all()
+    n = len(calls)
+    with torch.no_grad():
+        tgt.mul_(1.0)  # an in-place edit bumps the version counter
+    solver.plan(src, tgt)
+    assert len(calls) == n + 1
+    solver.plan(src, tgt.clone())  # another tensor object
+    assert len(calls) == n + 2
+    solver.epsilon = 2.0
+    solver.plan(src, tgt)
+    assert len(calls) == n + 3
+
+
 def test_sinkhorn_argument_errors():
     with pytest.raises(ValueError, match="epsilon"):
         tm.SinkhornSolver(epsilon=0)

@@ -19,6 +19,7 @@ reference does.
 
 from __future__ import annotations
 
+import weakref
 from typing import Optional
 
 import torch
@@ -138,17 +139,14 @@ def _log_iterations(a, b, cost_matrix, epsilon, max_iter, threshold):
 
 
 class _SinkhornDistance(torch.autograd.Function):
-    """<P, C> with envelope-theorem gradients (centred dual potentials) for a and b."""
+    """<P, C> from a solve's potentials, with envelope-theorem gradients (centred dual
+    potentials) for a and b."""
 
     @staticmethod
-    def forward(ctx, a, b, cost_matrix, epsilon, max_iter, threshold, log_space, tensor_cores):
-        if _use_tensor_cores(a, cost_matrix, tensor_cores):
-            log_u, log_v, cost, _, _ = _tensor_core_solve(a, b, cost_matrix, epsilon, max_iter,
-                                                          threshold)
+    def forward(ctx, a, b, cost_matrix, epsilon, log_u, log_v, cost):
+        if cost is not None:  # the tensor-core solve's <P, C>
             distance = cost.to(a.dtype)
         else:
-            iterate = _log_iterations if log_space else _scaling_iterations
-            log_u, log_v = iterate(a, b, cost_matrix, epsilon, max_iter, threshold)
             plan = torch.exp(log_u.unsqueeze(-1) - cost_matrix / epsilon + log_v.unsqueeze(-2))
             distance = (plan * cost_matrix).sum(dim=(-2, -1))
         f = epsilon * log_u
@@ -160,7 +158,7 @@ class _SinkhornDistance(torch.autograd.Function):
     def backward(ctx, grad_output):
         f, g = ctx.saved_tensors
         grad = grad_output.unsqueeze(-1)
-        return grad * f, grad * g, None, None, None, None, None, None
+        return grad * f, grad * g, None, None, None, None, None
 
 
 class SinkhornSolver(nn.Module):
@@ -181,6 +179,8 @@ class SinkhornSolver(nn.Module):
         self.p = p
         self.log_space = log_space
         self.tensor_cores = tensor_cores
+        # the last solve (see _solve), reused by forward / plan / potentials / solve
+        self._last = None
 
     def extra_repr(self):
         return (
@@ -208,11 +208,37 @@ class SinkhornSolver(nn.Module):
         target = target / target.sum(dim=-1, keepdim=True).clamp(min=1e-12)
         return source, target, cost_matrix
 
+    def _solve(self, inputs, a, b, cost_matrix):
+        """(log_u, log_v, tensor-core cost or None, row error or None, iterations) of the
+        preprocessed problem (a, b, cost_matrix).  The last solve is kept and returned
+        again while the caller's tensors `inputs` (source, target, cost or None) are the
+        same objects, unmodified (version counters), and the solver's parameters are
+        unchanged: forward, plan, potentials and solve on one problem run one solve.
+        The solver holds weak references only, so it keeps no input alive."""
+        params = (self.epsilon, self.max_iter, self.threshold, self.log_space, self.tensor_cores, self.p)
+        versions = tuple(None if t is None else t._version for t in inputs)
+        last = self._last
+        if last is not None and last[0] == params and last[2] == versions and all(
+                (r is None and t is None) or (r is not None and r() is t) for r, t in zip(last[1], inputs)):
+            return last[3]
+        with torch.no_grad():
+            if _use_tensor_cores(a, cost_matrix, self.tensor_cores):
+                result = _tensor_core_solve(a, b, cost_matrix, self.epsilon, self.max_iter, self.threshold)
+            else:
+                iterate = _log_iterations if self.log_space else _scaling_iterations
+                log_u, log_v = iterate(a.detach(), b.detach(), cost_matrix, self.epsilon, self.max_iter,
+                                       self.threshold)
+                result = (log_u, log_v, None, None, self.max_iter)
+        refs = tuple(None if t is None else weakref.ref(t) for t in inputs)
+        self._last = (params, refs, versions, result)
+        return result
+
     def forward(self, source: Tensor, target: Tensor, cost_matrix: Optional[Tensor] = None):
         """(n,) transport distances <P, C> between the rows of source and target."""
-        source, target, cost_matrix = self.data_preprocess(source, target, cost_matrix)
-        return _SinkhornDistance.apply(source, target, cost_matrix, self.epsilon, self.max_iter,
-                                       self.threshold, self.log_space, self.tensor_cores)
+        inputs = (source, target, cost_matrix)
+        a, b, c = self.data_preprocess(source, target, cost_matrix)
+        log_u, log_v, cost, _, _ = self._solve(inputs, a, b, c)
+        return _SinkhornDistance.apply(a, b, c, self.epsilon, log_u, log_v, cost)
 
     @torch.no_grad()
     def solve(self, source: Tensor, target: Tensor, cost_matrix: Optional[Tensor] = None):
@@ -220,18 +246,16 @@ class SinkhornSolver(nn.Module):
         potentials ``f``, ``g`` (n, d), ``marginal_error`` (n,) -- the L1 distance
         between the plan's row sums and the source histogram, in float64 -- and
         ``iterations``."""
+        inputs = (source, target, cost_matrix)
         source, target, cost_matrix = self.data_preprocess(source, target, cost_matrix)
-        if _use_tensor_cores(source, cost_matrix, self.tensor_cores):
-            log_u, log_v, cost, row_err, its = _tensor_core_solve(
-                source, target, cost_matrix, self.epsilon, self.max_iter, self.threshold)
+        log_u, log_v, cost, row_err, its = self._solve(inputs, source, target, cost_matrix)
+        if cost is not None:
             distance = cost.to(source.dtype)
         else:
-            log_u, log_v = self._iterate(source, target, cost_matrix)
             plan = torch.exp(log_u.unsqueeze(-1) - cost_matrix / self.epsilon
                              + log_v.unsqueeze(-2))
             distance = (plan * cost_matrix).sum(dim=(-2, -1))
             row_err = (plan.double().sum(-1) - source.double()).abs().sum(-1)
-            its = self.max_iter
         f = self.epsilon * log_u
         g = self.epsilon * log_v
         return {"distance": distance, "f": f - f.mean(dim=-1, keepdim=True),
@@ -240,24 +264,21 @@ class SinkhornSolver(nn.Module):
 
     @torch.no_grad()
     def plan(self, source: Tensor, target: Tensor, cost_matrix: Optional[Tensor] = None):
-        """(n, d, d) transport plans."""
+        """(n, d, d) transport plans, built in place in one (n, d, d) buffer with the
+        reference's operations and rounding (log_u - C / eps, + log_v, exp)."""
+        inputs = (source, target, cost_matrix)
         source, target, cost_matrix = self.data_preprocess(source, target, cost_matrix)
-        log_u, log_v = self._iterate(source, target, cost_matrix)
-        return torch.exp(log_u.unsqueeze(-1) - cost_matrix / self.epsilon + log_v.unsqueeze(-2))
+        log_u, log_v, _, _, _ = self._solve(inputs, source, target, cost_matrix)
+        plan = torch.sub(log_u.unsqueeze(-1), (cost_matrix / self.epsilon).unsqueeze(0))
+        plan.add_(log_v.unsqueeze(-2))
+        return plan.exp_()
 
     @torch.no_grad()
     def potentials(self, source: Tensor, target: Tensor, cost_matrix: Optional[Tensor] = None):
         """Centred dual potentials (f, g), each (n, d)."""
+        inputs = (source, target, cost_matrix)
         source, target, cost_matrix = self.data_preprocess(source, target, cost_matrix)
-        log_u, log_v = self._iterate(source, target, cost_matrix)
+        log_u, log_v, _, _, _ = self._solve(inputs, source, target, cost_matrix)
         f = self.epsilon * log_u
         g = self.epsilon * log_v
         return f - f.mean(dim=-1, keepdim=True), g - g.mean(dim=-1, keepdim=True)
-
-    def _iterate(self, a, b, cost_matrix):
-        if _use_tensor_cores(a, cost_matrix, self.tensor_cores):
-            log_u, log_v, _, _, _ = _tensor_core_solve(a, b, cost_matrix, self.epsilon,
-                                                       self.max_iter, self.threshold)
-            return log_u, log_v
-        iterate = _log_iterations if self.log_space else _scaling_iterations
-        return iterate(a, b, cost_matrix, self.epsilon, self.max_iter, self.threshold)
