@@ -644,7 +644,9 @@ def sinkhorn_lines(dev, stream, cpu_baseline=True):
     n, d = a.shape
     out = {}
     for eps in (0.05, 0.01):
-        solver = SinkhornSolver(epsilon=eps, max_iter=20000, threshold=1e-6, tensor_cores=True)
+        # reuse_solves=False: the timed call solves again instead of returning the warm-up's result
+        solver = SinkhornSolver(epsilon=eps, max_iter=20000, threshold=1e-6, tensor_cores=True,
+                                reuse_solves=False)
         solver.solve(a, b, cost)  # warm-up
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()

@@ -122,6 +122,10 @@ def test_sinkhorn_one_solve_per_problem(monkeypatch):
     solver.epsilon = 2.0
     solver.plan(src, tgt)
     assert len(calls) == n + 3
+    every = tm.SinkhornSolver(epsilon=1.5, max_iter=200, reuse_solves=False)
+    every.plan(src, tgt)
+    every.plan(src, tgt)
+    assert len(calls) == n + 5
 
 
 def test_sinkhorn_argument_errors():

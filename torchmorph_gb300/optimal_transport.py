@@ -165,7 +165,7 @@ class SinkhornSolver(nn.Module):
     """Entropy-regularised balanced OT between (n, d) histogram batches sharing a (d, d) cost."""
 
     def __init__(self, epsilon=1.0, max_iter=100, threshold=0.0, p=2, log_space=False,
-                 tensor_cores=None):
+                 tensor_cores=None, reuse_solves=True):
         super().__init__()
         if epsilon <= 0:
             raise ValueError("epsilon must be positive.")
@@ -179,7 +179,9 @@ class SinkhornSolver(nn.Module):
         self.p = p
         self.log_space = log_space
         self.tensor_cores = tensor_cores
-        # the last solve (see _solve), reused by forward / plan / potentials / solve
+        # the last solve (see _solve), reused by forward / plan / potentials / solve on the
+        # same problem unless reuse_solves is False (then every call solves)
+        self.reuse_solves = reuse_solves
         self._last = None
 
     def extra_repr(self):
@@ -214,11 +216,13 @@ class SinkhornSolver(nn.Module):
         again while the caller's tensors `inputs` (source, target, cost or None) are the
         same objects, unmodified (version counters), and the solver's parameters are
         unchanged: forward, plan, potentials and solve on one problem run one solve.
-        The solver holds weak references only, so it keeps no input alive."""
+        The solver holds weak references only, so it keeps no input alive.  Edits made
+        through ``.data`` do not move the version counter: a caller that mutates its
+        inputs that way constructs the solver with ``reuse_solves=False``."""
         params = (self.epsilon, self.max_iter, self.threshold, self.log_space, self.tensor_cores, self.p)
         versions = tuple(None if t is None else t._version for t in inputs)
         last = self._last
-        if last is not None and last[0] == params and last[2] == versions and all(
+        if self.reuse_solves and last is not None and last[0] == params and last[2] == versions and all(
                 (r is None and t is None) or (r is not None and r() is t) for r, t in zip(last[1], inputs)):
             return last[3]
         with torch.no_grad():
