@@ -530,7 +530,7 @@ struct Taps2DPair {
     float val_d[kT2MaxTaps], val_e[kT2MaxTaps];
 };
 
-template <int OP, int P>  // OP 0: gradient, 1: laplace
+template <int OP, int P, bool SYM>  // OP 0: gradient, 1: laplace; SYM: flat, same offsets for both
 __global__ void __launch_bounds__(kT2Threads, 3) grey_composite2d_kernel(const float *__restrict__ in,
                                                                          float *__restrict__ out, GradParams p,
                                                                          const __grid_constant__ Taps2DPair tp) {
@@ -565,22 +565,42 @@ __global__ void __launch_bounds__(kT2Threads, 3) grey_composite2d_kernel(const f
             emin[i] = INFINITY;
         }
         const float *base = stile + r0 * P + c;
-        for (int t = 0; t < tp.nd; t++) {
-            const float *q = base + tp.soff_d[t];
-            const float sv = tp.val_d[t];
+        if (SYM) {
+            // flat element whose dilation and erosion read the same offsets: one
+            // load per offset feeds both extrema (their values do not depend on the
+            // order); the flat taps' + 0 / - 0 is applied once at the end
+            for (int t = 0; t < tp.nd; t++) {
+                const float *q = base + tp.soff_d[t];
 #pragma unroll
-            for (int i = 0; i < kT2Rows; i++) {
-                const float v = q[i * P] + sv;
-                if (v > dmax[i]) dmax[i] = v;
+                for (int i = 0; i < kT2Rows; i++) {
+                    const float v = q[i * P];
+                    dmax[i] = fmaxf(dmax[i], v);
+                    emin[i] = fminf(emin[i], v);
+                }
             }
-        }
-        for (int t = 0; t < tp.ne; t++) {
-            const float *q = base + tp.soff_e[t];
-            const float sv = tp.val_e[t];
 #pragma unroll
             for (int i = 0; i < kT2Rows; i++) {
-                const float v = q[i * P] - sv;
-                if (v < emin[i]) emin[i] = v;
+                dmax[i] = __fadd_rn(dmax[i], 0.f);
+                emin[i] = __fsub_rn(emin[i], 0.f);
+            }
+        } else {
+            for (int t = 0; t < tp.nd; t++) {
+                const float *q = base + tp.soff_d[t];
+                const float sv = tp.val_d[t];
+#pragma unroll
+                for (int i = 0; i < kT2Rows; i++) {
+                    const float v = q[i * P] + sv;
+                    if (v > dmax[i]) dmax[i] = v;
+                }
+            }
+            for (int t = 0; t < tp.ne; t++) {
+                const float *q = base + tp.soff_e[t];
+                const float sv = tp.val_e[t];
+#pragma unroll
+                for (int i = 0; i < kT2Rows; i++) {
+                    const float v = q[i * P] - sv;
+                    if (v < emin[i]) emin[i] = v;
+                }
             }
         }
         if (x < W) {
@@ -756,9 +776,28 @@ int run_composite(int op, const float *in, float *out, int64_t batch, int ndim, 
         tp->soff_e[t] = (te.off[t][0] - mny) * P + (te.off[t][1] - mnx);
         tp->val_e[t] = te.val[t];
     }
+    // flat element whose dilation and erosion offsets are the same set
+    bool sym = true;
+    for (int t = 0; t < pd.ntaps && sym; t++) sym = td.val[t] == 0.f;
+    if (sym) {
+        std::vector<int> od(pd.ntaps), oe(pd.ntaps);
+        for (int t = 0; t < pd.ntaps; t++) {
+            od[t] = tp->soff_d[t];
+            oe[t] = tp->soff_e[t];
+        }
+        std::sort(od.begin(), od.end());
+        std::sort(oe.begin(), oe.end());
+        sym = od == oe;
+    }
     const size_t smem = (size_t)(kT2H + tp->ext_y) * P * sizeof(float);
-    auto kern = op == 0 ? (P == 136 ? grey_composite2d_kernel<0, 136> : grey_composite2d_kernel<0, 160>)
-                        : (P == 136 ? grey_composite2d_kernel<1, 136> : grey_composite2d_kernel<1, 160>);
+    using KernT = void (*)(const float *, float *, GradParams, const Taps2DPair);
+    KernT kern;
+    if (sym)
+        kern = op == 0 ? (P == 136 ? grey_composite2d_kernel<0, 136, true> : grey_composite2d_kernel<0, 160, true>)
+                       : (P == 136 ? grey_composite2d_kernel<1, 136, true> : grey_composite2d_kernel<1, 160, true>);
+    else
+        kern = op == 0 ? (P == 136 ? grey_composite2d_kernel<0, 136, false> : grey_composite2d_kernel<0, 160, false>)
+                       : (P == 136 ? grey_composite2d_kernel<1, 136, false> : grey_composite2d_kernel<1, 160, false>);
     cudaError_t e = cudaSuccess;
     if (smem > 48 * 1024) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) {
