@@ -16,6 +16,9 @@
 // point; nearest: a run at the edges; constant: j itself -- constant-border
 // reads never route a gradient).  Interior voxels take a fast path over flat
 // offsets.  Sums run in tap order, then coordinate order.
+//
+// The same 2-D tile machinery also runs the one-pass grey composites
+// (morphological gradient and laplace, tm_grey_gradient / tm_grey_laplace).
 #include <algorithm>
 #include <cstring>
 #include <vector>
