@@ -24,6 +24,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -62,7 +63,7 @@ class ClockSampler:
 
     def __init__(self, gpu_index=0):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"tm_clocks_bench_{os.getpid()}.csv")
         self.gpu = gpu_index
 
     def __enter__(self):

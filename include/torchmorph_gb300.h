@@ -39,7 +39,7 @@ typedef struct CUstream_st *tm_stream_t; /* same type as cudaStream_t */
 typedef enum tm_status {
     TM_OK = 0,
     TM_ERR_INVALID_ARGUMENT = 1, /* bad shape, pointer, origin, mode, ...   */
-    TM_ERR_UNSUPPORTED = 2,      /* valid request this build does not serve */
+    TM_ERR_UNSUPPORTED = 2,      /* valid request the library does not serve */
     TM_ERR_CUDA = 3,             /* a CUDA runtime call or launch failed    */
     TM_ERR_TOO_LARGE = 4,        /* sizes overflow the kernel's index types */
     TM_ERR_WORKSPACE = 5,        /* workspace missing or too small          */
