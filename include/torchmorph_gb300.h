@@ -23,6 +23,10 @@
  *   - Functions that need temporary device memory take a caller-owned
  *     `workspace` of at least the size its *_workspace_size() companion
  *     returns; the library itself never allocates device memory.
+ *   - Per-device state (kernel attributes, the tm_edt_noalloc scratch
+ *     address) is cached for the life of the process: calling
+ *     cudaDeviceReset() on a device while the library is loaded is not
+ *     supported.
  */
 #ifndef TORCHMORPH_GB300_H
 #define TORCHMORPH_GB300_H
@@ -172,10 +176,11 @@ int tm_edt(const void *input, int in_dtype, int64_t batch, int ndim, const int64
  * area that the library keeps on every GPU that loads it until the process
  * exits; larger batches (above ~4M voxels of 3-D items or ~16M of 2-D items)
  * are rejected with TM_ERR_TOO_LARGE, other shapes with TM_ERR_UNSUPPORTED.
- * The first call on a device looks up the scratch area's device address;
- * make that first call outside any CUDA stream capture.  All calls on a
- * device share the scratch: calls whose GPU work may overlap must be
- * serialised by the caller.  Outputs as for tm_edt.
+ * The first call on a device (2-D or 3-D alike: nothing else is set up
+ * lazily on this path) looks up the scratch area's device address; make
+ * that first call outside any CUDA stream capture.  All calls on a device
+ * share the scratch: calls whose GPU work may overlap must be serialised by
+ * the caller.  Outputs as for tm_edt.
  */
 int tm_edt_noalloc(const void *input, int in_dtype, int64_t batch, int ndim, const int64_t *shape,
                    float *dist, int32_t *indices, int32_t *sqdist, tm_stream_t stream);

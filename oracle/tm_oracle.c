@@ -305,122 +305,128 @@ static void edt_line_sampled(double *g, int64_t *f, int64_t L, double s, int64_t
     }
 }
 
+/* The passes are parallel over every line of every item (an item's lines
+ * along one axis are independent), so all host threads work on a batch of
+ * any size; the per-voxel set-up and the outputs are parallel over voxels. */
 int tmo_edt(const uint8_t *fg, int64_t batch, int ndim, const int64_t *shape,
             const double *sampling, int64_t *sqdist, double *dist, int32_t *indices,
             int nthreads) {
     if (ndim < 1 || ndim > TMO_MAX_NDIM) return -1;
     int64_t stride[TMO_MAX_NDIM];
     strides_of(shape, ndim, stride);
-    int64_t n = prod64(shape, ndim);
+    const int64_t n = prod64(shape, ndim);
+    const int64_t total = n * batch;
     int64_t maxL = 1;
     for (int d = 0; d < ndim; d++)
         if (shape[d] > maxL) maxL = shape[d];
     set_threads(nthreads);
-#pragma omp parallel for schedule(dynamic, 1)
-    for (int64_t b = 0; b < batch; b++) {
-        const uint8_t *img = fg + b * n;
-        int64_t *gi = NULL;
-        double *gd = NULL;
-        int64_t *feat = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);
-        int64_t *lv = (int64_t *)malloc(sizeof(int64_t) * (size_t)maxL);
-        int64_t *lf = (int64_t *)malloc(sizeof(int64_t) * (size_t)maxL);
-        int64_t *v = (int64_t *)malloc(sizeof(int64_t) * (size_t)maxL);
-        int64_t *tf = (int64_t *)malloc(sizeof(int64_t) * (size_t)maxL);
-        int64_t *lgi = NULL, *tgi = NULL;
-        double *lgd = NULL, *tgd = NULL;
-        int any_bg = 0;
-        if (sampling) {
-            gd = (double *)malloc(sizeof(double) * (size_t)n);
-            lgd = (double *)malloc(sizeof(double) * (size_t)maxL);
-            tgd = (double *)malloc(sizeof(double) * (size_t)maxL);
-        } else {
-            gi = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);
-            lgi = (int64_t *)malloc(sizeof(int64_t) * (size_t)maxL);
-            tgi = (int64_t *)malloc(sizeof(int64_t) * (size_t)maxL);
-        }
-        for (int64_t i = 0; i < n; i++) {
-            int bg = img[i] == 0;
-            any_bg |= bg;
-            feat[i] = bg ? i : -1;
-            if (sampling)
-                gd[i] = bg ? 0.0 : INFINITY;
-            else
-                gi[i] = bg ? 0 : EDT_INF;
-        }
-        if (any_bg) {
-            for (int a = 0; a < ndim; a++) {
-                int64_t L = shape[a], st = stride[a];
-                int64_t outer = n / (L * st);
-                for (int64_t o = 0; o < outer; o++) {
-                    for (int64_t in = 0; in < st; in++) {
-                        int64_t base = o * L * st + in;
-                        for (int64_t q = 0; q < L; q++) {
-                            lf[q] = feat[base + q * st];
-                            if (sampling)
-                                lgd[q] = gd[base + q * st];
-                            else
-                                lgi[q] = gi[base + q * st];
-                        }
-                        if (sampling)
-                            edt_line_sampled(lgd, lf, L, sampling[a], v, tgd, tf);
-                        else
-                            edt_line_exact(lgi, lf, L, v, tgi, tf);
-                        for (int64_t q = 0; q < L; q++) {
-                            feat[base + q * st] = lf[q];
-                            if (sampling)
-                                gd[base + q * st] = lgd[q];
-                            else
-                                gi[base + q * st] = lgi[q];
-                        }
-                    }
-                }
-            }
-        }
-        /* Outputs from the final feature.  With no background at all the
-         * feature is the virtual site (-1, 0, ..., 0) (scipy behaviour,
-         * reference edt_kernel.cu:415-437). */
-        for (int64_t i = 0; i < n; i++) {
-            int64_t fc[TMO_MAX_NDIM], xc[TMO_MAX_NDIM];
-            int64_t rem = i;
-            for (int d = 0; d < ndim; d++) {
-                xc[d] = rem / stride[d];
-                rem %= stride[d];
-            }
-            if (any_bg) {
-                int64_t fr = feat[i];
-                for (int d = 0; d < ndim; d++) {
-                    fc[d] = fr / stride[d];
-                    fr %= stride[d];
-                }
-            } else {
-                for (int d = 0; d < ndim; d++) fc[d] = d == 0 ? -1 : 0;
-            }
-            if (indices)
-                for (int d = 0; d < ndim; d++)
-                    indices[(int64_t)d * batch * n + b * n + i] = (int32_t)fc[d];
-            int64_t s2 = 0;
-            double ds = 0.0;
-            for (int d = 0; d < ndim; d++) {
-                int64_t delta = xc[d] - fc[d];
-                s2 += delta * delta;
-                double dd = (double)delta * (sampling ? sampling[d] : 1.0);
-                ds += dd * dd;
-            }
-            if (sqdist && !sampling) sqdist[b * n + i] = s2;
-            if (dist) dist[b * n + i] = sqrt(ds);
-        }
+    int64_t *feat = (int64_t *)malloc(sizeof(int64_t) * (size_t)(total ? total : 1));
+    int64_t *gi = sampling ? NULL : (int64_t *)malloc(sizeof(int64_t) * (size_t)(total ? total : 1));
+    double *gd = sampling ? (double *)malloc(sizeof(double) * (size_t)(total ? total : 1)) : NULL;
+    uint8_t *any_bg = (uint8_t *)calloc((size_t)(batch ? batch : 1), 1);
+    if (!feat || (!gi && !gd) || !any_bg) {
         free(feat);
-        free(lv);
-        free(lf);
-        free(v);
-        free(tf);
         free(gi);
         free(gd);
-        free(lgi);
-        free(tgi);
-        free(lgd);
-        free(tgd);
+        free(any_bg);
+        return -2;
     }
+#pragma omp parallel for schedule(static)
+    for (int64_t t = 0; t < total; t++) {
+        const int bg = fg[t] == 0;
+        feat[t] = bg ? t % n : -1;
+        if (sampling)
+            gd[t] = bg ? 0.0 : INFINITY;
+        else
+            gi[t] = bg ? 0 : EDT_INF;
+        if (bg && !any_bg[t / n]) any_bg[t / n] = 1; /* benign race: only ever set to 1 */
+    }
+    for (int a = 0; a < ndim; a++) {
+        const int64_t L = shape[a], st = stride[a];
+        const int64_t lines_per_item = n / L;
+        const int64_t lines = lines_per_item * batch;
+#pragma omp parallel
+        {
+            int64_t *lf = (int64_t *)malloc(sizeof(int64_t) * (size_t)maxL);
+            int64_t *v = (int64_t *)malloc(sizeof(int64_t) * (size_t)maxL);
+            int64_t *tf = (int64_t *)malloc(sizeof(int64_t) * (size_t)maxL);
+            int64_t *lgi = (int64_t *)malloc(sizeof(int64_t) * (size_t)maxL);
+            int64_t *tgi = (int64_t *)malloc(sizeof(int64_t) * (size_t)maxL);
+            double *lgd = (double *)malloc(sizeof(double) * (size_t)maxL);
+            double *tgd = (double *)malloc(sizeof(double) * (size_t)maxL);
+#pragma omp for schedule(static)
+            for (int64_t line = 0; line < lines; line++) {
+                const int64_t b = line / lines_per_item;
+                if (!any_bg[b]) continue;
+                const int64_t r = line % lines_per_item;
+                const int64_t o = r / st, in = r % st;
+                const int64_t base = b * n + o * L * st + in;
+                for (int64_t q = 0; q < L; q++) {
+                    lf[q] = feat[base + q * st];
+                    if (sampling)
+                        lgd[q] = gd[base + q * st];
+                    else
+                        lgi[q] = gi[base + q * st];
+                }
+                if (sampling)
+                    edt_line_sampled(lgd, lf, L, sampling[a], v, tgd, tf);
+                else
+                    edt_line_exact(lgi, lf, L, v, tgi, tf);
+                for (int64_t q = 0; q < L; q++) {
+                    feat[base + q * st] = lf[q];
+                    if (sampling)
+                        gd[base + q * st] = lgd[q];
+                    else
+                        gi[base + q * st] = lgi[q];
+                }
+            }
+            free(lf);
+            free(v);
+            free(tf);
+            free(lgi);
+            free(tgi);
+            free(lgd);
+            free(tgd);
+        }
+    }
+    /* Outputs from the final feature.  With no background at all the
+     * feature is the virtual site (-1, 0, ..., 0) (scipy behaviour,
+     * reference edt_kernel.cu:415-437). */
+#pragma omp parallel for schedule(static)
+    for (int64_t t = 0; t < total; t++) {
+        const int64_t b = t / n, i = t % n;
+        int64_t fc[TMO_MAX_NDIM], xc[TMO_MAX_NDIM];
+        int64_t rem = i;
+        for (int d = 0; d < ndim; d++) {
+            xc[d] = rem / stride[d];
+            rem %= stride[d];
+        }
+        if (any_bg[b]) {
+            int64_t fr = feat[t];
+            for (int d = 0; d < ndim; d++) {
+                fc[d] = fr / stride[d];
+                fr %= stride[d];
+            }
+        } else {
+            for (int d = 0; d < ndim; d++) fc[d] = d == 0 ? -1 : 0;
+        }
+        if (indices)
+            for (int d = 0; d < ndim; d++) indices[(int64_t)d * total + t] = (int32_t)fc[d];
+        int64_t s2 = 0;
+        double ds = 0.0;
+        for (int d = 0; d < ndim; d++) {
+            int64_t delta = xc[d] - fc[d];
+            s2 += delta * delta;
+            double dd = (double)delta * (sampling ? sampling[d] : 1.0);
+            ds += dd * dd;
+        }
+        if (sqdist && !sampling) sqdist[t] = s2;
+        if (dist) dist[t] = sqrt(ds);
+    }
+    free(feat);
+    free(gi);
+    free(gd);
+    free(any_bg);
     return 0;
 }
 

@@ -1010,7 +1010,33 @@ constexpr int kShellD2 = 16;
 constexpr int kShellN = 257;  // offsets with |d|^2 <= 16
 constexpr int kShellRows = 32;  // rows (axis 1) per CTA
 constexpr int kShellThreads = 128;
-__constant__ uint32_t c_shell[kShellN];  // packed (dz+8) | (dy+8) << 4 | (dx+8) << 8 | d2 << 12
+// The offset list, packed (dz+8) | (dy+8) << 4 | (dx+8) << 8 | d2 << 12, built at
+// compile time in list order (|d|^2, then dx, dy, dz ascending), so no launch
+// depends on a host-side upload.
+struct ShellTable {
+    uint32_t v[kShellN];
+};
+constexpr ShellTable make_shell_table() {
+    ShellTable t{};
+    int n = 0;
+    for (int d2 = 0; d2 <= kShellD2; d2++)
+        for (int dx = -kShellR; dx <= kShellR; dx++)
+            for (int dy = -kShellR; dy <= kShellR; dy++)
+                for (int dz = -kShellR; dz <= kShellR; dz++)
+                    if (dx * dx + dy * dy + dz * dz == d2 && n < kShellN)
+                        t.v[n++] = (uint32_t)(dz + 8) | ((uint32_t)(dy + 8) << 4) | ((uint32_t)(dx + 8) << 8) |
+                                   ((uint32_t)d2 << 12);
+    return t;
+}
+constexpr int shell_count() {
+    int n = 0;
+    for (int dx = -kShellR; dx <= kShellR; dx++)
+        for (int dy = -kShellR; dy <= kShellR; dy++)
+            for (int dz = -kShellR; dz <= kShellR; dz++) n += dx * dx + dy * dy + dz * dz <= kShellD2;
+    return n;
+}
+static_assert(shell_count() == kShellN, "offset list size");
+__constant__ ShellTable c_shell = make_shell_table();
 
 // Background bitmap, ceil(L2 / 32) words per row, one word per thread.  When
 // rows are a multiple of 32 voxels (and the input 16-byte aligned) a word is
@@ -1108,7 +1134,7 @@ __global__ void __launch_bounds__(kShellThreads) edt_shell_kernel(const uint32_t
     const int tid = threadIdx.x;
     if (tid == 0) s_unresolved = 0;
     for (int t = tid; t < kShellN; t += kShellThreads) {
-        const uint32_t e = c_shell[t];
+        const uint32_t e = c_shell.v[t];
         const int dz = (int)(e & 15u) - 8, dy = (int)((e >> 4) & 15u) - 8, dx = (int)((e >> 8) & 15u) - 8;
         const int d2 = (int)(e >> 12);
         tab[t] = make_int2(dz * planep + dy * pitch + (dx >= 0 ? 0 : -1), (dx >= 0 ? dx : 32 + dx) | (d2 << 8));
@@ -1342,7 +1368,7 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
     uint32_t *planes = planes_all[warp];
     pdl_trigger();  // the fallback passes may be scheduled as this grid's CTAs retire
     for (int t = threadIdx.x; t < kShellN; t += kShellCtThreads) {
-        const uint32_t c = c_shell[t];
+        const uint32_t c = c_shell.v[t];
         tab2[t] = make_int2((int)c, __float_as_int(__fsqrt_rn((float)(c >> 12))));
     }
     if (lane < 2) bits[kSwWords - 2 + lane] = 0u;
@@ -1504,37 +1530,6 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
         }
         __syncwarp();  // res and bits are free for the next unit
     }
-}
-
-// The offset table lives in constant memory: upload it once per device.
-int upload_shell_table() {
-    static std::mutex mu;
-    static bool done[64] = {};
-    int dev = 0;
-    TM_CHECK_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) return fail(TM_ERR_UNSUPPORTED, "device index %d", dev);
-    std::lock_guard<std::mutex> lock(mu);
-    if (done[dev]) return TM_OK;
-    int status = TM_OK;
-    {
-        std::vector<std::array<int, 4>> v;  // (d2, dx, dy, dz)
-        for (int dz = -kShellR; dz <= kShellR; dz++)
-            for (int dy = -kShellR; dy <= kShellR; dy++)
-                for (int dx = -kShellR; dx <= kShellR; dx++) {
-                    const int d2 = dz * dz + dy * dy + dx * dx;
-                    if (d2 <= kShellD2) v.push_back({d2, dx, dy, dz});
-                }
-        std::sort(v.begin(), v.end());
-        uint32_t packed[kShellN];
-        for (int t = 0; t < kShellN; t++)
-            packed[t] = (uint32_t)(v[t][3] + 8) | ((uint32_t)(v[t][2] + 8) << 4) | ((uint32_t)(v[t][1] + 8) << 8) |
-                        ((uint32_t)v[t][0] << 12);
-        status = (int)v.size() == kShellN ? cuda_check(cudaMemcpyToSymbol(c_shell, packed, sizeof(packed)),
-                                                          "cudaMemcpyToSymbol(c_shell)")
-                                          : fail(TM_ERR_UNSUPPORTED, "shell table size mismatch");
-    }
-    if (status == TM_OK) done[dev] = true;
-    return status;
 }
 
 // ------------------------------------------------- chamfer, distances only
@@ -1811,8 +1806,7 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
     // the unfused pass 1 is unused on this path and holds the bitmap + flags.
     int *todo = nullptr;
     if (fused && p.L2 <= 1024) {
-        int st = upload_shell_table();
-        if (st != TM_OK) return st;
+        int st = TM_OK;
         const int ww = (p.L2 + 31) / 32;
         const int64_t nwords = g.batch * (int64_t)p.L0 * p.L1 * ww;
         uint32_t *bm = reinterpret_cast<uint32_t *>(c2);
