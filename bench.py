@@ -694,23 +694,30 @@ def sinkhorn_lines(dev, stream, cpu_baseline=True):
                      "scope": "whole iteration (2 split-bf16 GEMMs of 8192x256x8192 with 3 MMA "
                               "passes each + 2 potential-split kernels); executed bf16 MMA flops"}}
 
-    # the plain FP32 fused iterations (reference sinkhorn_fastiter / sinkhorn_logiter)
-    K = torch.exp(-cost / 0.05)
-    K_T = K.T.contiguous()
-    C_T = cost.T.contiguous()
-    u, v = torch.ones_like(a), torch.ones_like(b)
-    la, lb = a.log(), b.log()
-    lu, lv = torch.zeros_like(a), torch.zeros_like(b)
-    t_scal = time_device(lambda _: _C.sinkhorn_fastiter(a, b, K, K_T, u, v, 1), [None], 5, 1,
-                         stream) / 5
-    t_log = time_device(lambda _: _C.sinkhorn_logiter(la, lb, cost, C_T, lu, lv, 1, 0.05), [None],
-                        2, 1, stream) / 2
-    tc_it = t_it
-    out["sinkhorn_fp32_fused_256x8192"] = {
-        "ms_per_iteration_scaling": round(t_scal * 1e3, 3),
-        "ms_per_iteration_log": round(t_log * 1e3, 3),
-        "tensor_core_speedup_per_iteration_vs_scaling": round(t_scal / tc_it, 1),
-        "tensor_core_speedup_per_iteration_vs_log": round(t_log / tc_it, 1)}
+    # the FP32 CUDA-core solver on the same GPU (tiled contractions, one persistent
+    # launch per solve): per-iteration time from 13 minus 3 fixed iterations
+    fp32 = {}
+    for form, log_space in (("scaling", False), ("log", True)):
+        t = {}
+        for k in (3, 13):
+            _C.sinkhorn_f32_solve(a, b, cost, 0.05, k, 0.0, log_space)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            _C.sinkhorn_f32_solve(a, b, cost, 0.05, k, 0.0, log_space)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t[k] = e0.elapsed_time(e1) / 1e3
+        fp32[form] = (t[13] - t[3]) / 10
+    # scaling form: 2 d^2 n FMAs per half-step on the CUDA cores (2 flops each)
+    fp32_flops = 2 * 2.0 * d * d * n
+    out["sinkhorn_fp32_256x8192"] = {
+        "ms_per_iteration_scaling": round(fp32["scaling"] * 1e3, 3),
+        "ms_per_iteration_log": round(fp32["log"] * 1e3, 3),
+        "scaling_TFLOPs_fp32": round(fp32_flops / fp32["scaling"] / 1e12, 1),
+        "log_ex2_per_s": float(f"{2.0 * d * d * n / fp32['log']:.4g}"),
+        "tensor_core_speedup_per_iteration_vs_scaling": round(fp32["scaling"] / t_it, 1),
+        "tensor_core_speedup_per_iteration_vs_log": round(fp32["log"] / t_it, 1)}
     return out
 
 

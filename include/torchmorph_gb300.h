@@ -84,6 +84,14 @@ int tm_version(void);
  * waits). */
 int tm_device_error(int reset);
 
+/* Poll budget of the grid barriers of the cooperative persistent kernels
+ * (tm_pointcloud_sinkhorn, the FP32 Sinkhorn iterations): a CTA that waits
+ * longer records a timeout in the device status word (tm_device_error) and
+ * every CTA of the launch returns.  polls < 0 restores the default (2^26
+ * polls of ~64 ns).  The waits that guard TMA copies and tensor-core work
+ * keep their own fixed budget.  No counterpart in the reference. */
+void tm_set_grid_wait_budget(int64_t polls);
+
 /* ------------------------------------------------------------------ grey --
  * Replaces grey_erosion_cuda / grey_dilation_cuda
  * (torchmorph/csrc/torchmorph.cpp:3-19, torchmorph/csrc/grey_kernel.cu:332-356).
@@ -241,22 +249,71 @@ int tm_ragged_binary_dilation(const uint8_t *in, uint8_t *out, const void *plan,
                               const int64_t *origin, int border_value, tm_stream_t stream);
 
 /* -------------------------------------------------------------- sinkhorn --
+ * FP32 Sinkhorn on the CUDA cores for n histogram pairs sharing one (d, d)
+ * matrix.  Every call runs its iterations in ONE cooperative persistent
+ * launch (tiles of 128 matrix rows x 16 or 64 pairs, bounded grid barriers
+ * between half-steps); the workspace holds the launch's control block.
+ *
  * Replaces sinkhorn_fastiter (torchmorph/csrc/torchmorph.cpp:58-66,
  * torchmorph/csrc/ot_kernel.cu:188-233): n_iter scaling iterations
  * u = a / (K v + 1e-12), v = b / (K^T u + 1e-12) on (n, d) batches sharing
- * K (d, d).  u and v are updated in place.
+ * K (d, d).  u and v are updated in place.  workspace: 16-byte aligned,
+ * tm_sinkhorn_iter_workspace_size() bytes.
  */
+size_t tm_sinkhorn_iter_workspace_size(void);
 int tm_sinkhorn_fastiter(const float *a, const float *b, const float *K, const float *K_T,
                          float *u, float *v, int64_t n, int64_t d, int64_t n_iter,
-                         tm_stream_t stream);
+                         void *workspace, size_t workspace_bytes, tm_stream_t stream);
 
 /* Replaces sinkhorn_logiter (torchmorph/csrc/torchmorph.cpp:68-77,
  * torchmorph/csrc/ot_kernel.cu:235-283): n_iter log-domain iterations
- * log_u = log_a - LSE_j(-M_ij/eps + log_v_j), then the same for log_v with M_T.
+ * log_u = log_a - LSE_j(-M_ij/eps + log_v_j), then the same for log_v with
+ * M_T; -inf wherever every term is -inf.  Workspace as for fastiter.
  */
 int tm_sinkhorn_logiter(const float *log_a, const float *log_b, const float *M,
                         const float *M_T, float *log_u, float *log_v, int64_t n, int64_t d,
-                        int64_t n_iter, double epsilon, tm_stream_t stream);
+                        int64_t n_iter, double epsilon, void *workspace, size_t workspace_bytes,
+                        tm_stream_t stream);
+
+/* A whole FP32 solve on the device.  Replaces the fused branch of
+ * _scaling_iterations / _log_iterations and the plan materialisation of
+ * _SinkhornDistance.forward (torchmorph/optimal_transport.py:38-144):
+ * builds K = exp(-C/eps) and K^T (scaling form) or C^T (log form), starts
+ * from u = v = 1 (log u = log v = 0), runs up to max_iter iterations in one
+ * launch and, when threshold > 0, stops after the first iteration k with
+ * (k + 1) % check_every == 0 at which every pair's L1 row-marginal residual
+ * sum_i |a_i - (P 1)_i| of the plan that iteration started from is <=
+ * threshold (decided on the device: no host round trip).  Outputs: log_u,
+ * log_v (device fp32 (n, d), the reference's u.log() / log-potentials),
+ * cost[b] = <P_b, C> and row_err[b] (fp64 [n], for the returned potentials,
+ * P never materialised) and iterations (int32 scalar); cost, row_err and
+ * iterations may be NULL.  a, b: fp32 (n, d) rows summing to 1; C: fp32
+ * (d, d).  workspace: 256-byte aligned, tm_sinkhorn_f32_workspace_size bytes.
+ * No counterpart in the reference's extension (it exposes the iterations
+ * only). */
+size_t tm_sinkhorn_f32_workspace_size(int64_t n, int64_t d, int log_space, int64_t max_iter,
+                                      int64_t check_every);
+int tm_sinkhorn_f32_solve(const float *a, const float *b, const float *C, int64_t n, int64_t d,
+                          double epsilon, int log_space, int64_t max_iter, double threshold,
+                          int64_t check_every, float *log_u, float *log_v, double *cost,
+                          double *row_err, int32_t *iterations, void *workspace,
+                          size_t workspace_bytes, tm_stream_t stream);
+
+/* Transport plans plan[b, i, j] = exp((log_u[b, i] - C[i, j] / eps) +
+ * log_v[b, j]) (device fp32 (n, d, d)) in one pass, with the operations and
+ * rounding of SinkhornSolver.plan (torchmorph/optimal_transport.py:228-237).
+ */
+int tm_sinkhorn_plan(const float *log_u, const float *log_v, const float *C, int64_t n,
+                     int64_t d, double epsilon, float *plan, tm_stream_t stream);
+
+/* Gradient of sum_b grad_distance[b] * distance[b] with respect to the cost
+ * matrix by the envelope theorem: grad_C = sum_b grad_distance[b] P_b, plan
+ * entries recomputed from the log-potentials and never stored (device fp32
+ * (d, d)).  The reference returns no cost gradient
+ * (torchmorph/optimal_transport.py:146-150). */
+int tm_sinkhorn_cost_grad(const float *log_u, const float *log_v, const float *C,
+                          const float *grad_distance, int64_t n, int64_t d, double epsilon,
+                          float *grad_C, tm_stream_t stream);
 
 /* ------------------------------------------------ sinkhorn, tensor cores --
  * Shared-cost batched Sinkhorn on the tcgen05 tensor cores.  Replaces, for

@@ -79,12 +79,28 @@ def test_rejects_bad_geometry_without_touching_the_device():
     s, msg = _err(lib.tm_cdt(ctypes.c_void_p(16), 0, 1, 2, shape, 0, ctypes.c_void_p(16), None,
                              None, 0, None))
     assert s == 5 and "workspace" in msg
-    s, msg = _err(lib.tm_sinkhorn_logiter(None, None, None, None, None, None, 1, 4, 1, 1.0, None))
+    s, msg = _err(lib.tm_sinkhorn_logiter(None, None, None, None, None, None, 1, 4, 1, 1.0, None, 0,
+                                          None))
     assert s == 1
+    p = ctypes.c_void_p(256)
+    s, msg = _err(lib.tm_sinkhorn_fastiter(p, p, p, p, p, p, 2, 4, 3, None, 0, None))
+    assert s == 5 and "workspace" in msg
+    s, msg = _err(lib.tm_sinkhorn_f32_solve(p, p, p, 2, 4, 0.0, 0, 10, 0.0, 1, p, p, None, None, None,
+                                            None, 0, None))
+    assert s == 1 and "epsilon" in msg
+    s, msg = _err(lib.tm_sinkhorn_f32_solve(p, p, p, 2, 4, 0.1, 0, 10, 0.0, 1, p, p, None, None, None,
+                                            None, 0, None))
+    assert s == 5 and "workspace" in msg
+    s, msg = _err(lib.tm_sinkhorn_plan(p, p, p, 0, 4, 0.1, p, None))
+    assert s == 1 and "n >= 1" in msg
 
 
 def test_workspace_sizes():
     lib = _lib.load()
+    assert lib.tm_sinkhorn_iter_workspace_size() == 256
+    w = lib.tm_sinkhorn_f32_workspace_size(3, 300, 0, 100, 10)
+    assert w >= 2 * 300 * 300 * 4 + 2 * 3 * 300 * 4
+    assert lib.tm_sinkhorn_f32_workspace_size(3, 300, 1, 100, 10) < w  # the log form keeps no K
     assert lib.tm_edt_workspace_size(1, 1, _lib.i64_array([10]), None) == 0
     n2 = lib.tm_edt_workspace_size(4, 3, _lib.i64_array([8, 8, 8]), None)
     assert n2 >= 4 * 512 * (2 + 4)

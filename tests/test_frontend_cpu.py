@@ -91,13 +91,13 @@ def test_sinkhorn_one_solve_per_problem(monkeypatch):
     import torchmorph_gb300.optimal_transport as ot
 
     calls = []
-    real = ot._scaling_iterations
+    real = ot._torch_iterations
 
     def counting(*args, **kw):
         calls.append(1)
         return real(*args, **kw)
 
-    monkeypatch.setattr(ot, "_scaling_iterations", counting)
+    monkeypatch.setattr(ot, "_torch_iterations", counting)
     g = torch.Generator().manual_seed(43)
     src = (torch.rand((3, 6), generator=g, dtype=torch.float64) + 0.1).requires_grad_(True)
     tgt = torch.rand((3, 6), generator=g, dtype=torch.float64) + 0.1
@@ -126,6 +126,38 @@ def test_sinkhorn_one_solve_per_problem(monkeypatch):
     every.plan(src, tgt)
     every.plan(src, tgt)
     assert len(calls) == n + 5
+
+
+@pytest.mark.parametrize("log_space", [True, False])
+def test_sinkhorn_cost_gradient_is_the_envelope_gradient(log_space):
+    """d/dC of sum_b w_b <P_b, C> through the solver = sum_b w_b P_b, and that is the
+    derivative of the regularised cost W_b(C) = <a, f> + <b, g> - eps sum_ij P_ij
+    (f = eps log u, g = eps log v at the optimum): central differences of W along a
+    random direction, float64."""
+    import torchmorph_gb300.optimal_transport as ot
+
+    g = torch.Generator().manual_seed(5)
+    n, d, eps = 3, 7, 0.5
+    src = torch.rand((n, d), generator=g, dtype=torch.float64) + 0.1
+    tgt = torch.rand((n, d), generator=g, dtype=torch.float64) + 0.1
+    C = torch.rand((d, d), generator=g, dtype=torch.float64)
+    w = torch.rand(n, generator=g, dtype=torch.float64)
+    solver = tm.SinkhornSolver(epsilon=eps, max_iter=20000, threshold=1e-15, log_space=log_space)
+    Cg = C.clone().requires_grad_(True)
+    (solver(src, tgt, Cg) * w).sum().backward()
+    P = solver.plan(src, tgt, C)
+    torch.testing.assert_close(Cg.grad, (w[:, None, None] * P).sum(0), rtol=1e-12, atol=1e-15)
+
+    def regularised(Cx):
+        a, b, c = solver.data_preprocess(src, tgt, Cx)
+        lu, lv = ot._torch_iterations(a, b, c, eps, 20000, 1e-15, True)
+        mass = torch.exp(lu[:, :, None] + lv[:, None, :] - c / eps).sum((-2, -1))
+        return ((a * eps * lu).sum(-1) + (b * eps * lv).sum(-1) - eps * mass) @ w
+
+    delta = torch.rand((d, d), generator=g, dtype=torch.float64) - 0.5
+    h = 1e-5
+    fd = (regularised(C + h * delta) - regularised(C - h * delta)) / (2 * h)
+    torch.testing.assert_close(fd, (Cg.grad * delta).sum(), rtol=1e-7, atol=1e-10)
 
 
 def test_sinkhorn_argument_errors():

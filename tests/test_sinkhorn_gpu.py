@@ -5,7 +5,7 @@ import pytest
 import torch
 
 import oracle
-from torchmorph_gb300 import SinkhornSolver, _C, build_cost_matrix
+from torchmorph_gb300 import SinkhornSolver, _C, _lib, build_cost_matrix
 
 pytestmark = pytest.mark.gpu
 
@@ -72,3 +72,154 @@ def test_logiter_vs_oracle(cuda, eps):
 def test_cost_matrix_on_cuda(cuda):
     c = build_cost_matrix((3, 4), device="cuda")
     assert c.shape == (12, 12) and c.is_cuda
+
+
+# ------------------------------------------------------ the FP32 device solver
+def _ot_problem(n, d, seed):
+    r = np.random.default_rng(seed)
+    pts = r.random((d, 2))
+    cost = ((pts[:, None] - pts[None]) ** 2).sum(-1)
+    cost /= cost.max()
+    a = r.dirichlet(np.ones(d), n)
+    b = r.dirichlet(np.ones(d), n)
+    return a, b, cost
+
+
+def _f32(x):
+    return torch.tensor(x, dtype=torch.float32, device="cuda")
+
+
+def _centred(lu):
+    ok = np.isfinite(lu)
+    x = np.where(ok, lu, 0.0)
+    return np.where(ok, x - x.sum(1, keepdims=True) / ok.sum(1, keepdims=True), 0.0)
+
+
+# n = 5 and 30 take the 16-pair tiles, 70 the 64-pair tiles; d = 300 spans three
+# 128-row blocks, d = 301 takes the scalar staging path (d % 4 != 0)
+@pytest.mark.parametrize("log_space", [False, True])
+@pytest.mark.parametrize("n,d,eps,its", [(5, 96, 0.05, 300), (30, 300, 0.1, 200), (70, 301, 0.2, 120),
+                                         (1, 7, 0.5, 50)])
+def test_f32_solve_vs_fp64_oracle(cuda, log_space, n, d, eps, its):
+    a, b, cost = _ot_problem(n, d, seed=n + d)
+    lu, lv, dist, row_err, k = _C.sinkhorn_f32_solve(_f32(a), _f32(b), _f32(cost), eps, its, 0.0, log_space)
+    torch.cuda.synchronize()
+    assert int(k) == its
+    lu, lv = lu.double().cpu().numpy(), lv.double().cpu().numpy()
+    lu_o, lv_o, _ = oracle.sinkhorn(a, b, cost, eps, its, log_space=log_space)
+    # potentials up to the plan's (u c, v / c) invariance
+    assert np.max(np.abs(_centred(lu) - _centred(lu_o))) < 2e-4 / eps
+    # the fused cost and residual equal float64 sums over the returned potentials
+    a32 = a.astype(np.float32).astype(np.float64)
+    c32 = cost.astype(np.float32).astype(np.float64)
+    dist_here, rm, _ = oracle.sinkhorn_cost(c32, lu, lv, eps)
+    np.testing.assert_allclose(dist.cpu().numpy(), dist_here, rtol=2e-5)
+    np.testing.assert_allclose(row_err.cpu().numpy(), np.abs(rm - a32).sum(-1), rtol=1e-3, atol=2e-6)
+    dist_o, _, _ = oracle.sinkhorn_cost(cost, lu_o, lv_o, eps)
+    assert np.max(np.abs(dist.cpu().numpy() - dist_o) / dist_o) < 1e-4
+
+
+@pytest.mark.parametrize("log_space", [False, True])
+def test_f32_fixed_iterations_and_early_stop(cuda, log_space):
+    """The drop-in in-place iterations equal the solve's; a threshold stops on the
+    device at a multiple of 10 iterations with every residual below it, and the
+    stopped potentials equal a fixed run of that many iterations bit for bit."""
+    n, d, eps = 40, 200, 0.1
+    a, b, cost = _ot_problem(n, d, seed=3)
+    A, B, C = _f32(a), _f32(b), _f32(cost)
+    lu, lv, _, _, _ = _C.sinkhorn_f32_solve(A, B, C, eps, 37, 0.0, log_space)
+    if log_space:
+        u, v = torch.zeros_like(A), torch.zeros_like(B)
+        _C.sinkhorn_logiter(A.log(), B.log(), C, C.T.contiguous(), u, v, 37, eps)
+        fu, fv = u, v
+    else:
+        K = torch.exp(-C / eps)
+        u, v = torch.ones_like(A), torch.ones_like(B)
+        _C.sinkhorn_fastiter(A, B, K, K.T.contiguous(), u, v, 37)
+        fu, fv = u.log(), v.log()
+    torch.testing.assert_close(fu, lu, rtol=2e-6, atol=2e-6)
+    torch.testing.assert_close(fv, lv, rtol=2e-6, atol=2e-6)
+    tol = 1e-4
+    su, sv, _, err, k = _C.sinkhorn_f32_solve(A, B, C, eps, 5000, tol, log_space)
+    k = int(k)
+    assert 0 < k < 5000 and k % 10 == 0
+    assert err.max().item() <= 1.5 * tol
+    fu2, fv2, _, _, k2 = _C.sinkhorn_f32_solve(A, B, C, eps, k, 0.0, log_space)
+    assert int(k2) == k
+    assert torch.equal(su, fu2) and torch.equal(sv, fv2)
+    # the check before (iteration k - 10, measuring the plan after k - 11 iterations)
+    # found a residual above the threshold: the solve did not stop early
+    _, _, _, err_before, _ = _C.sinkhorn_f32_solve(A, B, C, eps, k - 11, 0.0, log_space)
+    assert err_before.max().item() > tol * 0.9
+
+
+def test_f32_solver_module_and_no_plan_in_forward(cuda):
+    """SinkhornSolver on CUDA float32 below the tensor-core sizes runs the device solve;
+    forward allocates no (n, d, d) plan (its peak memory stays far below one)."""
+    n, d = 8, 1024
+    a, b, cost = _ot_problem(n, d, seed=9)
+    A, B, C = _f32(a), _f32(b), _f32(cost)
+    solver = SinkhornSolver(epsilon=0.05, max_iter=100)
+    solver(A, B, C)
+    torch.cuda.synchronize()
+    torch.cuda.reset_peak_memory_stats()
+    base = torch.cuda.memory_allocated()
+    dist = SinkhornSolver(epsilon=0.05, max_iter=100)(A, B, C)
+    torch.cuda.synchronize()
+    # the scaling form's workspace holds K and K^T (2 d^2 floats); the plans would be n d^2
+    assert torch.cuda.max_memory_allocated() - base < n * d * d * 4 // 2
+    lu_o, lv_o, _ = oracle.sinkhorn(a, b, cost, 0.05, 100, log_space=False)
+    dist_o, _, _ = oracle.sinkhorn_cost(cost, lu_o, lv_o, 0.05)
+    assert np.max(np.abs(dist.cpu().numpy() - dist_o) / dist_o) < 1e-4
+
+
+@pytest.mark.parametrize("d", [64, 130])
+def test_plan_kernel_matches_the_reference_formula(cuda, d):
+    n, eps = 3, 0.07
+    a, b, cost = _ot_problem(n, d, seed=d)
+    lu = torch.randn((n, d), device="cuda")
+    lv = torch.randn((n, d), device="cuda")
+    C = _f32(cost)
+    got = _C.sinkhorn_plan(lu, lv, C, eps)
+    ref = torch.exp(lu.unsqueeze(-1) - C / eps + lv.unsqueeze(-2))
+    torch.testing.assert_close(got, ref, rtol=3e-7, atol=0)
+
+
+@pytest.mark.parametrize("tensor_cores", [False, True])
+def test_cost_gradient_kernel(cuda, tensor_cores):
+    """grad_C = sum_b w_b P_b from the solve's potentials, against float64 torch."""
+    n, d, eps = 40, 260, 0.05
+    a, b, cost = _ot_problem(n, d, seed=11)
+    A, B = _f32(a), _f32(b)
+    C = _f32(cost).requires_grad_(True)
+    w = torch.rand(n, device="cuda")
+    solver = SinkhornSolver(epsilon=eps, max_iter=200, tensor_cores=tensor_cores)
+    (solver(A, B, C) * w).sum().backward()
+    lu, lv, _, _, _ = solver._solve((A, B, C), *solver.data_preprocess(A, B, C))
+    P = torch.exp(lu.double().unsqueeze(-1) - C.detach().double() / eps + lv.double().unsqueeze(-2))
+    ref = (w.double()[:, None, None] * P).sum(0)
+    torch.testing.assert_close(C.grad.double(), ref, rtol=2e-5, atol=1e-9)
+
+
+def test_grid_barrier_wait_budget_times_out_and_returns(cuda):
+    """A poll budget of 0 makes the persistent solver's grid barriers give up: the
+    device status word reports the timeout, the call returns, and with the default
+    budget restored the next solve is correct again."""
+    lib = _lib.load()
+    n, d, eps = 70, 600, 0.1  # 5 x 2 tiles: several CTAs meet at every barrier
+    a, b, cost = _ot_problem(n, d, seed=2)
+    A, B, C = _f32(a), _f32(b), _f32(cost)
+    ref = _C.sinkhorn_f32_solve(A, B, C, eps, 50, 0.0, False)
+    torch.cuda.synchronize()
+    assert lib.tm_device_error(1) == 0
+    lib.tm_set_grid_wait_budget(0)
+    try:
+        _C.sinkhorn_f32_solve(A, B, C, eps, 50, 0.0, False)
+        torch.cuda.synchronize()
+        assert lib.tm_device_error(1) == 1
+    finally:
+        lib.tm_set_grid_wait_budget(-1)
+    again = _C.sinkhorn_f32_solve(A, B, C, eps, 50, 0.0, False)
+    torch.cuda.synchronize()
+    assert lib.tm_device_error(1) == 0
+    assert torch.equal(again[0], ref[0]) and torch.equal(again[1], ref[1])

@@ -66,6 +66,25 @@ def test_noalloc_matches_regular_entry_point_twice(shape, p):
             assert torch.equal(a, b)
 
 
+def test_noalloc_shell_search_volume_vs_oracle():
+    """A 128^3 Bernoulli(0.9) volume: rows of 128 voxels take the bitmap shell search
+    (the benchmarked fast path) on the shared scratch.  Distances, indices and squared
+    distances equal the oracle's on two calls in a row."""
+    if not torch.cuda.is_available():
+        pytest.skip("CUDA device required")
+    import oracle
+
+    lib = _lib.load()
+    for seed in (0, 1):
+        xn = np.random.default_rng(seed).random((1, 1, 128, 128, 128)) < 0.9
+        d, i, s = _noalloc(lib, torch.from_numpy(xn).cuda())
+        torch.cuda.synchronize()
+        sq, od, oi = oracle.edt(xn)
+        np.testing.assert_array_equal(d.cpu().numpy(), od.astype(np.float32))
+        np.testing.assert_array_equal(i.cpu().numpy(), oi)
+        np.testing.assert_array_equal(s.cpu().numpy(), sq.astype(np.int32))
+
+
 def test_noalloc_rejects_batches_beyond_its_scratch():
     if not torch.cuda.is_available():
         pytest.skip("CUDA device required")

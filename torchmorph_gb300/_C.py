@@ -335,8 +335,13 @@ def _ot_shapes(u, mat):
     return u.shape[0], u.shape[1]
 
 
+def _iter_workspace(device):
+    return _workspace(_lib.load().tm_sinkhorn_iter_workspace_size(), device)
+
+
 def sinkhorn_fastiter(a, b, K, K_T, u, v, n_iter):
-    """n_iter scaling-form iterations in place (reference ot_kernel.cu:188-233)."""
+    """n_iter scaling-form iterations in place, one persistent launch
+    (reference ot_kernel.cu:188-233)."""
     n, d = _ot_shapes(u, K)
     for t, name in ((a, "a"), (b, "b"), (u, "u"), (v, "v")):
         _ot_check(t, n * d, name)
@@ -344,15 +349,17 @@ def sinkhorn_fastiter(a, b, K, K_T, u, v, n_iter):
     _ot_check(K_T, d * d, "K_T")
     lib = _lib.load()
     with torch.cuda.device(u.device):
+        ws = _iter_workspace(u.device)
         st = lib.tm_sinkhorn_fastiter(_lib.ptr(a), _lib.ptr(b), _lib.ptr(K), _lib.ptr(K_T),
-                                      _lib.ptr(u), _lib.ptr(v), n, d, int(n_iter),
-                                      _lib.stream_of(u.device))
+                                      _lib.ptr(u), _lib.ptr(v), n, d, int(n_iter), _lib.ptr(ws),
+                                      ws.numel(), _lib.stream_of(u.device))
     _lib.check(st, "sinkhorn_fastiter")
     return u, v
 
 
 def sinkhorn_logiter(log_a, log_b, M, M_T, log_u, log_v, n_iter, epsilon):
-    """n_iter log-domain iterations in place (reference ot_kernel.cu:235-283)."""
+    """n_iter log-domain iterations in place, one persistent launch
+    (reference ot_kernel.cu:235-283)."""
     _require(epsilon > 0, f"epsilon must be positive, got {epsilon}")
     n, d = _ot_shapes(log_u, M)
     for t, name in ((log_a, "log_a"), (log_b, "log_b"), (log_u, "log_u"), (log_v, "log_v")):
@@ -361,11 +368,85 @@ def sinkhorn_logiter(log_a, log_b, M, M_T, log_u, log_v, n_iter, epsilon):
     _ot_check(M_T, d * d, "M_T")
     lib = _lib.load()
     with torch.cuda.device(log_u.device):
+        ws = _iter_workspace(log_u.device)
         st = lib.tm_sinkhorn_logiter(_lib.ptr(log_a), _lib.ptr(log_b), _lib.ptr(M), _lib.ptr(M_T),
                                      _lib.ptr(log_u), _lib.ptr(log_v), n, d, int(n_iter),
-                                     float(epsilon), _lib.stream_of(log_u.device))
+                                     float(epsilon), _lib.ptr(ws), ws.numel(),
+                                     _lib.stream_of(log_u.device))
     _lib.check(st, "sinkhorn_logiter")
     return log_u, log_v
+
+
+def sinkhorn_f32_solve(a, b, cost_matrix, epsilon, max_iter, threshold=0.0, log_space=False,
+                       check_every=10):
+    """A whole FP32 Sinkhorn solve on the device (libtmcore tm_sinkhorn_f32_solve).
+
+    a, b: (n, d) float32 CUDA histograms (rows summing to 1); cost_matrix (d, d).
+    Runs max_iter iterations in one launch, or, with threshold > 0, stops on
+    the device after the first multiple of `check_every` iterations at which
+    every pair's L1 row-marginal residual is <= threshold.  Returns (log_u,
+    log_v, cost, row_err, iterations): fp32 (n, d) log-potentials with the
+    reference's meaning, fp64 (n,) transport costs <P, C> and L1 row-marginal
+    residuals of the returned potentials (no plan is materialised), and the
+    iteration count as a 0-dim int32 device tensor (no host synchronisation).
+    """
+    _require(epsilon > 0, f"epsilon must be positive, got {epsilon}")
+    _require(a.dim() == 2 and a.shape == b.shape, "a and b must be (n, d) of the same shape")
+    n, d = a.shape
+    for t, name in ((a, "a"), (b, "b")):
+        _ot_check(t, n * d, name)
+    _ot_check(cost_matrix, d * d, "cost_matrix")
+    lib = _lib.load()
+    dev = a.device
+    check = int(check_every) if threshold > 0 else 0
+    with torch.cuda.device(dev):
+        nbytes = lib.tm_sinkhorn_f32_workspace_size(n, d, int(bool(log_space)), int(max_iter), check)
+        ws = _workspace(nbytes, dev)
+        log_u = torch.empty((n, d), dtype=torch.float32, device=dev)
+        log_v = torch.empty_like(log_u)
+        cost = torch.empty(n, dtype=torch.float64, device=dev)
+        row_err = torch.empty_like(cost)
+        its = torch.empty((), dtype=torch.int32, device=dev)
+        st = lib.tm_sinkhorn_f32_solve(_lib.ptr(a), _lib.ptr(b), _lib.ptr(cost_matrix), n, d,
+                                       float(epsilon), int(bool(log_space)), int(max_iter),
+                                       float(threshold), max(check, 1), _lib.ptr(log_u),
+                                       _lib.ptr(log_v), _lib.ptr(cost), _lib.ptr(row_err),
+                                       _lib.ptr(its), _lib.ptr(ws), nbytes, _lib.stream_of(dev))
+    _lib.check(st, "sinkhorn_f32_solve")
+    return log_u, log_v, cost, row_err, its
+
+
+def _plan_args(log_u, log_v, cost_matrix, epsilon):
+    _require(epsilon > 0, f"epsilon must be positive, got {epsilon}")
+    n, d = log_u.shape
+    for t, name in ((log_u, "log_u"), (log_v, "log_v")):
+        _ot_check(t, n * d, name)
+    _ot_check(cost_matrix, d * d, "cost_matrix")
+    return n, d
+
+
+def sinkhorn_plan(log_u, log_v, cost_matrix, epsilon):
+    """(n, d, d) transport plans exp((log u - C / eps) + log v), one pass."""
+    n, d = _plan_args(log_u, log_v, cost_matrix, epsilon)
+    out = torch.empty((n, d, d), dtype=torch.float32, device=log_u.device)
+    with torch.cuda.device(log_u.device):
+        st = _lib.load().tm_sinkhorn_plan(_lib.ptr(log_u), _lib.ptr(log_v), _lib.ptr(cost_matrix), n, d,
+                                          float(epsilon), _lib.ptr(out), _lib.stream_of(log_u.device))
+    _lib.check(st, "sinkhorn_plan")
+    return out
+
+
+def sinkhorn_cost_grad(log_u, log_v, cost_matrix, epsilon, grad_distance):
+    """(d, d) envelope gradient sum_b grad_distance[b] P_b, plans recomputed, never stored."""
+    n, d = _plan_args(log_u, log_v, cost_matrix, epsilon)
+    _ot_check(grad_distance, n, "grad_distance")
+    out = torch.empty((d, d), dtype=torch.float32, device=log_u.device)
+    with torch.cuda.device(log_u.device):
+        st = _lib.load().tm_sinkhorn_cost_grad(_lib.ptr(log_u), _lib.ptr(log_v), _lib.ptr(cost_matrix),
+                                               _lib.ptr(grad_distance), n, d, float(epsilon),
+                                               _lib.ptr(out), _lib.stream_of(log_u.device))
+    _lib.check(st, "sinkhorn_cost_grad")
+    return out
 
 
 # ----------------------------------------------- sinkhorn on tensor cores

@@ -52,10 +52,19 @@ SIGNATURES = {
     "tm_bfdt_workspace_size": (c_size, [c_i64, c_int, I64P]),
     "tm_bfdt": (c_int, [c_void, c_int, c_i64, c_int, I64P, c_int, F32P, c_void, c_void, c_void,
                         c_size, c_void]),
+    "tm_set_grid_wait_budget": (None, [c_i64]),
+    "tm_sinkhorn_iter_workspace_size": (c_size, []),
     "tm_sinkhorn_fastiter": (c_int, [c_void, c_void, c_void, c_void, c_void, c_void, c_i64, c_i64,
-                                     c_i64, c_void]),
+                                     c_i64, c_void, c_size, c_void]),
     "tm_sinkhorn_logiter": (c_int, [c_void, c_void, c_void, c_void, c_void, c_void, c_i64, c_i64,
-                                    c_i64, c_double, c_void]),
+                                    c_i64, c_double, c_void, c_size, c_void]),
+    "tm_sinkhorn_f32_workspace_size": (c_size, [c_i64, c_i64, c_int, c_i64, c_i64]),
+    "tm_sinkhorn_f32_solve": (c_int, [c_void, c_void, c_void, c_i64, c_i64, c_double, c_int, c_i64,
+                                      c_double, c_i64, c_void, c_void, c_void, c_void, c_void, c_void,
+                                      c_size, c_void]),
+    "tm_sinkhorn_plan": (c_int, [c_void, c_void, c_void, c_i64, c_i64, c_double, c_void, c_void]),
+    "tm_sinkhorn_cost_grad": (c_int, [c_void, c_void, c_void, c_void, c_i64, c_i64, c_double, c_void,
+                                      c_void]),
     "tm_gemm_bf16x3": (c_int, [c_void, c_void, c_void, c_void, c_void, c_i64, c_i64, c_i64,
                                c_void]),
     "tm_sinkhorn_tc_workspace_size": (c_size, [c_i64, c_i64]),

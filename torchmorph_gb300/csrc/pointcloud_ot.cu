@@ -94,11 +94,12 @@ struct PcArgs {
     int *status;
     float eps, threshold;
     int max_iter, check_every;
+    long long spin_limit;  // polls a barrier wait may take (tm_set_grid_wait_budget)
 };
 
 // Bounded grid barrier (sense by generation).  Returns false when it gave up
 // or another CTA aborted.
-__device__ bool grid_barrier(PcControl *ctl, unsigned nblocks, int *status) {
+__device__ bool grid_barrier(PcControl *ctl, unsigned nblocks, int *status, long long spin_limit) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -114,7 +115,7 @@ __device__ bool grid_barrier(PcControl *ctl, unsigned nblocks, int *status) {
         } else {
             long long polls = 0;
             while (*gen == g) {
-                if (*abort || ++polls > kSpinLimit) {
+                if (*abort || ++polls > spin_limit) {
                     ok = 0;
                     break;
                 }
@@ -312,7 +313,7 @@ __global__ void __launch_bounds__(kPcThreads) pc_sinkhorn_kernel(PcArgs a) {
                         (tile - P.row_tile0) * kPcTile, P.n, P.m, a.eps, make_float3(P.ox, P.oy, P.oz), nullptr,
                         nullptr, s_part);
         }
-        if (!grid_barrier(a.ctl, nblocks, a.status)) return;
+        if (!grid_barrier(a.ctl, nblocks, a.status, a.spin_limit)) return;
         const bool check = ((it + 1) % a.check_every == 0) || it + 1 == a.max_iter;
         // g-update over the column tiles (+ the column-marginal error on check iterations)
         const int ncol = *(volatile int *)&a.ctl->n_col_list;
@@ -339,7 +340,7 @@ __global__ void __launch_bounds__(kPcThreads) pc_sinkhorn_kernel(PcArgs a) {
                 if (threadIdx.x == 0) atomicAdd(&a.err[p], s_err);
             }
         }
-        if (!grid_barrier(a.ctl, nblocks, a.status)) return;
+        if (!grid_barrier(a.ctl, nblocks, a.status, a.spin_limit)) return;
         if (check) {
             if (blockIdx.x == 0) {
                 for (int p = threadIdx.x; p < a.nprob; p += kPcThreads) {
@@ -354,7 +355,7 @@ __global__ void __launch_bounds__(kPcThreads) pc_sinkhorn_kernel(PcArgs a) {
                 rebuild_lists(a, s_scan);
                 __threadfence();
             }
-            if (!grid_barrier(a.ctl, nblocks, a.status)) return;
+            if (!grid_barrier(a.ctl, nblocks, a.status, a.spin_limit)) return;
             if (*(volatile int *)&a.ctl->n_active <= 0) {
                 it++;
                 break;
@@ -641,6 +642,7 @@ extern "C" int tm_pointcloud_sinkhorn(const float *x, const float *y, const floa
     args.threshold = (float)threshold;
     args.max_iter = (int)max_iter;
     args.check_every = (int)check_every;
+    args.spin_limit = grid_wait_budget();
     void *params[] = {&args};
     TM_CHECK_CUDA(cudaLaunchCooperativeKernel((const void *)pc_sinkhorn_kernel, dim3(blocks), dim3(kPcThreads), params,
                                               0, s));

@@ -2,6 +2,7 @@
 #include <cudaTypedefs.h>
 
 #include <cstring>
+#include <atomic>
 #include <mutex>
 
 #include "tm_common.cuh"
@@ -124,7 +125,15 @@ int encode_tensor_map(CUtensorMap *map, CUtensorMapDataType dtype, int rank, con
     return TM_OK;
 }
 
+static std::atomic<long long> g_grid_wait_budget{kSpinLimit};
+
+long long grid_wait_budget() { return g_grid_wait_budget.load(); }
+
 }  // namespace tmc
+
+extern "C" void tm_set_grid_wait_budget(int64_t polls) {
+    tmc::g_grid_wait_budget.store(polls < 0 ? tmc::kSpinLimit : (long long)polls);
+}
 
 extern "C" int tm_device_error(int reset) {
     int *word = nullptr;

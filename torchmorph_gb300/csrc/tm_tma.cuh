@@ -27,6 +27,12 @@ int encode_tensor_map(CUtensorMap *map, CUtensorMapDataType dtype, int rank, con
 
 constexpr long long kSpinLimit = 1LL << 26;
 
+// Poll budget of the grid barriers of the cooperative persistent kernels
+// (point-cloud and FP32 Sinkhorn solvers): kSpinLimit unless the host set
+// another with tm_set_grid_wait_budget().  The waits that guard TMA copies and
+// tensor-core work in flight always use kSpinLimit.
+long long grid_wait_budget();
+
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }

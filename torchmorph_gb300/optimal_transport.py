@@ -1,26 +1,34 @@
 """Entropic optimal transport (reference torchmorph/optimal_transport.py).
 
-``SinkhornSolver`` keeps the reference's constructor, forward/plan/potentials
-API, preprocessing and autograd contract.  CUDA float32 inputs run libtmcore:
+``SinkhornSolver`` keeps the reference's constructor, forward / plan /
+potentials API, preprocessing and autograd contract.  CUDA float32 inputs are
+solved by libtmcore in one call each, with no host synchronisation:
 
 * many histogram pairs sharing one cost (``tensor_cores=None`` picks this
   for n >= 32 pairs of d >= 256 points; ``True`` forces it) run the
   tensor-core solver ``_C.sinkhorn_tc_solve``: the K v and K^T u products of
-  all pairs as one error-compensated BF16 GEMM per half-iteration, the
-  transport cost as one more GEMM (no (n, d, d) plan is materialised), and,
-  when ``threshold > 0``, a stop once every pair's L1 row-marginal residual
-  is <= threshold (checked every 10 iterations, fp64);
-* otherwise the fused FP32 iterations (``_C.sinkhorn_logiter`` /
-  ``_C.sinkhorn_fastiter``), as in the reference.
+  all pairs as one error-compensated BF16 GEMM per half-iteration and the
+  transport cost as one more GEMM;
+* otherwise the FP32 solver ``_C.sinkhorn_f32_solve``: the reference's
+  scaling or log-domain iterations as tiled CUDA-core contractions, every
+  iteration of the solve in one persistent launch, the transport cost
+  <P, C> fused (no (n, d, d) plan is materialised).
 
-Other dtypes/devices run the same iterations in plain torch, exactly as the
-reference does.
+With ``threshold > 0`` both stop once every pair's L1 row-marginal residual
+is <= threshold (checked every 10 iterations).  Inputs that are not CUDA
+float32 tensors (CPU tensors, float64) run the reference's torch iterations
+(:func:`_torch_iterations`), so the module stays a drop-in for them.
+
+Gradients (envelope theorem): w.r.t. the histograms, the centred dual
+potentials (the reference's rule); w.r.t. the cost matrix, sum_b g_b P_b,
+computed by ``_C.sinkhorn_cost_grad`` from the potentials without storing a
+plan (the reference returns no cost gradient).
 """
 
 from __future__ import annotations
 
 import weakref
-from typing import Optional
+from typing import NamedTuple, Optional
 
 import torch
 from torch import Tensor, nn
@@ -33,17 +41,25 @@ def build_cost_matrix(shape, p=2, device=None) -> Tensor:
     return torch.cdist(pts, pts, p=p)
 
 
-def _use_fused_kernels(t: Tensor) -> bool:
+_TC_MIN_PAIRS = 32
+_TC_MIN_POINTS = 256
+_CHECK_EVERY = 10
+
+
+class _Solution(NamedTuple):
+    log_u: Tensor          # (n, d) log-potentials (the reference's u.log() / log_u)
+    log_v: Tensor
+    cost: Optional[Tensor]     # (n,) <P, C> in float64 when the solver computed it
+    row_err: Optional[Tensor]  # (n,) L1 row-marginal residual of the returned potentials
+    iterations: object         # int, or a 0-dim device tensor (read only by solve())
+
+
+def _on_device(t: Tensor) -> bool:
     return t.is_cuda and t.dtype == torch.float32
 
 
-_TC_MIN_PAIRS = 32
-_TC_MIN_POINTS = 256
-_TC_CHECK_EVERY = 10
-
-
 def _use_tensor_cores(a: Tensor, cost_matrix: Tensor, tensor_cores) -> bool:
-    eligible = _use_fused_kernels(a) and cost_matrix.shape == (a.shape[1], a.shape[1])
+    eligible = _on_device(a) and cost_matrix.shape == (a.shape[1], a.shape[1])
     if tensor_cores is None:
         return eligible and a.shape[0] >= _TC_MIN_PAIRS and a.shape[1] >= _TC_MIN_POINTS
     if tensor_cores and not eligible:
@@ -51,114 +67,96 @@ def _use_tensor_cores(a: Tensor, cost_matrix: Tensor, tensor_cores) -> bool:
     return bool(tensor_cores)
 
 
-def _tensor_core_solve(a, b, cost_matrix, epsilon, max_iter, threshold):
+def _device_solve(a, b, cost_matrix, epsilon, max_iter, threshold, log_space, tensor_cores):
+    """One libtmcore call: the whole solve, its transport cost and residual."""
     from . import _C
 
-    return _C.sinkhorn_tc_solve(a.contiguous(), b.contiguous(), cost_matrix, epsilon, max_iter,
-                                threshold, _TC_CHECK_EVERY)
+    a, b = a.contiguous(), b.contiguous()
+    if tensor_cores:
+        out = _C.sinkhorn_tc_solve(a, b, cost_matrix, epsilon, max_iter, threshold, _CHECK_EVERY)
+    else:
+        out = _C.sinkhorn_f32_solve(a, b, cost_matrix, epsilon, max_iter, threshold, log_space,
+                                    _CHECK_EVERY)
+    return _Solution(*out)
 
 
-def _transpose_or_self(matrix: Tensor) -> Tensor:
-    return matrix if torch.equal(matrix, matrix.mT) else matrix.mT.contiguous()
+def _torch_iterations(a, b, cost_matrix, epsilon, max_iter, threshold, log_space):
+    """The reference's iterations for inputs that are not CUDA float32 (its CPU /
+    float64 path, optimal_transport.py:84-93 and 115-125): u is updated first,
+    scaling denominators carry +1e-12, and with threshold > 0 the loop stops
+    when, at an iteration i with i % 10 == 0, the largest L1 change of u over
+    the pairs is <= threshold.  Returns the log-potentials."""
+    if log_space:
+        log_k = -cost_matrix / epsilon
+        num = (a.log(), b.log())
+        mats = (log_k, log_k.mT)
+        state = [torch.zeros_like(a), torch.zeros_like(b)]
+
+        def half(k, other):
+            return num[k] - torch.logsumexp(mats[k] + other.unsqueeze(-2), dim=-1)
+    else:
+        kern = torch.exp(-cost_matrix / epsilon)
+        num = (a, b)
+        mats = (kern.mT, kern)
+        state = [torch.ones_like(a), torch.ones_like(b)]
+
+        def half(k, other):
+            return num[k] / (other @ mats[k] + 1e-12)
+
+    for i in range(max_iter):
+        before = state[0]
+        state[0] = half(0, state[1])
+        state[1] = half(1, state[0])
+        if threshold > 0 and i % 10 == 0 and (state[0] - before).abs().sum(dim=-1).max() <= threshold:
+            break
+    if log_space:
+        return state[0], state[1]
+    return state[0].log(), state[1].log()
 
 
-_GRAPH_MIN_ITER = 100
-_GRAPH_CHUNK = 25
-
-
-def _run_fused(launch, max_iter, device):
-    """Enqueue `max_iter` in-place iterations via launch(k); long runs replay a captured chunk."""
-    if max_iter < _GRAPH_MIN_ITER or torch.cuda.is_current_stream_capturing():
-        launch(max_iter)
-        return
-    try:
-        with torch.cuda.device(device):
-            side = torch.cuda.Stream()
-            side.wait_stream(torch.cuda.current_stream())
-            with torch.cuda.stream(side):
-                launch(_GRAPH_CHUNK)
-            torch.cuda.current_stream().wait_stream(side)
-            graph = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(graph):
-                launch(_GRAPH_CHUNK)
-            for _ in range(max_iter // _GRAPH_CHUNK - 1):
-                graph.replay()
-            rest = max_iter % _GRAPH_CHUNK
-            if rest:
-                launch(rest)
-    except RuntimeError:
-        launch(max_iter)  # fixed-point steps: extra iterations are harmless
-
-
-def _scaling_iterations(a, b, cost_matrix, epsilon, max_iter, threshold):
-    K = torch.exp(-cost_matrix / epsilon)
-    if _use_fused_kernels(a):
+def _plan(log_u, log_v, cost_matrix, epsilon):
+    """(n, d, d) plans exp((log u - C / eps) + log v) with the reference's rounding."""
+    if _on_device(log_u):
         from . import _C
 
-        a, b = a.contiguous(), b.contiguous()
-        K_T = _transpose_or_self(K)
-        u = torch.ones_like(a)
-        v = torch.ones_like(b)
-        _run_fused(lambda k: _C.sinkhorn_fastiter(a, b, K, K_T, u, v, k), max_iter, a.device)
-        return u.log(), v.log()
-    u = torch.ones_like(a)
-    v = torch.ones_like(b)
-    for i in range(max_iter):
-        u_prev = u
-        u = a / (v @ K.mT + 1e-12)
-        v = b / (u @ K + 1e-12)
-        if threshold > 0 and i % 10 == 0:
-            if (u - u_prev).abs().sum(dim=-1).max() <= threshold:
-                break
-    return u.log(), v.log()
-
-
-def _log_iterations(a, b, cost_matrix, epsilon, max_iter, threshold):
-    log_a, log_b = a.log(), b.log()
-    if _use_fused_kernels(a):
-        from . import _C
-
-        log_a, log_b = log_a.contiguous(), log_b.contiguous()
-        cost_T = _transpose_or_self(cost_matrix)
-        log_u = torch.zeros_like(a)
-        log_v = torch.zeros_like(b)
-        _run_fused(lambda k: _C.sinkhorn_logiter(log_a, log_b, cost_matrix, cost_T, log_u, log_v,
-                                                 k, epsilon), max_iter, a.device)
-        return log_u, log_v
-    log_K = -cost_matrix / epsilon
-    log_u = torch.zeros_like(a)
-    log_v = torch.zeros_like(b)
-    for i in range(max_iter):
-        prev = log_u
-        log_u = log_a - torch.logsumexp(log_K + log_v.unsqueeze(-2), dim=-1)
-        log_v = log_b - torch.logsumexp(log_K.mT + log_u.unsqueeze(-2), dim=-1)
-        if threshold > 0 and i % 10 == 0:
-            if (log_u - prev).abs().sum(dim=-1).max() <= threshold:
-                break
-    return log_u, log_v
+        return _C.sinkhorn_plan(log_u.contiguous(), log_v.contiguous(), cost_matrix, epsilon)
+    plan = torch.sub(log_u.unsqueeze(-1), (cost_matrix / epsilon).unsqueeze(0))
+    plan.add_(log_v.unsqueeze(-2))
+    return plan.exp_()
 
 
 class _SinkhornDistance(torch.autograd.Function):
-    """<P, C> from a solve's potentials, with envelope-theorem gradients (centred dual
-    potentials) for a and b."""
+    """<P, C> of a solve, with envelope-theorem gradients: the centred dual
+    potentials for a and b, sum_b g_b P_b for the cost matrix."""
 
     @staticmethod
     def forward(ctx, a, b, cost_matrix, epsilon, log_u, log_v, cost):
-        if cost is not None:  # the tensor-core solve's <P, C>
+        if cost is not None:  # computed by the device solver
             distance = cost.to(a.dtype)
         else:
-            plan = torch.exp(log_u.unsqueeze(-1) - cost_matrix / epsilon + log_v.unsqueeze(-2))
-            distance = (plan * cost_matrix).sum(dim=(-2, -1))
+            distance = (_plan(log_u, log_v, cost_matrix, epsilon) * cost_matrix).sum(dim=(-2, -1))
         f = epsilon * log_u
         g = epsilon * log_v
-        ctx.save_for_backward(f - f.mean(dim=-1, keepdim=True), g - g.mean(dim=-1, keepdim=True))
+        ctx.epsilon = epsilon
+        ctx.save_for_backward(f - f.mean(dim=-1, keepdim=True), g - g.mean(dim=-1, keepdim=True),
+                              log_u, log_v, cost_matrix)
         return distance
 
     @staticmethod
     def backward(ctx, grad_output):
-        f, g = ctx.saved_tensors
+        f, g, log_u, log_v, cost_matrix = ctx.saved_tensors
         grad = grad_output.unsqueeze(-1)
-        return grad * f, grad * g, None, None, None, None, None
+        grad_cost = None
+        if ctx.needs_input_grad[2]:
+            if _on_device(log_u):
+                from . import _C
+
+                grad_cost = _C.sinkhorn_cost_grad(log_u.contiguous(), log_v.contiguous(), cost_matrix,
+                                                  ctx.epsilon, grad_output.float().contiguous())
+            else:
+                plan = _plan(log_u, log_v, cost_matrix, ctx.epsilon)
+                grad_cost = (grad_output.to(plan.dtype)[:, None, None] * plan).sum(0)
+        return grad * f, grad * g, grad_cost, None, None, None, None
 
 
 class SinkhornSolver(nn.Module):
@@ -210,15 +208,15 @@ class SinkhornSolver(nn.Module):
         target = target / target.sum(dim=-1, keepdim=True).clamp(min=1e-12)
         return source, target, cost_matrix
 
-    def _solve(self, inputs, a, b, cost_matrix):
-        """(log_u, log_v, tensor-core cost or None, row error or None, iterations) of the
-        preprocessed problem (a, b, cost_matrix).  The last solve is kept and returned
-        again while the caller's tensors `inputs` (source, target, cost or None) are the
-        same objects, unmodified (version counters), and the solver's parameters are
-        unchanged: forward, plan, potentials and solve on one problem run one solve.
-        The solver holds weak references only, so it keeps no input alive.  Edits made
-        through ``.data`` do not move the version counter: a caller that mutates its
-        inputs that way constructs the solver with ``reuse_solves=False``."""
+    def _solve(self, inputs, a, b, cost_matrix) -> _Solution:
+        """The solution of the preprocessed problem (a, b, cost_matrix).  The last
+        solve is kept and returned again while the caller's tensors `inputs` (source,
+        target, cost or None) are the same objects, unmodified (version counters),
+        and the solver's parameters are unchanged: forward, plan, potentials and solve
+        on one problem run one solve.  The solver holds weak references only, so it
+        keeps no input alive.  Edits made through ``.data`` do not move the version
+        counter: a caller that mutates its inputs that way constructs the solver with
+        ``reuse_solves=False``."""
         params = (self.epsilon, self.max_iter, self.threshold, self.log_space, self.tensor_cores, self.p)
         versions = tuple(None if t is None else t._version for t in inputs)
         last = self._last
@@ -226,13 +224,16 @@ class SinkhornSolver(nn.Module):
                 (r is None and t is None) or (r is not None and r() is t) for r, t in zip(last[1], inputs)):
             return last[3]
         with torch.no_grad():
-            if _use_tensor_cores(a, cost_matrix, self.tensor_cores):
-                result = _tensor_core_solve(a, b, cost_matrix, self.epsilon, self.max_iter, self.threshold)
+            a, b, c = a.detach(), b.detach(), cost_matrix.detach()
+            if _on_device(a):
+                result = _device_solve(a, b, c, self.epsilon, self.max_iter, self.threshold, self.log_space,
+                                       _use_tensor_cores(a, c, self.tensor_cores))
             else:
-                iterate = _log_iterations if self.log_space else _scaling_iterations
-                log_u, log_v = iterate(a.detach(), b.detach(), cost_matrix, self.epsilon, self.max_iter,
-                                       self.threshold)
-                result = (log_u, log_v, None, None, self.max_iter)
+                if self.tensor_cores:
+                    _use_tensor_cores(a, c, True)  # raises: tensor cores need CUDA float32
+                log_u, log_v = _torch_iterations(a, b, c, self.epsilon, self.max_iter, self.threshold,
+                                                 self.log_space)
+                result = _Solution(log_u, log_v, None, None, self.max_iter)
         refs = tuple(None if t is None else weakref.ref(t) for t in inputs)
         self._last = (params, refs, versions, result)
         return result
@@ -241,48 +242,46 @@ class SinkhornSolver(nn.Module):
         """(n,) transport distances <P, C> between the rows of source and target."""
         inputs = (source, target, cost_matrix)
         a, b, c = self.data_preprocess(source, target, cost_matrix)
-        log_u, log_v, cost, _, _ = self._solve(inputs, a, b, c)
-        return _SinkhornDistance.apply(a, b, c, self.epsilon, log_u, log_v, cost)
+        sol = self._solve(inputs, a, b, c)
+        return _SinkhornDistance.apply(a, b, c, self.epsilon, sol.log_u, sol.log_v, sol.cost)
 
     @torch.no_grad()
     def solve(self, source: Tensor, target: Tensor, cost_matrix: Optional[Tensor] = None):
         """One solve with its diagnostics: a dict with ``distance`` (n,), centred
         potentials ``f``, ``g`` (n, d), ``marginal_error`` (n,) -- the L1 distance
         between the plan's row sums and the source histogram, in float64 -- and
-        ``iterations``."""
+        ``iterations`` (an int; reading it synchronises with the device)."""
         inputs = (source, target, cost_matrix)
         source, target, cost_matrix = self.data_preprocess(source, target, cost_matrix)
-        log_u, log_v, cost, row_err, its = self._solve(inputs, source, target, cost_matrix)
-        if cost is not None:
-            distance = cost.to(source.dtype)
+        sol = self._solve(inputs, source, target, cost_matrix)
+        if sol.cost is not None:
+            distance, row_err = sol.cost.to(source.dtype), sol.row_err
         else:
-            plan = torch.exp(log_u.unsqueeze(-1) - cost_matrix / self.epsilon
-                             + log_v.unsqueeze(-2))
+            plan = _plan(sol.log_u, sol.log_v, cost_matrix, self.epsilon)
             distance = (plan * cost_matrix).sum(dim=(-2, -1))
             row_err = (plan.double().sum(-1) - source.double()).abs().sum(-1)
-        f = self.epsilon * log_u
-        g = self.epsilon * log_v
+        f = self.epsilon * sol.log_u
+        g = self.epsilon * sol.log_v
         return {"distance": distance, "f": f - f.mean(dim=-1, keepdim=True),
                 "g": g - g.mean(dim=-1, keepdim=True), "marginal_error": row_err,
-                "iterations": its}
+                "iterations": int(sol.iterations)}
 
     @torch.no_grad()
     def plan(self, source: Tensor, target: Tensor, cost_matrix: Optional[Tensor] = None):
-        """(n, d, d) transport plans, built in place in one (n, d, d) buffer with the
-        reference's operations and rounding (log_u - C / eps, + log_v, exp)."""
+        """(n, d, d) transport plans exp((log u - C / eps) + log v), with the
+        reference's operations and rounding; CUDA float32 plans are written by one
+        kernel pass."""
         inputs = (source, target, cost_matrix)
         source, target, cost_matrix = self.data_preprocess(source, target, cost_matrix)
-        log_u, log_v, _, _, _ = self._solve(inputs, source, target, cost_matrix)
-        plan = torch.sub(log_u.unsqueeze(-1), (cost_matrix / self.epsilon).unsqueeze(0))
-        plan.add_(log_v.unsqueeze(-2))
-        return plan.exp_()
+        sol = self._solve(inputs, source, target, cost_matrix)
+        return _plan(sol.log_u, sol.log_v, cost_matrix, self.epsilon)
 
     @torch.no_grad()
     def potentials(self, source: Tensor, target: Tensor, cost_matrix: Optional[Tensor] = None):
         """Centred dual potentials (f, g), each (n, d)."""
         inputs = (source, target, cost_matrix)
         source, target, cost_matrix = self.data_preprocess(source, target, cost_matrix)
-        log_u, log_v, _, _, _ = self._solve(inputs, source, target, cost_matrix)
-        f = self.epsilon * log_u
-        g = self.epsilon * log_v
+        sol = self._solve(inputs, source, target, cost_matrix)
+        f = self.epsilon * sol.log_u
+        g = self.epsilon * sol.log_v
         return f - f.mean(dim=-1, keepdim=True), g - g.mean(dim=-1, keepdim=True)
