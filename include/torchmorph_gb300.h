@@ -92,6 +92,29 @@ int tm_device_error(int reset);
  * keep their own fixed budget.  No counterpart in the reference. */
 void tm_set_grid_wait_budget(int64_t polls);
 
+/* ------------------------------------------------------------ autotuning --
+ * Implementation variants of four operators, picked per work class by the
+ * autotuner (torchmorph_gb300/autotune.py).  Every variant of an operator
+ * computes bit-identical results; variant -1 restores the library's built-in
+ * choice.  The table is process-wide (host memory), so a tuning applies to
+ * every device of the process.  No counterpart in the reference (its block
+ * sizes are compile-time constants, e.g. torchmorph/csrc/ot_kernel.cu:9).
+ *   op 0  grey / binary flat 1-D / 2-D boxes: 0 TMA-staged persistent tiles,
+ *         1 plain loads (one CTA per tile), 2 / 3 TMA tiles with at most 1 / 2
+ *         CTAs per SM;                       class: log2(voxels)
+ *   op 1  FP32 Sinkhorn: bit 0 = 64 pairs per tile (else 16), bit 1 = one CTA
+ *         per SM (else two);                 class: 8 min(7, log2 n) + min(7, log2 d - 6)
+ *   op 2  3-D exact EDT: 0 bitmap shell search first, 1 separable passes only;
+ *                                             class: log2(voxels)
+ *   op 3  3-D chamfer distances: 0 bitmap shell search first, 1 raster passes
+ *         only;                               class: log2(voxels)
+ * tm_tune_class(op, a, b): the class of a call (a = voxels, or a = n pairs and
+ * b = d points for op 1). */
+int tm_tune_variants(int op);
+int tm_tune_class(int op, int64_t a, int64_t b);
+int tm_tune_set(int op, int cls, int variant);
+int tm_tune_get(int op, int cls);
+
 /* ------------------------------------------------------------------ grey --
  * Replaces grey_erosion_cuda / grey_dilation_cuda
  * (torchmorph/csrc/torchmorph.cpp:3-19, torchmorph/csrc/grey_kernel.cu:332-356).

@@ -53,6 +53,10 @@ SIGNATURES = {
     "tm_bfdt": (c_int, [c_void, c_int, c_i64, c_int, I64P, c_int, F32P, c_void, c_void, c_void,
                         c_size, c_void]),
     "tm_set_grid_wait_budget": (None, [c_i64]),
+    "tm_tune_variants": (c_int, [c_int]),
+    "tm_tune_class": (c_int, [c_int, c_i64, c_i64]),
+    "tm_tune_set": (c_int, [c_int, c_int, c_int]),
+    "tm_tune_get": (c_int, [c_int, c_int]),
     "tm_sinkhorn_iter_workspace_size": (c_size, []),
     "tm_sinkhorn_fastiter": (c_int, [c_void, c_void, c_void, c_void, c_void, c_void, c_i64, c_i64,
                                      c_i64, c_void, c_size, c_void]),
@@ -138,6 +142,14 @@ def load():
             fn.restype = res
             fn.argtypes = args
         _lib = lib
+    # install the autotuner's cached choices for this device (a missing or bad
+    # cache leaves the built-in choices)
+    try:
+        from . import autotune
+
+        autotune.apply_cache()
+    except Exception:  # noqa: BLE001 -- tuning is an optimisation, never a failure
+        pass
     return _lib
 
 

@@ -421,7 +421,9 @@ extern "C" int tm_cdt(const void *input, int in_dtype, int64_t batch, int ndim, 
     cudaStream_t s = (cudaStream_t)stream;
     int *todo = nullptr;
     bool cleared = false;
-    if (cdt_shell_shape(g) && cdt_shell_eligible(g, dist, indices)) {
+    // autotuned variant 1: the raster passes for every item (no shell search)
+    const bool shell = tune_variant(kTuneCdt3D, tune_class(kTuneCdt3D, g.numel, 0)) != 1;
+    if (shell && cdt_shell_shape(g) && cdt_shell_eligible(g, dist, indices)) {
         // counters first, so that nothing but kernels follows the shell search
         TM_CHECK_CUDA(clear_cdt_counters(ws, pl, s));
         cleared = true;

@@ -1805,7 +1805,9 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
     // for the items it could not finish (todo flags).  The (f0, f1) plane of
     // the unfused pass 1 is unused on this path and holds the bitmap + flags.
     int *todo = nullptr;
-    if (fused && p.L2 <= 1024) {
+    // autotuned variant 1: the separable passes for every item (no shell search)
+    const bool shell = tune_variant(kTuneEdt3D, tune_class(kTuneEdt3D, g.numel, 0)) != 1;
+    if (fused && p.L2 <= 1024 && shell) {
         int st = TM_OK;
         const int ww = (p.L2 + 31) / 32;
         const int64_t nwords = g.batch * (int64_t)p.L0 * p.L1 * ww;

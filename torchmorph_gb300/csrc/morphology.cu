@@ -339,9 +339,12 @@ int launch_flat2d(const T *in, T *out, Flat2DParams p, int64_t batch, int sms, c
     }
     // one persistent launch takes every tile (TMA for interior tiles) once a
     // batch has a few tiles per SM; otherwise the plain kernel does all
-    const bool tma_ok = (p.W % tp.align) == 0 && ((uintptr_t)in & 15) == 0 && tp.bw <= 256 && RH <= 256 &&
-                        p.H >= RH && p.W >= tp.bw && tp.ntiles >= 2LL * sms && tp.ntiles < ((int64_t)1 << 31) &&
-                        batch < ((int64_t)1 << 31);
+    // autotuned variant: 0 TMA-staged persistent tiles at full occupancy, 1 plain
+    // loads (one CTA per tile), 2 / 3 TMA with at most 1 / 2 CTAs per SM
+    const int variant = tune_variant(kTuneGreyFlat2D, tune_class(kTuneGreyFlat2D, batch * (int64_t)p.H * p.W, 0));
+    const bool tma_ok = variant != 1 && (p.W % tp.align) == 0 && ((uintptr_t)in & 15) == 0 && tp.bw <= 256 &&
+                        RH <= 256 && p.H >= RH && p.W >= tp.bw && tp.ntiles >= 2LL * sms &&
+                        tp.ntiles < ((int64_t)1 << 31) && batch < ((int64_t)1 << 31);
     if (!tma_ok) {
         flat2d_kernel<T, MAX, KH, KW><<<grid, kFlatThreads, smem, stream>>>(in, out, p);
         TM_LAUNCH_CHECK("flat2d_kernel");
@@ -375,7 +378,7 @@ int launch_flat2d(const T *in, T *out, Flat2DParams p, int64_t batch, int sms, c
         cached_smem = tsmem;
         cached_dev = dev;
     }
-    const int per_sm = cached_per_sm;
+    const int per_sm = variant == 2 ? 1 : (variant == 3 ? std::min(cached_per_sm, 2) : cached_per_sm);
     const int64_t ctas = std::min<int64_t>(tp.ntiles, (int64_t)sms * per_sm);
     flat2d_tma_kernel<T, MAX, KH, KW><<<(unsigned)ctas, kFlatThreads, tsmem, stream>>>(map, in, out, p, tp, status);
     TM_LAUNCH_CHECK("flat2d_tma_kernel");

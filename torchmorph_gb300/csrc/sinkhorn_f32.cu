@@ -594,13 +594,17 @@ int sk_launch(bool log_form, SkArgs A, cudaStream_t s) {
     if (st != TM_OK) return st;
     A.status = status;
     A.spin_limit = grid_wait_budget();
-    const bool wide = A.n > 24;  // 64 pairs per tile, else 16
+    // autotuned variant: bit 0 = 64 pairs per tile (else 16), bit 1 = one CTA per SM
+    // (else two); built-in: 64 pairs per tile above 24 pairs, two CTAs per SM
+    const int variant = tune_variant(kTuneSinkhornF32, tune_class(kTuneSinkhornF32, A.n, A.d));
+    const bool wide = variant < 0 ? A.n > 24 : (variant & 1) != 0;
     const void *kern;
     if (log_form) kern = wide ? (const void *)sk_solve_kernel<true, 4> : (const void *)sk_solve_kernel<true, 1>;
     else kern = wide ? (const void *)sk_solve_kernel<false, 4> : (const void *)sk_solve_kernel<false, 1>;
     int per_sm = 0;
     TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSkThreads, 0));
     if (per_sm < 1) return fail(TM_ERR_UNSUPPORTED, "Sinkhorn kernel does not fit on an SM");
+    if (variant >= 0 && (variant & 2)) per_sm = 1;
     const int tb = wide ? 64 : 16;
     const int64_t tiles = ceil_div(A.d, kSkRows) * ceil_div(A.n, tb);
     const int blocks = (int)std::min<int64_t>(tiles, (int64_t)per_sm * sm_count());

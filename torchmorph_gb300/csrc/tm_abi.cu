@@ -2,6 +2,7 @@
 #include <cudaTypedefs.h>
 
 #include <cstring>
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 
@@ -125,11 +126,74 @@ int encode_tensor_map(CUtensorMap *map, CUtensorMapDataType dtype, int rank, con
     return TM_OK;
 }
 
+// --------------------------------------------------------------- autotuning
+// Variant table: (operator, work class) -> variant, -1 = built-in choice.
+constexpr int kTuneClasses = 64;
+static const int kTuneVariants[kTuneOps] = {4, 4, 2, 2};
+static std::atomic<int> g_tune[kTuneOps][kTuneClasses];
+static std::once_flag g_tune_once;
+
+static void tune_init() {
+    std::call_once(g_tune_once, [] {
+        for (auto &row : g_tune)
+            for (auto &v : row) v.store(-1);
+    });
+}
+
+static int floor_log2(int64_t x) {
+    int k = 0;
+    while (x > 1) {
+        x >>= 1;
+        k++;
+    }
+    return k;
+}
+
+// Work class: log2 of the voxel count (morphology, distance transforms), or
+// 8 * min(7, log2 n) + min(7, log2 d - 6) for n histogram pairs of d points.
+int tune_class(int op, int64_t a, int64_t b) {
+    if (op == kTuneSinkhornF32) {
+        const int cn = std::min(7, floor_log2(std::max<int64_t>(a, 1)));
+        const int cd = std::min(7, std::max(0, floor_log2(std::max<int64_t>(b, 1)) - 6));
+        return 8 * cn + cd;
+    }
+    return std::min(kTuneClasses - 1, floor_log2(std::max<int64_t>(a, 1)));
+}
+
+int tune_variant(int op, int cls) {
+    if (op < 0 || op >= kTuneOps || cls < 0 || cls >= kTuneClasses) return -1;
+    tune_init();
+    return g_tune[op][cls].load(std::memory_order_relaxed);
+}
+
 static std::atomic<long long> g_grid_wait_budget{kSpinLimit};
 
 long long grid_wait_budget() { return g_grid_wait_budget.load(); }
 
 }  // namespace tmc
+
+extern "C" int tm_tune_variants(int op) {
+    if (op < 0 || op >= tmc::kTuneOps) return tmc::fail(TM_ERR_INVALID_ARGUMENT, "unknown tuning operator %d", op), 0;
+    return tmc::kTuneVariants[op];
+}
+
+extern "C" int tm_tune_class(int op, int64_t a, int64_t b) {
+    if (op < 0 || op >= tmc::kTuneOps) return -1;
+    return tmc::tune_class(op, a, b);
+}
+
+extern "C" int tm_tune_set(int op, int cls, int variant) {
+    using namespace tmc;
+    if (op < 0 || op >= kTuneOps) return fail(TM_ERR_INVALID_ARGUMENT, "unknown tuning operator %d", op);
+    if (cls < 0 || cls >= kTuneClasses) return fail(TM_ERR_INVALID_ARGUMENT, "work class %d out of range", cls);
+    if (variant < -1 || variant >= kTuneVariants[op])
+        return fail(TM_ERR_INVALID_ARGUMENT, "operator %d has variants 0..%d (-1: built-in)", op, kTuneVariants[op] - 1);
+    tune_init();
+    g_tune[op][cls].store(variant);
+    return TM_OK;
+}
+
+extern "C" int tm_tune_get(int op, int cls) { return tmc::tune_variant(op, cls); }
 
 extern "C" void tm_set_grid_wait_budget(int64_t polls) {
     tmc::g_grid_wait_budget.store(polls < 0 ? tmc::kSpinLimit : (long long)polls);

@@ -26,6 +26,13 @@ inline int launch_check(const char *kernel) { return cuda_check(cudaGetLastError
 // Number of SMs of the current device (cached per device).
 int sm_count();
 
+// Implementation variants picked by the autotuner (tm_tune_set), per operator
+// and work class; -1 = the library's built-in choice.  Every variant of an
+// operator gives bit-identical results.
+enum TuneOp { kTuneGreyFlat2D = 0, kTuneSinkhornF32 = 1, kTuneEdt3D = 2, kTuneCdt3D = 3, kTuneOps = 4 };
+int tune_variant(int op, int cls);
+int tune_class(int op, int64_t a, int64_t b);
+
 // Host-side geometry of a batch of items.
 struct Geometry {
     int ndim;
