@@ -271,6 +271,59 @@ int tm_ragged_binary_dilation(const uint8_t *in, uint8_t *out, const void *plan,
                               int64_t n_items, const uint8_t *structure, const int64_t *sshape,
                               const int64_t *origin, int border_value, tm_stream_t stream);
 
+/* Ragged batches of 3-D volumes (volume i: depths[i] x heights[i] x
+ * widths[i] elements from element offsets[i]).  Each operator is ONE
+ * persistent launch over the 4 x 8 x 32 output tiles of all volumes, taken
+ * from the plan's work queue and computed from a shared-memory copy of the
+ * tile's input region; per volume the result equals the uniform-batch
+ * operator on that volume (batch 1, ndim 3), i.e. the reference's per-volume
+ * calls of grey_erosion_cuda ... (torchmorph/csrc/torchmorph.cpp:3-33).
+ * Structures up to 255 per axis and 1024 active taps.  Other arguments as
+ * for the 2-D ragged operators. */
+size_t tm_ragged3d_plan_size(int64_t n_items);
+int tm_ragged3d_plan(int64_t n_items, const int64_t *depths, const int64_t *heights,
+                     const int64_t *widths, const int64_t *offsets, void *plan, size_t plan_bytes,
+                     tm_stream_t stream);
+int tm_ragged3d_grey_erosion(const float *in, float *out, const void *plan, size_t plan_bytes,
+                             int64_t n_items, const float *structure, const uint8_t *footprint,
+                             const int64_t *sshape, const int64_t *origin, int mode, float cval,
+                             tm_stream_t stream);
+int tm_ragged3d_grey_dilation(const float *in, float *out, const void *plan, size_t plan_bytes,
+                              int64_t n_items, const float *structure, const uint8_t *footprint,
+                              const int64_t *sshape, const int64_t *origin, int mode, float cval,
+                              tm_stream_t stream);
+int tm_ragged3d_binary_erosion(const uint8_t *in, uint8_t *out, const void *plan, size_t plan_bytes,
+                               int64_t n_items, const uint8_t *structure, const int64_t *sshape,
+                               const int64_t *origin, int border_value, tm_stream_t stream);
+int tm_ragged3d_binary_dilation(const uint8_t *in, uint8_t *out, const void *plan, size_t plan_bytes,
+                                int64_t n_items, const uint8_t *structure, const int64_t *sshape,
+                                const int64_t *origin, int border_value, tm_stream_t stream);
+
+/* Ragged exact EDT (unit spacing) of n_items 2-D or 3-D items (shapes:
+ * int64[n_items * ndim] host, item i at element offsets[i] of the packed
+ * input), in ONE cooperative persistent launch: the separable passes of
+ * edt_cuda (torchmorph/csrc/edt_kernel.cu:904-958, scipy's tie rule) run for
+ * all items at once, one grid-wide phase per axis.  Replaces the reference's
+ * per-item calls of torchmorph/distance_transform.py:72-102.
+ *   tm_ragged_edt_plan   builds the device descriptor table once per layout;
+ *   tm_ragged_edt        input: float32 or uint8 (nonzero = foreground);
+ *                        total = packed element count; max_line = longest
+ *                        axis of any item; lines[a] = sum over items of
+ *                        numel / shape[a]; dist float32[total], indices
+ *                        int32 (ndim, total) (item-local coordinates), sqdist
+ *                        int32[total], each optional; workspace of
+ *                        tm_ragged_edt_workspace_size(total, max_line) bytes,
+ *                        256-byte aligned.
+ * Axes up to 32767 voxels, items below 2^31 voxels. */
+size_t tm_ragged_edt_plan_size(int64_t n_items);
+int tm_ragged_edt_plan(int64_t n_items, int ndim, const int64_t *shapes, const int64_t *offsets,
+                       void *plan, size_t plan_bytes, tm_stream_t stream);
+size_t tm_ragged_edt_workspace_size(int64_t total, int64_t max_line);
+int tm_ragged_edt(const void *input, int in_dtype, const void *plan, size_t plan_bytes,
+                  int64_t n_items, int ndim, int64_t total, int64_t max_line, const int64_t *lines,
+                  float *dist, int32_t *indices, int32_t *sqdist, void *workspace,
+                  size_t workspace_bytes, tm_stream_t stream);
+
 /* -------------------------------------------------------------- sinkhorn --
  * FP32 Sinkhorn on the CUDA cores for n histogram pairs sharing one (d, d)
  * matrix.  Every call runs its iterations in ONE cooperative persistent

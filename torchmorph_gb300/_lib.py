@@ -97,6 +97,21 @@ SIGNATURES = {
     "tm_pointcloud_sinkhorn_grad": (c_int, [c_void, c_void, c_void, c_void, c_void, c_void, c_i64, I64P,
                                             I64P, c_double, c_void, c_void, c_void, c_void, c_size,
                                             c_void]),
+    "tm_ragged3d_plan_size": (c_size, [c_i64]),
+    "tm_ragged3d_plan": (c_int, [c_i64, I64P, I64P, I64P, I64P, c_void, c_size, c_void]),
+    "tm_ragged3d_grey_erosion": (c_int, [c_void, c_void, c_void, c_size, c_i64, F32P, U8P, I64P, I64P,
+                                         c_int, c_float, c_void]),
+    "tm_ragged3d_grey_dilation": (c_int, [c_void, c_void, c_void, c_size, c_i64, F32P, U8P, I64P, I64P,
+                                          c_int, c_float, c_void]),
+    "tm_ragged3d_binary_erosion": (c_int, [c_void, c_void, c_void, c_size, c_i64, U8P, I64P, I64P, c_int,
+                                           c_void]),
+    "tm_ragged3d_binary_dilation": (c_int, [c_void, c_void, c_void, c_size, c_i64, U8P, I64P, I64P, c_int,
+                                            c_void]),
+    "tm_ragged_edt_plan_size": (c_size, [c_i64]),
+    "tm_ragged_edt_plan": (c_int, [c_i64, c_int, I64P, I64P, c_void, c_size, c_void]),
+    "tm_ragged_edt_workspace_size": (c_size, [c_i64, c_i64]),
+    "tm_ragged_edt": (c_int, [c_void, c_int, c_void, c_size, c_i64, c_int, c_i64, c_i64, I64P, c_void, c_void,
+                              c_void, c_void, c_size, c_void]),
     "tm_ragged_plan_size": (c_size, [c_i64]),
     "tm_ragged_plan": (c_int, [c_i64, I64P, I64P, I64P, c_void, c_size, c_void]),
     "tm_ragged_grey_erosion": (c_int, [c_void, c_void, c_void, c_size, c_i64, F32P, U8P, I64P, I64P,

@@ -11,6 +11,18 @@
 namespace tmc {
 namespace morph {
 
+}  // namespace morph
+
+// 3-D items on shared-memory tiles (stencil3d.cu).  Sets *done = false and
+// returns TM_OK, launching nothing, when the element does not fit the tile
+// kernel (more than 1024 active taps, or a tile beyond shared memory).
+template <typename T, bool MAX>
+int stencil3d_uniform(const T *in, T *out, int64_t batch, const int64_t *shape, const float *structure,
+                      const uint8_t *footprint, const int64_t *sshape, const int64_t *origin, int mode, float cval,
+                      cudaStream_t s, bool *done);
+
+namespace morph {
+
 // ---------------------------------------------------------------- op traits
 template <typename T, bool MAX>
 struct MorphOp;

@@ -460,6 +460,12 @@ int run_morphology(const T *in, T *out, int64_t batch, int ndim, const int64_t *
         }
     }
 stencil:
+    if (ndim == 3 && g.numel_item < ((int64_t)1 << 31)) {  // 3-D items: shared-memory tiles
+        bool done = false;
+        st = stencil3d_uniform<T, MAX>(in, out, batch, shape, structure, footprint, sshape, origin, mode, cval,
+                                       stream, &done);
+        if (st != TM_OK || done) return st;
+    }
     {
         StencilParams p;
         std::memset(&p, 0, sizeof(p));

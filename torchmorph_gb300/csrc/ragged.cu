@@ -255,8 +255,16 @@ int persistent_grid(K kernel, size_t smem, int *grid) {
                 return TM_OK;
             }
     }
-    if (smem > 48 * 1024)
-        TM_CHECK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // the attribute allows the largest tile on the device (minus the kernel's static
+    // shared memory), so that a later launch with a larger tile than a cached one fits
+    int optin = 0;
+    TM_CHECK_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    TM_CHECK_CUDA(cudaFuncGetAttributes(&fa, kernel));
+    const int max_dynamic = optin - (int)fa.sharedSizeBytes;
+    if (smem > (size_t)max_dynamic)
+        return fail(TM_ERR_UNSUPPORTED, "ragged tile needs %zu bytes of shared memory", smem);
+    TM_CHECK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic));
     int per_sm = 0;
     TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kFlatThreads, smem));
     if (per_sm < 1) return fail(TM_ERR_UNSUPPORTED, "ragged tile does not fit on an SM");

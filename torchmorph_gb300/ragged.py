@@ -1,12 +1,16 @@
-"""Ragged batches of 2-D images: one persistent launch per operator.
+"""Ragged batches of 2-D images or 3-D volumes: one persistent launch per operator.
 
-A :class:`RaggedBatch` packs 2-D images of different sizes one after another
-in a single flat CUDA buffer and keeps a device plan with one descriptor per
-image.  Every operator here runs as ONE launch over the tiles of all images
-(libtmcore ``tm_ragged_*``) instead of one launch per image; the result for
-each image is bit-identical to the uniform-batch operator applied to
-``image[None, None]`` (``grey_erosion`` ... in ``torchmorph_gb300.morphology``,
-i.e. the reference's ``torchmorph/morphology/grey.py`` and ``binary.py``).
+A :class:`RaggedBatch` packs items of different sizes -- all 2-D images or
+all 3-D volumes -- one after another in a single flat CUDA buffer and keeps
+a device plan with one descriptor per item.  Every operator here runs as ONE
+launch over the tiles of all items (libtmcore ``tm_ragged_*`` for images,
+``tm_ragged3d_*`` for volumes, ``tm_ragged_edt`` for the distance transform)
+instead of one launch per item; the result for each item is bit-identical to
+the uniform-batch operator applied to ``item[None, None]`` (``grey_erosion``
+... in ``torchmorph_gb300.morphology`` and
+``euclidean_distance_transform``, i.e. the reference's
+``torchmorph/morphology/grey.py``, ``binary.py`` and
+``distance_transform.py:72-102``).
 
 The plan depends only on the image shapes, so batches derived from one
 another share it, and a fixed sequence of operators can be captured once into
@@ -28,40 +32,46 @@ from .morphology.structure import _normalize_origin, _validate_origin, generate_
 
 
 class RaggedBatch:
-    """2-D images of different shapes packed in one contiguous 1-D CUDA buffer."""
+    """Items of different shapes (all 2-D or all 3-D) packed in one contiguous 1-D CUDA buffer."""
 
     def __init__(self, data: Tensor, shapes: Sequence[Sequence[int]], offsets: Sequence[int] | None = None,
                  plan: Tensor | None = None):
         if data.dim() != 1 or not data.is_contiguous():
             raise ValueError("RaggedBatch data must be a contiguous 1-D tensor")
         self.data = data
-        self.shapes = [(int(h), int(w)) for h, w in shapes]
+        self.shapes = [tuple(int(v) for v in sh) for sh in shapes]
         if not self.shapes:
             raise ValueError("a RaggedBatch needs at least one image")
-        if any(h < 1 or w < 1 for h, w in self.shapes):
+        nd = len(self.shapes[0])
+        if nd not in (2, 3) or any(len(sh) != nd for sh in self.shapes):
+            raise ValueError("RaggedBatch items must all be 2-D or all be 3-D")
+        if any(v < 1 for sh in self.shapes for v in sh):
             raise ValueError("RaggedBatch images must be non-empty")
+        sizes = [_numel(sh) for sh in self.shapes]
         if offsets is None:
             offsets, pos = [], 0
-            for h, w in self.shapes:
+            for n in sizes:
                 offsets.append(pos)
-                pos += h * w
+                pos += n
         self.offsets = [int(o) for o in offsets]
-        end = max(o + h * w for o, (h, w) in zip(self.offsets, self.shapes))
+        end = max(o + n for o, n in zip(self.offsets, sizes))
         if min(self.offsets) < 0 or end > data.numel():
             raise ValueError("RaggedBatch offsets run outside the data buffer")
         self._plan = plan
+        self._edt_plan = None
 
     @classmethod
     def from_images(cls, images: Sequence[Tensor]) -> "RaggedBatch":
-        """Pack images of shape (H, W) (or (1, 1, H, W)) into one buffer (a copy)."""
+        """Pack items of shape (H, W) or (D, H, W) (or with leading (1, 1)) into one buffer (a copy)."""
         if len(images) == 0:
             raise ValueError("a RaggedBatch needs at least one image")
         flat, shapes = [], []
         for im in images:
-            if im.dim() == 4 and im.shape[0] == 1 and im.shape[1] == 1:
+            if im.dim() in (4, 5) and im.shape[0] == 1 and im.shape[1] == 1:
                 im = im[0, 0]
-            if im.dim() != 2:
-                raise ValueError("RaggedBatch images must be (H, W) or (1, 1, H, W)")
+            if im.dim() not in (2, 3):
+                raise ValueError("RaggedBatch images must be (H, W) or (1, 1, H, W), volumes (D, H, W) "
+                                 "or (1, 1, D, H, W)")
             shapes.append(tuple(im.shape))
             flat.append(im.reshape(-1))
         return cls(torch.cat(flat).contiguous(), shapes)
@@ -70,12 +80,16 @@ class RaggedBatch:
         return len(self.shapes)
 
     def __getitem__(self, i: int) -> Tensor:
-        h, w = self.shapes[i]
         o = self.offsets[i]
-        return self.data[o:o + h * w].view(h, w)
+        return self.data[o:o + _numel(self.shapes[i])].view(self.shapes[i])
 
     def images(self) -> list[Tensor]:
         return [self[i] for i in range(len(self))]
+
+    @property
+    def ndim(self) -> int:
+        """Spatial dimensions of the items (2 or 3)."""
+        return len(self.shapes[0])
 
     @property
     def device(self):
@@ -87,7 +101,7 @@ class RaggedBatch:
 
     @property
     def numel(self) -> int:
-        return sum(h * w for h, w in self.shapes)
+        return sum(_numel(sh) for sh in self.shapes)
 
     @property
     def plan(self) -> Tensor:
@@ -97,13 +111,21 @@ class RaggedBatch:
                 raise ValueError("ragged operators need a CUDA RaggedBatch")
             lib = _lib.load()
             n = len(self.shapes)
-            nbytes = lib.tm_ragged_plan_size(n)
-            plan = torch.empty(int(nbytes), dtype=torch.uint8, device=self.data.device)
+            dims = list(zip(*self.shapes))
             with torch.cuda.device(self.data.device):
-                _lib.check(lib.tm_ragged_plan(n, _lib.i64_array([h for h, _ in self.shapes]),
-                                              _lib.i64_array([w for _, w in self.shapes]),
-                                              _lib.i64_array(self.offsets), _lib.ptr(plan), nbytes,
-                                              _lib.stream_of(self.data.device)), "tm_ragged_plan")
+                if self.ndim == 2:
+                    nbytes = lib.tm_ragged_plan_size(n)
+                    plan = torch.empty(int(nbytes), dtype=torch.uint8, device=self.data.device)
+                    _lib.check(lib.tm_ragged_plan(n, _lib.i64_array(dims[0]), _lib.i64_array(dims[1]),
+                                                  _lib.i64_array(self.offsets), _lib.ptr(plan), nbytes,
+                                                  _lib.stream_of(self.data.device)), "tm_ragged_plan")
+                else:
+                    nbytes = lib.tm_ragged3d_plan_size(n)
+                    plan = torch.empty(int(nbytes), dtype=torch.uint8, device=self.data.device)
+                    _lib.check(lib.tm_ragged3d_plan(n, _lib.i64_array(dims[0]), _lib.i64_array(dims[1]),
+                                                    _lib.i64_array(dims[2]), _lib.i64_array(self.offsets),
+                                                    _lib.ptr(plan), nbytes, _lib.stream_of(self.data.device)),
+                               "tm_ragged3d_plan")
             self._plan = plan
         return self._plan
 
@@ -119,6 +141,13 @@ class RaggedBatch:
     def map(self, fn: Callable[[Tensor], Tensor]) -> "RaggedBatch":
         """Elementwise op on the whole buffer in one launch (e.g. ``lambda x: x > 0.5``)."""
         return self.with_data(fn(self.data).contiguous())
+
+
+def _numel(shape) -> int:
+    n = 1
+    for v in shape:
+        n *= int(v)
+    return n
 
 
 def _check_batch(batch: RaggedBatch, dtype, what: str):
@@ -144,8 +173,11 @@ def _output(batch: RaggedBatch, output: RaggedBatch | None, dtype) -> RaggedBatc
 
 def _grey(name, batch, size, footprint, structure, mode, cval, origin, output):
     _check_batch(batch, torch.float32, name)
-    struct, fp = _resolve_element(2, size, footprint, structure)
-    o = _normalize_origin(origin, 2)
+    nd = batch.ndim
+    if nd == 3:
+        name = name.replace("tm_ragged_", "tm_ragged3d_")
+    struct, fp = _resolve_element(nd, size, footprint, structure)
+    o = _normalize_origin(origin, nd)
     _validate_origin(o, struct)
     if mode not in _MODE_MAP:
         raise ValueError(f"Unknown mode '{mode}'. Must be one of {list(_MODE_MAP.keys())}.")
@@ -163,13 +195,13 @@ def _grey(name, batch, size, footprint, structure, mode, cval, origin, output):
 
 def grey_erosion(batch: RaggedBatch, size=None, footprint=None, structure=None, mode="reflect", cval=0.0,
                  origin=0, output: RaggedBatch | None = None) -> RaggedBatch:
-    """Per-image grey erosion of a float32 RaggedBatch, one launch for all images."""
+    """Per-item grey erosion of a float32 RaggedBatch, one launch for all items."""
     return _grey("tm_ragged_grey_erosion", batch, size, footprint, structure, mode, cval, origin, output)
 
 
 def grey_dilation(batch: RaggedBatch, size=None, footprint=None, structure=None, mode="reflect", cval=0.0,
                   origin=0, output: RaggedBatch | None = None) -> RaggedBatch:
-    """Per-image grey dilation of a float32 RaggedBatch, one launch for all images."""
+    """Per-item grey dilation of a float32 RaggedBatch, one launch for all items."""
     return _grey("tm_ragged_grey_dilation", batch, size, footprint, structure, mode, cval, origin, output)
 
 
@@ -185,12 +217,15 @@ def grey_closing(batch, size=None, footprint=None, structure=None, mode="reflect
 
 def _binary(name, batch, structure, border_value, origin, output):
     _check_batch(batch, torch.bool, name)
+    nd = batch.ndim
+    if nd == 3:
+        name = name.replace("tm_ragged_", "tm_ragged3d_")
     if structure is None:
-        structure = generate_binary_structure(2, 1)
-    if structure.ndim != 2:
-        raise ValueError(f"structure dimension is not 2, got {structure.ndim}")
+        structure = generate_binary_structure(nd, 1)
+    if structure.ndim != nd:
+        raise ValueError(f"structure dimension is not {nd}, got {structure.ndim}")
     st = (structure != 0).detach().to(device="cpu", dtype=torch.bool).contiguous()
-    o = _normalize_origin(origin, 2)
+    o = _normalize_origin(origin, nd)
     _validate_origin(o, st)
     plan = batch.plan
     out = _output(batch, output, torch.bool)
@@ -208,13 +243,13 @@ def _binary(name, batch, structure, border_value, origin, output):
 
 def binary_erosion(batch: RaggedBatch, structure=None, border_value=False, origin=0,
                    output: RaggedBatch | None = None) -> RaggedBatch:
-    """Per-image binary erosion (one iteration, no mask) of a bool RaggedBatch."""
+    """Per-item binary erosion (one iteration, no mask) of a bool RaggedBatch."""
     return _binary("tm_ragged_binary_erosion", batch, structure, border_value, origin, output)
 
 
 def binary_dilation(batch: RaggedBatch, structure=None, border_value=False, origin=0,
                     output: RaggedBatch | None = None) -> RaggedBatch:
-    """Per-image binary dilation (one iteration, no mask) of a bool RaggedBatch."""
+    """Per-item binary dilation (one iteration, no mask) of a bool RaggedBatch."""
     return _binary("tm_ragged_binary_dilation", batch, structure, border_value, origin, output)
 
 
@@ -226,6 +261,62 @@ def binary_opening(batch, structure=None, border_value=False, origin=0):
 def binary_closing(batch, structure=None, border_value=False, origin=0):
     return binary_erosion(binary_dilation(batch, structure, border_value, origin), structure, border_value,
                           origin)
+
+
+def euclidean_distance_transform(batch: RaggedBatch, return_distances: bool = True,
+                                 return_indices: bool = False):
+    """Exact Euclidean distance transform (unit sampling) of every item of a ragged batch
+    of 2-D images or 3-D volumes, in ONE launch for all items (libtmcore
+    ``tm_ragged_edt``).  Item by item the result equals
+    ``euclidean_distance_transform(item[None, None])`` (reference
+    ``distance_transform.py:72-102``): the distance to the nearest background (zero)
+    voxel, ties to the smallest last-axis coordinate as scipy.ndimage breaks them, and
+    the virtual site (-1, 0, ...) for an item without background.
+
+    Returns the distances as a float32 RaggedBatch with the input's layout, and/or the
+    feature indices as an int32 tensor (ndim, batch.data.numel()) whose plane d holds,
+    at every packed voxel, coordinate d of its nearest background voxel inside its item.
+    """
+    if not isinstance(batch, RaggedBatch):
+        raise TypeError("euclidean_distance_transform expects a RaggedBatch")
+    if not batch.data.is_cuda:
+        raise ValueError("Input tensor must be on CUDA device.")
+    if not return_distances and not return_indices:
+        raise ValueError("At least one of return_distances or return_indices must be True.")
+    if batch.dtype in (torch.bool, torch.uint8):
+        data, in_dtype = batch.data.view(torch.uint8), _lib.TM_U8
+    elif batch.dtype == torch.float32:
+        data, in_dtype = batch.data, _lib.TM_F32
+    else:
+        raise ValueError(f"ragged EDT needs a bool, uint8 or float32 RaggedBatch, got {batch.dtype}")
+    lib = _lib.load()
+    n, nd, total = len(batch), batch.ndim, batch.data.numel()
+    dev = batch.device
+    with torch.cuda.device(dev):
+        stream = _lib.stream_of(dev)
+        plan = batch._edt_plan
+        if plan is None:
+            nbytes = lib.tm_ragged_edt_plan_size(n)
+            plan = torch.empty(int(nbytes), dtype=torch.uint8, device=dev)
+            flat_shapes = [v for sh in batch.shapes for v in sh]
+            _lib.check(lib.tm_ragged_edt_plan(n, nd, _lib.i64_array(flat_shapes), _lib.i64_array(batch.offsets),
+                                              _lib.ptr(plan), nbytes, stream), "tm_ragged_edt_plan")
+            batch._edt_plan = plan
+        lines = [sum(_numel(sh) // sh[a] for sh in batch.shapes) for a in range(nd)]
+        max_line = max(max(sh) for sh in batch.shapes)
+        wbytes = lib.tm_ragged_edt_workspace_size(total, max_line)
+        ws = torch.empty(int(wbytes), dtype=torch.uint8, device=dev)
+        dist = torch.empty(total, dtype=torch.float32, device=dev) if return_distances else None
+        idx = torch.empty((nd, total), dtype=torch.int32, device=dev) if return_indices else None
+        _lib.check(lib.tm_ragged_edt(_lib.ptr(data), in_dtype, _lib.ptr(plan), plan.numel(), n, nd, total, max_line,
+                                     _lib.i64_array(lines), _lib.ptr(dist), _lib.ptr(idx), None, _lib.ptr(ws), wbytes,
+                                     stream), "tm_ragged_edt")
+    out = []
+    if return_distances:
+        out.append(RaggedBatch(dist, batch.shapes, batch.offsets, batch._plan))
+    if return_indices:
+        out.append(idx)
+    return out[0] if len(out) == 1 else tuple(out)
 
 
 def capture(fn: Callable, *args, warmup: int = 1):
