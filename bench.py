@@ -127,6 +127,27 @@ def time_device(fn, sets, steps, warmup, stream):
     return start.elapsed_time(end) / 1e3
 
 
+def graph_time(fn, sets, steps, warmup, stream):
+    """Capture one CUDA graph per set holding fn(set) (one public-operator call), then
+    time replays rotating over the sets: device time without the Python / launch
+    overhead of eager calls.  Returns seconds per call."""
+    import torch
+
+    side = torch.cuda.Stream()
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        for st in sets:
+            fn(st)
+    stream.wait_stream(side)
+    graphs = []
+    for st in sets:
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            fn(st)
+        graphs.append(g)
+    return time_device(lambda g: g.replay(), graphs, steps, warmup, stream) / steps
+
+
 def bench_ours(args, rank, world):
     import torch
 
@@ -230,6 +251,27 @@ def bench_ours(args, rank, world):
     torch.cuda.synchronize()
     t_e2e = e_start.elapsed_time(e_end) / 1e3
     e2e_value = world * nvox * e2e_steps / t_e2e / 1e9
+    # the copy bound of the e2e step: the same outputs read back with plain pinned
+    # device-to-host copies on the same two streams, no EDT
+    def d2h_only(nsteps):
+        for st in e2e_streams:
+            st.wait_stream(stream)
+        for k in range(nsteps):
+            _, dev_d, dev_i, pin_d, pin_i = e2e_bufs[k % 2]
+            with torch.cuda.stream(e2e_streams[k % 2]):
+                pin_d.copy_(dev_d, non_blocking=True)
+                pin_i.copy_(dev_i, non_blocking=True)
+        for st in e2e_streams:
+            stream.wait_stream(st)
+
+    d2h_only(3)
+    torch.cuda.synchronize()
+    e_start.record(stream)
+    d2h_only(e2e_steps)
+    e_end.record(stream)
+    torch.cuda.synchronize()
+    t_d2h = e_start.elapsed_time(e_end) / 1e3
+    d2h_gbps = nvox * 16 * e2e_steps / t_d2h / 1e9
     # the host copies must hold the same result as the device-resident runs
     for _, _, _, pin_d, pin_i in e2e_bufs:
         assert torch.equal(pin_i, sets[0][2].cpu()) and torch.equal(pin_d, sets[0][1].cpu())
@@ -255,7 +297,10 @@ def bench_ours(args, rank, world):
         "e2e": {"value": round(e2e_value, 4), "unit": "Gvoxel/s",
                 "h2d_bytes_per_step": int(nvox), "d2h_bytes_per_step": int(nvox * 16),
                 "how": "public euclidean_distance_transform, pinned host input in and all outputs back every "
-                       "step, two streams so that step k+1's copy-in and EDT overlap step k's read-back"},
+                       "step, two streams so that step k+1's copy-in and EDT overlap step k's read-back",
+                "d2h_copy_GBps": round(d2h_gbps, 1),
+                "copy_bound_Gvoxel_s": round(d2h_gbps / 16, 3),
+                "frac_of_copy_bound": round(e2e_value / world / (d2h_gbps / 16), 4)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
                      "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
                      "peak_kind": peak_kind,
@@ -368,16 +413,50 @@ def secondary(args, dev, stream, hbm_peak):
             _C.cdt(s[0], metric, True, False, distances_out=s[1])
 
         csteps = max(args.steps, 12)
-        t = time_device(cstep, cvols, csteps, max(args.warmup, 3), stream) / csteps
+        t_eager = time_device(cstep, cvols, csteps, max(args.warmup, 3), stream) / csteps
+        t = graph_time(cstep, cvols, csteps, max(args.warmup, 3), stream)
         nv = cvols[0][0].numel()
         out[f"cdt_{metric}_4x128^3"] = {
             "Gvoxel/s": round(nv / t / 1e9, 3), "us_per_call": round(t * 1e6, 1),
+            "us_per_eager_call": round(t_eager * 1e6, 1),
             "frac_of_hbm": round(5.0 * nv / t / 1e9 / hbm, 4), "peak_kind": kind,
-            "volumes": "Bernoulli(0.9) foreground, seeds 0-2 rotating"}
+            "volumes": "Bernoulli(0.9) foreground, seeds 0-2 rotating",
+            "timing": "replays of one CUDA graph per rotating set (one call each)"}
 
+    out.update(edt_shape_lines(args, dev, stream, hbm))
     out.update(ragged_lines(dev, stream, max(args.steps, 10), args.warmup))
+    out.update(ragged_volume_lines(dev, stream, max(args.steps, 10), args.warmup))
     out.update(sinkhorn_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline))
     out.update(pointcloud_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline))
+    return out
+
+
+def edt_shape_lines(args, dev, stream, hbm):
+    """EDT with indices off the headline shape: rows of 200 voxels (2 x 96 x 160 x 200,
+    Bernoulli(0.9): the general-width shell search) and a sparse background (4 x 128^3,
+    Bernoulli(0.999): the separable passes), 17 algorithmic B/voxel."""
+    import torch
+
+    from torchmorph_gb300 import _C
+
+    out = {}
+    for name, shape, p in (("edt_2x96x160x200_p0.9", (2, 1, 96, 160, 200), 0.9),
+                           ("edt_4x128^3_p0.999", EDT_SHAPE, 0.999)):
+        sets = []
+        for k in range(3):
+            x = torch.from_numpy(np.random.default_rng(50 + k).random(shape) < p).to(dev)
+            sets.append((x, torch.empty(shape, dtype=torch.float32, device=dev),
+                         torch.empty((3, *shape), dtype=torch.int32, device=dev)))
+
+        def step(s):
+            _C.edt(s[0], None, True, True, distances_out=s[1], indices_out=s[2])
+
+        steps = max(args.steps, 10)
+        t = graph_time(step, sets, steps, max(args.warmup, 3), stream)
+        nv = int(np.prod(shape))
+        out[name] = {"Gvoxel/s": round(nv / t / 1e9, 3), "us_per_call": round(t * 1e6, 1),
+                     "frac_of_hbm": round(17.0 * nv / t / 1e9 / hbm, 4),
+                     "timing": "replays of one CUDA graph per rotating set (three seeded sets)"}
     return out
 
 
@@ -451,6 +530,53 @@ def ragged_lines(dev, stream, steps, warmup):
                      "scope": "whole pipeline (5 launches incl. the x > 0.5 threshold), 18 "
                               "algorithmic B/pixel"},
         "gpu_launches_per_step": 5}}
+
+
+def ragged_volume_lines(dev, stream, steps, warmup):
+    """Ragged 3-D batch: 64 volumes with D, H, W iid uniform in [16, 96], Bernoulli(0.9)
+    foreground -- exact EDT with indices (one cooperative launch for all volumes) and
+    grey erosion 3x3x3 of U[0, 1) values (one persistent launch), each replayed as a CUDA
+    graph, against per-volume calls of the uniform operators."""
+    import torch
+
+    import torchmorph_gb300 as tm
+    from torchmorph_gb300 import RaggedBatch, ragged
+
+    rng = np.random.default_rng(0)
+    shapes = [tuple(int(v) for v in rng.integers(16, 97, 3)) for _ in range(64)]
+    fg = [rng.random(s) < 0.9 for s in shapes]
+    vals = [rng.random(s, dtype=np.float32) for s in shapes]
+    rb = RaggedBatch.from_images([torch.from_numpy(v).to(dev) for v in fg])
+    rv = RaggedBatch.from_images([torch.from_numpy(v).to(dev) for v in vals])
+    nvox = rb.numel
+    views = [v[None, None] for v in rb.images()]
+    vviews = [v[None, None] for v in rv.images()]
+    # correctness gate against the per-volume operators
+    d, _ = ragged.euclidean_distance_transform(rb, return_indices=True)
+    e = ragged.grey_erosion(rv, size=3)
+    for k in (0, 31, 63):
+        dk, _ = tm.euclidean_distance_transform(views[k], return_indices=True)
+        assert torch.equal(d[k], dk[0, 0])
+        assert torch.equal(e[k], tm.grey_erosion(vviews[k], size=3)[0, 0])
+    g_edt, _ = ragged.capture(lambda b: ragged.euclidean_distance_transform(b, return_indices=True), rb)
+    g_ero, _ = ragged.capture(lambda b: ragged.grey_erosion(b, size=3), rv)
+    t_edt = time_device(lambda _: g_edt.replay(), [None], steps, warmup, stream) / steps
+    t_ero = time_device(lambda _: g_ero.replay(), [None], steps, warmup, stream) / steps
+    t_edt_vol = time_device(lambda _: [tm.euclidean_distance_transform(v, return_indices=True) for v in views],
+                            [None], 3, 1, stream) / 3
+    t_ero_vol = time_device(lambda _: [tm.grey_erosion(v, size=3) for v in vviews], [None], 3, 1, stream) / 3
+    hbm, _, kind = peaks()
+    return {"ragged_64_volumes_edt_erosion3": {
+        "voxels": nvox,
+        "edt_ms_one_launch_graph": round(t_edt * 1e3, 3), "edt_ms_per_volume_calls": round(t_edt_vol * 1e3, 3),
+        "edt_speedup_vs_per_volume": round(t_edt_vol / t_edt, 2),
+        "edt_Gvoxel/s": round(nvox / t_edt / 1e9, 3),
+        "edt_frac_of_hbm": round(17.0 * nvox / t_edt / 1e9 / hbm, 4),
+        "erosion3_ms_one_launch_graph": round(t_ero * 1e3, 3),
+        "erosion3_ms_per_volume_calls": round(t_ero_vol * 1e3, 3),
+        "erosion3_speedup_vs_per_volume": round(t_ero_vol / t_ero, 2),
+        "erosion3_frac_of_hbm": round(8.0 * nvox / t_ero / 1e9 / hbm, 4), "peak_kind": kind,
+        "shapes": "D, H, W iid uniform integers in [16, 96], numpy seed 0"}}
 
 
 def pointcloud_profile_case(dev):
@@ -826,7 +952,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--case", choices=["all", "grey", "sinkhorn", "ragged", "pointcloud", "pointcloud-profile"],
+    ap.add_argument("--case", choices=["all", "grey", "sinkhorn", "ragged", "ragged3d", "edt-shapes", "pointcloud",
+                                       "pointcloud-profile"],
                     default="all",
                     help="only the shared-cost Sinkhorn, ragged-batch or point-cloud lines (one JSON object); "
                          "pointcloud-profile: the small fixed-iteration case used for ncu captures")
@@ -845,6 +972,10 @@ def main():
             print(json.dumps(pointcloud_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline)))
         elif args.case == "pointcloud-profile":
             print(json.dumps(pointcloud_profile_case(dev)))
+        elif args.case == "ragged3d":
+            print(json.dumps(ragged_volume_lines(dev, stream, max(args.steps, 10), args.warmup)))
+        elif args.case == "edt-shapes":
+            print(json.dumps(edt_shape_lines(args, dev, stream, peaks()[0])))
         else:
             print(json.dumps(ragged_lines(dev, stream, max(args.steps, 10), args.warmup)))
         return

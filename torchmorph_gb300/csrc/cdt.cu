@@ -20,11 +20,13 @@
 // where V(k) is the best candidate from every other offset -- a prefix
 // minimum of V(k) - w k, evaluated as a warp-shuffle scan.  The result is
 // therefore bit-identical to the sequential raster pass.
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
 #include "edt_internal.cuh"
 #include "tm_common.cuh"
+#include "tm_tma.cuh"
 
 namespace tmc {
 namespace {
@@ -63,18 +65,13 @@ __device__ __forceinline__ int tau_of_row(uint32_t r, const CdtParams &p) {
     return tau;
 }
 
-__global__ void cdt_count_kernel(int *__restrict__ cnt, CdtParams p, const int *__restrict__ any) {
-    pdl_wait();
-    if (any && !*any) return;  // the shell search finished every item
+__device__ void cdt_count(int *__restrict__ cnt, const CdtParams &p) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < p.rows; r += gridDim.x * blockDim.x)
         atomicAdd(&cnt[tau_of_row((uint32_t)r, p)], 1);
 }
 
-// Exclusive scan of T counters (single CTA); off[T] = total.
-__global__ void cdt_scan_kernel(const int *__restrict__ cnt, int *__restrict__ off, int T,
-                                const int *__restrict__ any) {
-    pdl_wait();
-    if (any && !*any) return;
+// Exclusive scan of T counters (one CTA); off[T] = total.
+__device__ void cdt_scan(const int *__restrict__ cnt, int *__restrict__ off, int T) {
     __shared__ int carry;
     __shared__ int warp_sums[32];
     if (threadIdx.x == 0) carry = 0;
@@ -82,7 +79,7 @@ __global__ void cdt_scan_kernel(const int *__restrict__ cnt, int *__restrict__ o
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int base = 0; base < T; base += blockDim.x) {
         int i = base + threadIdx.x;
-        int v = i < T ? cnt[i] : 0;
+        int v = i < T ? __ldcg(cnt + i) : 0;
         int x = v;
         for (int s = 1; s < 32; s <<= 1) {
             int y = __shfl_up_sync(0xffffffffu, x, s);
@@ -108,25 +105,20 @@ __global__ void cdt_scan_kernel(const int *__restrict__ cnt, int *__restrict__ o
     if (threadIdx.x == 0) off[T] = carry;
 }
 
-__global__ void cdt_scatter_kernel(const int *__restrict__ off, int *__restrict__ cursor,
-                                   int *__restrict__ order, CdtParams p, const int *__restrict__ any) {
-    pdl_wait();
-    if (any && !*any) return;
+__device__ void cdt_scatter(const int *__restrict__ off, int *__restrict__ cursor, int *__restrict__ order,
+                            const CdtParams &p) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < p.rows; r += gridDim.x * blockDim.x) {
         int t = tau_of_row((uint32_t)r, p);
         int pos = atomicAdd(&cursor[t], 1);
-        order[off[t] + pos] = r;
+        order[__ldcg(off + t) + pos] = r;
     }
 }
 
 // todo (optional): 1 for the items the raster passes must compute; the
 // others were finished by the bitmap shell search and are left alone.
 template <typename In>
-__global__ void cdt_init_kernel(const In *__restrict__ in, int32_t *__restrict__ dt, int32_t *__restrict__ ft,
-                                int64_t numel, int64_t numel_item, const int *__restrict__ todo,
-                                const int *__restrict__ any) {
-    pdl_wait();
-    if (any && !*any) return;
+__device__ void cdt_init(const In *__restrict__ in, int32_t *__restrict__ dt, int32_t *__restrict__ ft,
+                         int64_t numel, int64_t numel_item, const int *__restrict__ todo) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < numel;
          i += (int64_t)gridDim.x * blockDim.x) {
         if (todo && !todo[i / numel_item]) continue;
@@ -145,13 +137,8 @@ struct ScanPair {
 __device__ __forceinline__ ScanPair pmin(ScanPair a, ScanPair b) { return b.key < a.key ? b : a; }
 
 template <bool BACKWARD>
-__global__ void __launch_bounds__(kCdtThreads) cdt_pass_kernel(int32_t *__restrict__ dt, int32_t *__restrict__ ft,
-                                                               const int *__restrict__ order,
-                                                               const int *__restrict__ woff, CdtParams p,
-                                                               CdtOffsets offs, const int *__restrict__ todo,
-                                                               const int *__restrict__ any) {
-    pdl_wait();
-    if (any && !*any) return;
+__device__ void cdt_pass(int32_t *dt, int32_t *ft, const int *order, const int *woff, const CdtParams &p,
+                         const CdtOffsets &offs, const int *__restrict__ todo) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
     const int nd = p.ndim;
@@ -162,9 +149,9 @@ __global__ void __launch_bounds__(kCdtThreads) cdt_pass_kernel(int32_t *__restri
         int32_t *F = ft + item * p.numel_item;
         for (int step = 0; step < p.T; step++) {
             const int t = BACKWARD ? p.T - 1 - step : step;
-            const int r0 = woff[t], r1 = woff[t + 1];
+            const int r0 = __ldcg(woff + t), r1 = __ldcg(woff + t + 1);
             for (int ri = r0 + warp; ri < r1; ri += nwarps) {
-                const int row = order[ri];
+                const int row = __ldcg(order + ri);
                 // row coordinates (dims 0..n-2)
                 int rc[TM_MAX_NDIM];
                 uint32_t rem = (uint32_t)row;
@@ -184,7 +171,7 @@ __global__ void __launch_bounds__(kCdtThreads) cdt_pass_kernel(int32_t *__restri
                     ScanPair mine{kKeyInf, 0};
                     if (valid) {
                         const int64_t e = rbase + x;
-                        int best = D[e];
+                        int best = __ldcg(D + e);
                         int64_t bi = -1;
                         if (best != 0) {
                             const bool inner = row_inner && x >= 1 && x <= p.W - 2;
@@ -208,7 +195,7 @@ __global__ void __launch_bounds__(kCdtThreads) cdt_pass_kernel(int32_t *__restri
                                     }
                                     if (!ok) continue;
                                 }
-                                const int tv = D[nb];
+                                const int tv = __ldcg(D + nb);
                                 if (tv < 0) continue;
                                 const int cand = tv + offs.weight[k];
                                 if (best < 0 || cand < best) {
@@ -219,7 +206,7 @@ __global__ void __launch_bounds__(kCdtThreads) cdt_pass_kernel(int32_t *__restri
                         }
                         if (best >= 0) {
                             mine.key = (long long)(best - p.wchain * j) * 4294967296LL + (4294967295LL - j);
-                            mine.feat = bi >= 0 ? F[bi] : F[e];
+                            mine.feat = bi >= 0 ? __ldcg(F + bi) : __ldcg(F + e);
                         }
                     }
                     // inclusive warp min-scan over the chunk, then the carry
@@ -249,19 +236,16 @@ __global__ void __launch_bounds__(kCdtThreads) cdt_pass_kernel(int32_t *__restri
     }
 }
 
-__global__ void cdt_finalize_kernel(const int32_t *__restrict__ dt, const int32_t *__restrict__ ft,
-                                    float *__restrict__ dist, int32_t *__restrict__ indices, int64_t numel,
-                                    int64_t numel_item, int ndim, CdtParams p, float divisor,
-                                    const int *__restrict__ todo, const int *__restrict__ any) {
-    pdl_wait();
-    if (any && !*any) return;
+__device__ void cdt_finalize(const int32_t *dt, const int32_t *ft, float *__restrict__ dist,
+                             int32_t *__restrict__ indices, int64_t numel, int64_t numel_item, int ndim,
+                             const CdtParams &p, float divisor, const int *__restrict__ todo) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < numel;
          i += (int64_t)gridDim.x * blockDim.x) {
         if (todo && !todo[i / numel_item]) continue;
-        const int v = dt[i];
+        const int v = __ldcg(dt + i);
         if (dist) dist[i] = v < 0 ? -1.0f : (float)v / divisor;
         if (indices) {
-            int64_t f = ft[i];
+            int64_t f = __ldcg(ft + i);
             for (int d = 0; d < ndim; d++) {
                 int64_t q = f / p.stride[d];
                 f -= q * p.stride[d];
@@ -271,11 +255,90 @@ __global__ void cdt_finalize_kernel(const int32_t *__restrict__ dt, const int32_
     }
 }
 
+struct CdtControl {
+    unsigned barrier_count;
+    unsigned barrier_gen;
+    int abort;
+    int pad[61];
+};
+static_assert(sizeof(CdtControl) == 256, "control block is 256 bytes");
+
+__device__ bool cdt_barrier(CdtControl *ctl, int *status, long long spin_limit) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = &ctl->barrier_gen;
+        volatile int *abort = &ctl->abort;
+        const unsigned g = *gen;
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(&ctl->barrier_count, 1u) == gridDim.x - 1) {
+            ctl->barrier_count = 0;
+            __threadfence();
+            atomicAdd(&ctl->barrier_gen, 1u);
+        } else {
+            long long polls = 0;
+            while (*gen == g) {
+                if (*abort || ++polls > spin_limit) {
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        if (!ok) {
+            atomicExch(&ctl->abort, 1);
+            if (status) atomicExch(status, TM_DEV_ERR_TIMEOUT);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+struct CdtRasterArgs {
+    const void *in;
+    int32_t *dt, *ft;
+    int *order, *woff, *cnt, *cur;
+    float *dist;
+    int32_t *indices;
+    int64_t numel;
+    float divisor;
+    const int *todo;  // per-item flags of the shell search (NULL: every item)
+    const int *any;   // flag after them: some item is marked
+    CdtControl *ctl;
+    int *status;
+    long long spin_limit;
+};
+
+// The whole raster transform in ONE cooperative launch: wavefront counts,
+// their scan, the row order and the initial costs, then for every item (one
+// CTA per item) the forward and the backward pass, then the outputs -- with
+// bounded grid barriers between the phases.  After the shell search, the
+// launch returns at once unless some item was marked.
+template <typename In>
+__global__ void __launch_bounds__(kCdtThreads, 1) cdt_raster_kernel(CdtRasterArgs a, CdtParams p, CdtOffsets offs) {
+    if (a.any && !*(volatile const int *)a.any) return;  // uniform: every CTA leaves
+    cdt_count(a.cnt, p);
+    if (!cdt_barrier(a.ctl, a.status, a.spin_limit)) return;
+    if (blockIdx.x == 0) cdt_scan(a.cnt, a.woff, p.T);
+    cdt_init(static_cast<const In *>(a.in), a.dt, a.ft, a.numel, p.numel_item, a.todo);
+    if (!cdt_barrier(a.ctl, a.status, a.spin_limit)) return;
+    cdt_scatter(a.woff, a.cur, a.order, p);
+    if (!cdt_barrier(a.ctl, a.status, a.spin_limit)) return;
+    // an item's two passes run on the same CTA: no grid barrier between them
+    cdt_pass<false>(a.dt, a.ft, a.order, a.woff, p, offs, a.todo);
+    cdt_pass<true>(a.dt, a.ft, a.order, a.woff, p, offs, a.todo);
+    if (!cdt_barrier(a.ctl, a.status, a.spin_limit)) return;
+    cdt_finalize(a.dt, a.ft, a.dist, a.indices, a.numel, p.numel_item, p.ndim, p, a.divisor, a.todo);
+}
+
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct CdtPlan {
     int rows, T;
-    size_t dt_off, ft_off, order_off, woff_off, cnt_off, cur_off, total;
+    size_t dt_off, ft_off, order_off, woff_off, cnt_off, cur_off, ctl_off, total;
 };
 
 CdtPlan plan_cdt(const Geometry &g) {
@@ -297,15 +360,16 @@ CdtPlan plan_cdt(const Geometry &g) {
     o += align256((size_t)pl.T * 4);
     pl.cur_off = o;
     o += align256((size_t)pl.T * 4);
+    pl.ctl_off = o;  // the raster launch's barrier block, right after the counters
+    o += sizeof(CdtControl);
     pl.total = o;
     return pl;
 }
 
-// Zero the wavefront counters of the raster passes (before their launches).
+// Zero the wavefront counters and the barrier block of the raster launch
+// (contiguous in the workspace: one memset).
 cudaError_t clear_cdt_counters(unsigned char *ws, const CdtPlan &pl, cudaStream_t stream) {
-    cudaError_t e = cudaMemsetAsync(ws + pl.cnt_off, 0, (size_t)pl.T * 4, stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ws + pl.cur_off, 0, (size_t)pl.T * 4, stream);
-    return e;
+    return cudaMemsetAsync(ws + pl.cnt_off, 0, pl.ctl_off + sizeof(CdtControl) - pl.cnt_off, stream);
 }
 
 template <typename In>
@@ -349,37 +413,40 @@ int run_cdt(const In *in, const Geometry &g, int metric, float *dist, int32_t *i
     }
     p.noff = n;
     p.wchain = metric == TM_CDT_CHAMFER345 ? 3 : 1;
-    int32_t *dt = reinterpret_cast<int32_t *>(ws + pl.dt_off);
-    int32_t *ft = reinterpret_cast<int32_t *>(ws + pl.ft_off);
-    int *order = reinterpret_cast<int *>(ws + pl.order_off);
-    int *woff = reinterpret_cast<int *>(ws + pl.woff_off);
-    int *cnt = reinterpret_cast<int *>(ws + pl.cnt_off);
-    int *cur = reinterpret_cast<int *>(ws + pl.cur_off);
-    const int sms = sm_count();
+    CdtRasterArgs a;
+    a.in = in;
+    a.dt = reinterpret_cast<int32_t *>(ws + pl.dt_off);
+    a.ft = reinterpret_cast<int32_t *>(ws + pl.ft_off);
+    a.order = reinterpret_cast<int *>(ws + pl.order_off);
+    a.woff = reinterpret_cast<int *>(ws + pl.woff_off);
+    a.cnt = reinterpret_cast<int *>(ws + pl.cnt_off);
+    a.cur = reinterpret_cast<int *>(ws + pl.cur_off);
+    a.ctl = reinterpret_cast<CdtControl *>(ws + pl.ctl_off);
+    a.dist = dist;
+    a.indices = indices;
+    a.numel = g.numel;
+    a.divisor = metric == TM_CDT_CHAMFER345 ? 3.0f : 1.0f;
+    a.todo = todo;
+    a.any = todo ? todo + g.batch : nullptr;  // the flag after the per-item flags
+    int st = device_status_word(&a.status);
+    if (st != TM_OK) return st;
+    a.spin_limit = grid_wait_budget();
     if (!counters_cleared) TM_CHECK_CUDA(clear_cdt_counters(ws, pl, stream));
-    // after the shell search (todo given): every kernel is launched as a
-    // programmatic dependent of the previous one and returns at once when no
-    // item was marked (the flag after the per-item flags)
-    const int *any = todo ? todo + g.batch : nullptr;
-    auto go = [&](auto kernel, unsigned grid, unsigned block, auto... args) -> cudaError_t {
-        if (todo) return launch_pdl(kernel, dim3(grid), dim3(block), 0, stream, args...);
-        kernel<<<grid, block, 0, stream>>>(args...);
-        return cudaGetLastError();
-    };
-    unsigned rb = (unsigned)std::min<int64_t>(ceil_div(pl.rows, 256), sms * 4);
-    TM_CHECK_CUDA(go(cdt_count_kernel, rb, 256, cnt, p, any));
-    TM_CHECK_CUDA(go(cdt_scan_kernel, 1, 1024, (const int *)cnt, woff, pl.T, any));
-    TM_CHECK_CUDA(go(cdt_scatter_kernel, rb, 256, (const int *)woff, cur, order, p, any));
-    unsigned eb = (unsigned)std::min<int64_t>(ceil_div(g.numel, 256), (int64_t)sms * 16);
-    TM_CHECK_CUDA(go(cdt_init_kernel<In>, eb, 256, in, dt, ft, g.numel, g.numel_item, todo, any));
-    unsigned ib = (unsigned)std::min<int64_t>(g.batch, (int64_t)1 << 20);
-    TM_CHECK_CUDA(go(cdt_pass_kernel<false>, ib, kCdtThreads, dt, ft, (const int *)order, (const int *)woff, p, local,
-                     todo, any));
-    TM_CHECK_CUDA(go(cdt_pass_kernel<true>, ib, kCdtThreads, dt, ft, (const int *)order, (const int *)woff, p, local,
-                     todo, any));
-    TM_CHECK_CUDA(go(cdt_finalize_kernel, eb, 256, (const int32_t *)dt, (const int32_t *)ft, dist, indices, g.numel,
-                     g.numel_item, nd, p, metric == TM_CDT_CHAMFER345 ? 3.0f : 1.0f, todo, any));
-    TM_LAUNCH_CHECK("cdt_finalize_kernel");
+    static thread_local int cached_dev = -1, cached_per_sm = 0;
+    int dev = 0;
+    TM_CHECK_CUDA(cudaGetDevice(&dev));
+    if (cached_dev != dev) {
+        TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_per_sm, cdt_raster_kernel<In>,
+                                                                    kCdtThreads, 0));
+        cached_dev = dev;
+    }
+    if (cached_per_sm < 1) return fail(TM_ERR_UNSUPPORTED, "raster chamfer kernel does not fit on an SM");
+    const int64_t blocks = std::min<int64_t>((int64_t)cached_per_sm * sm_count(),
+                                             std::max<int64_t>(g.batch, ceil_div(g.numel, kCdtThreads)));
+    void *params[] = {&a, &p, &local};
+    TM_CHECK_CUDA(cudaLaunchCooperativeKernel((const void *)cdt_raster_kernel<In>, dim3((unsigned)blocks),
+                                              dim3(kCdtThreads), params, 0, stream));
+    TM_LAUNCH_CHECK("cdt_raster_kernel");
     return TM_OK;
 }
 

@@ -689,9 +689,13 @@ constexpr uint16_t kNoF01 = 0xFFFF;
 
 struct C12Smem {
     int L1, L2, rowp;  // rowp: padded pass-2 row length
-    size_t tab, f0s, p1, stk, flag, total;
+    size_t tab, f0s, p1, stk, flag, rflag, total;
 };
 
+// The envelope stacks of the fallbacks (sparse backgrounds) live in one
+// shared region, used first by the pass-1 columns (L1 entries per column,
+// interleaved over the 128 columns of a group) and then by the pass-2 rows
+// (W entries per row, interleaved over the L1 rows).
 __host__ __device__ inline C12Smem c12_smem(int L1, int L2) {
     C12Smem m;
     m.L1 = L1;
@@ -705,9 +709,12 @@ __host__ __device__ inline C12Smem c12_smem(int L1, int L2) {
     m.p1 = off;
     off += ((size_t)L1 * m.rowp * 2 + 15) / 16 * 16;
     m.stk = off;
-    off += ((size_t)kC12Warps * L2 * 2 + 15) / 16 * 16;
+    const size_t col_stack = (size_t)L1 * kC12Cols * 2, row_stack = (size_t)L1 * L2 * 2;
+    off += ((col_stack > row_stack ? col_stack : row_stack) + 15) / 16 * 16;
     m.flag = off;
     off += (size_t)kC12Cols * 4;
+    m.rflag = off;
+    off += ((size_t)L1 * 4 + 15) / 16 * 16;
     m.total = off;
     return m;
 }
@@ -723,8 +730,9 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
     float *tab = reinterpret_cast<float *>(smem_raw + sm.tab);
     uint8_t *f0s = smem_raw + sm.f0s + kC12PadTop * W;  // row y at f0s + y * W, y in -4 .. L1+11
     uint16_t *p1 = reinterpret_cast<uint16_t *>(smem_raw + sm.p1);  // row y at p1 + y * rowp + kC12PadX
-    int16_t *stk_all = reinterpret_cast<int16_t *>(smem_raw + sm.stk);
+    int16_t *stk = reinterpret_cast<int16_t *>(smem_raw + sm.stk);
     int *colflag = reinterpret_cast<int *>(smem_raw + sm.flag);
+    int *rowflag = reinterpret_cast<int *>(smem_raw + sm.rflag);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t item = blk / L0;
     const int z = (int)(blk - item * L0);
@@ -752,7 +760,6 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
     __syncthreads();
 
     // ---- pass 1: columns along axis 1, 2 threads per column
-    const int64_t nlines1 = p.batch * (int64_t)L0 * W;
     for (int xg = 0; xg < W; xg += kC12Cols) {
         const int xl = tid % kC12Cols, seg = tid / kC12Cols;
         const int x = xg + xl;
@@ -794,8 +801,9 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
         if (fallback) colflag[xl] = 1;
         __syncthreads();
         if (seg == 0 && x < W && colflag[xl]) {
-            // exact lower envelope of the column, stack in the workspace
-            const int64_t lid = (item * L0 + z) * (int64_t)W + x;
+            // exact lower envelope of the column, stack in shared memory
+            // (entry k of column xl at stk[k * kC12Cols + xl])
+            int16_t *cst = stk + xl;
             int k = -1, top = 0, sec = 0;
             int32_t Gtop = 0, Gsec = 0;
             for (int q = 0; q < L1; q++) {
@@ -810,12 +818,12 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
                     top = sec;
                     Gtop = Gsec;
                     if (k >= 1) {
-                        sec = gstack[(int64_t)(k - 1) * nlines1 + lid];
+                        sec = cst[(k - 1) * kC12Cols];
                         Gsec = (int32_t)G1(sec) + sec * sec;
                     }
                 }
                 k++;
-                gstack[(int64_t)k * nlines1 + lid] = (int16_t)q;
+                cst[k * kC12Cols] = (int16_t)q;
                 sec = top;
                 Gsec = Gtop;
                 top = q;
@@ -824,10 +832,10 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
             if (k < 0) {
                 for (int q = 0; q < L1; q++) p1[q * rowp + kC12PadX + x] = kNoF01;
             } else {
-                int j = 0, cur = gstack[lid], nxt = 0;
+                int j = 0, cur = cst[0], nxt = 0;
                 uint32_t gcur = G1(cur), gnxt = 0;
                 if (k >= 1) {
-                    nxt = gstack[nlines1 + lid];
+                    nxt = cst[kC12Cols];
                     gnxt = G1(nxt);
                 }
                 for (int q = 0; q < L1; q++) {
@@ -840,7 +848,7 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
                         gcur = gnxt;
                         fc = fn;
                         if (j < k) {
-                            nxt = gstack[(int64_t)(j + 1) * nlines1 + lid];
+                            nxt = cst[(j + 1) * kC12Cols];
                             gnxt = G1(nxt);
                         }
                     }
@@ -853,7 +861,8 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
 
     // ---- pass 2: rows along axis 2, one warp per row, 4 voxels per lane
     const int64_t numel = p.numel;
-    int16_t *st = stk_all + warp * W;
+    for (int i = tid; i < L1; i += kC12Threads) rowflag[i] = 0;
+    __syncthreads();
     for (int y = warp; y < L1; y += kC12Warps) {
         const uint16_t *row = p1 + y * rowp + kC12PadX;
         auto dec = [&](uint32_t f) -> uint32_t {
@@ -918,43 +927,69 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
                 *reinterpret_cast<int4 *>(indices + 2 * numel + gi) = make_int4(i2[0], i2[1], i2[2], i2[3]);
             }
         }
-        if (!__any_sync(0xffffffffu, fallback)) continue;
-        // exact lower envelope of the row: lane 0 builds it, every lane searches it
-        int ktop = 0;
-        if (lane == 0) {
-            int k = -1, top = 0, sec = 0;
-            int32_t Gtop = 0, Gsec = 0;
-            for (int q = 0; q < W; q++) {
-                const uint32_t gq = G2(q);
-                if (gq >= kBig) continue;
-                const int32_t Gq = (int32_t)gq + q * q;
-                while (k >= 1) {
-                    const long long lhs = (long long)(Gq - Gtop) * (top - sec);
-                    const long long rhs = (long long)(Gtop - Gsec) * (q - top);
-                    if (lhs > rhs) break;
-                    k--;
-                    top = sec;
-                    Gtop = Gsec;
-                    if (k >= 1) {
-                        sec = st[k - 1];
-                        Gsec = (int32_t)G2(sec) + sec * sec;
-                    }
+        if (__any_sync(0xffffffffu, fallback) && lane == 0) rowflag[y] = 1;
+    }
+    __syncthreads();
+    // rows the windows could not finish (sparse backgrounds): every thread builds
+    // the exact lower envelope of one row (entry k of row y at stk[k * L1 + y]);
+    // rowflag becomes 2 + the index of the top entry
+    if (tid < L1 && rowflag[tid]) {
+        const int y = tid;
+        const uint16_t *row = p1 + y * rowp + kC12PadX;
+        auto G2 = [&](int pp) -> uint32_t {
+            const uint32_t f = row[pp];
+            if (f == kNoF01) return kBig;
+            const int f0 = (int)(f & 255u), f1 = (int)(f >> 8);
+            return (uint32_t)((z - f0) * (z - f0) + (y - f1) * (y - f1));
+        };
+        int16_t *rst = stk + y;
+        int k = -1, top = 0, sec = 0;
+        int32_t Gtop = 0, Gsec = 0;
+        for (int q = 0; q < W; q++) {
+            const uint32_t gq = G2(q);
+            if (gq >= kBig) continue;
+            const int32_t Gq = (int32_t)gq + q * q;
+            while (k >= 1) {
+                const long long lhs = (long long)(Gq - Gtop) * (top - sec);
+                const long long rhs = (long long)(Gtop - Gsec) * (q - top);
+                if (lhs > rhs) break;
+                k--;
+                top = sec;
+                Gtop = Gsec;
+                if (k >= 1) {
+                    sec = rst[(k - 1) * L1];
+                    Gsec = (int32_t)G2(sec) + sec * sec;
                 }
-                st[++k] = (int16_t)q;
-                sec = top;
-                Gsec = Gtop;
-                top = q;
-                Gtop = Gq;
             }
-            ktop = k;
+            k++;
+            rst[k * L1] = (int16_t)q;
+            sec = top;
+            Gsec = Gtop;
+            top = q;
+            Gtop = Gq;
         }
-        ktop = __shfl_sync(0xffffffffu, ktop, 0);
-        __syncwarp();
+        rowflag[y] = 2 + k;  // flagged rows have a site: k >= 0
+    }
+    __syncthreads();
+    // outputs of those rows: one warp per row, every lane searches the envelope
+    for (int y = warp; y < L1; y += kC12Warps) {
+        const int flag = rowflag[y];
+        if (flag < 2) continue;
+        const int ktop = flag - 2;
+        const uint16_t *row = p1 + y * rowp + kC12PadX;
+        auto G2 = [&](int pp) -> uint32_t {
+            const uint32_t f = row[pp];
+            if (f == kNoF01) return kBig;
+            const int f0 = (int)(f & 255u), f1 = (int)(f >> 8);
+            return (uint32_t)((z - f0) * (z - f0) + (y - f1) * (y - f1));
+        };
+        const int16_t *rst = stk + y;
+        const int64_t base = plane + (int64_t)y * W;
         for (int q = lane; q < W; q += 32) {
             int lo = 0, hi = ktop;
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
-                const int a = st[mid - 1], b = st[mid];
+                const int a = rst[(mid - 1) * L1], b = rst[mid * L1];
                 const uint32_t fa = (uint32_t)((q - a) * (q - a)) + G2(a);
                 const uint32_t fb = (uint32_t)((q - b) * (q - b)) + G2(b);
                 if (fb < fa)
@@ -962,7 +997,7 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
                 else
                     hi = mid - 1;
             }
-            const int bp = st[lo];
+            const int bp = rst[lo * L1];
             const uint32_t best = (uint32_t)((q - bp) * (q - bp)) + G2(bp);
             const uint32_t f = row[bp];
             const int64_t gi = base + q;
@@ -974,7 +1009,6 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
                 indices[2 * numel + gi] = bp;
             }
         }
-        __syncwarp();
     }
 }
 
