@@ -403,8 +403,24 @@ def secondary(args, dev, stream, hbm_peak):
     out["binary_dilation_3x3_8x256x256"] = {"Gvoxel/s": round(xb.numel() / (t / steps) / 1e9, 3),
                                             "us_per_call": round(t / steps * 1e6, 2)}
 
-    # chamfer distances (distances only) on the EDT volumes: three independently
-    # seeded volumes rotating, preallocated outputs, 1 B in + 4 B out per voxel
+    hbm = peaks()[0]
+    out.update(cdt_lines(args, dev, stream))
+    out.update(edt_shape_lines(args, dev, stream, hbm))
+    out.update(ragged_lines(dev, stream, max(args.steps, 10), args.warmup))
+    out.update(ragged_volume_lines(dev, stream, max(args.steps, 10), args.warmup))
+    out.update(sinkhorn_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline))
+    out.update(pointcloud_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline))
+    return out
+
+
+def cdt_lines(args, dev, stream):
+    """Chamfer distances (distances only) on the EDT volumes: three independently seeded
+    volumes rotating, preallocated outputs, 1 B in + 4 B out per voxel."""
+    import torch
+
+    from torchmorph_gb300 import _C
+
+    out = {}
     hbm, _, kind = peaks()
     cvols = [(torch.from_numpy(edt_volumes(k)).to(dev), torch.empty(EDT_SHAPE, dtype=torch.float32, device=dev))
              for k in range(3)]
@@ -423,11 +439,6 @@ def secondary(args, dev, stream, hbm_peak):
             "volumes": "Bernoulli(0.9) foreground, seeds 0-2 rotating",
             "timing": "replays of one CUDA graph per rotating set (one call each)"}
 
-    out.update(edt_shape_lines(args, dev, stream, hbm))
-    out.update(ragged_lines(dev, stream, max(args.steps, 10), args.warmup))
-    out.update(ragged_volume_lines(dev, stream, max(args.steps, 10), args.warmup))
-    out.update(sinkhorn_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline))
-    out.update(pointcloud_lines(dev, stream, cpu_baseline=not args.no_cpu_baseline))
     return out
 
 
@@ -952,7 +963,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--case", choices=["all", "grey", "sinkhorn", "ragged", "ragged3d", "edt-shapes", "pointcloud",
+    ap.add_argument("--case", choices=["all", "grey", "cdt", "sinkhorn", "ragged", "ragged3d", "edt-shapes", "pointcloud",
                                        "pointcloud-profile"],
                     default="all",
                     help="only the shared-cost Sinkhorn, ragged-batch or point-cloud lines (one JSON object); "
@@ -974,6 +985,8 @@ def main():
             print(json.dumps(pointcloud_profile_case(dev)))
         elif args.case == "ragged3d":
             print(json.dumps(ragged_volume_lines(dev, stream, max(args.steps, 10), args.warmup)))
+        elif args.case == "cdt":
+            print(json.dumps(cdt_lines(args, dev, stream)))
         elif args.case == "edt-shapes":
             print(json.dumps(edt_shape_lines(args, dev, stream, peaks()[0])))
         else:

@@ -106,8 +106,9 @@ void tm_set_grid_wait_budget(int64_t polls);
  *         per SM (else two);                 class: 8 min(7, log2 n) + min(7, log2 d - 6)
  *   op 2  3-D exact EDT: 0 bitmap shell search first, 1 separable passes only;
  *                                             class: log2(voxels)
- *   op 3  3-D chamfer distances: 0 bitmap shell search first, 1 raster passes
- *         only;                               class: log2(voxels)
+ *   op 3  3-D chamfer distances: 0 bitmap shell search first (persistent warps
+ *         on a queue of 8-row units), 1 raster passes only, 2 shell search with
+ *         one CTA per 32-row block;           class: log2(voxels)
  * tm_tune_class(op, a, b): the class of a call (a = voxels, or a = n pairs and
  * b = d points for op 1). */
 int tm_tune_variants(int op);
@@ -168,6 +169,27 @@ int tm_grey_gradient(const float *in, float *out, int64_t batch, int ndim, const
                      const float *structure, const uint8_t *footprint, const int64_t *sshape,
                      const int64_t *origin, int mode, float cval, tm_stream_t stream);
 int tm_grey_laplace(const float *in, float *out, int64_t batch, int ndim, const int64_t *shape,
+                    const float *structure, const uint8_t *footprint, const int64_t *sshape,
+                    const int64_t *origin, int mode, float cval, tm_stream_t stream);
+
+/* One-pass grey opening / closing and white / black top-hats of 1-D or 2-D
+ * items with flat rectangular elements (footprint all active, one structure
+ * value, up to 33 per axis): the first operator, the intermediate image's
+ * border handling and the second operator (and the top-hat difference) in
+ * one kernel per 32 x 128 output tile, bit-identical to the reference's
+ * composition (torchmorph/morphology/grey.py:162-197, 224-265).  Arguments
+ * as for tm_grey_dilation; TM_ERR_UNSUPPORTED outside these limits, where
+ * the caller composes the operators. */
+int tm_grey_opening(const float *in, float *out, int64_t batch, int ndim, const int64_t *shape,
+                    const float *structure, const uint8_t *footprint, const int64_t *sshape,
+                    const int64_t *origin, int mode, float cval, tm_stream_t stream);
+int tm_grey_closing(const float *in, float *out, int64_t batch, int ndim, const int64_t *shape,
+                    const float *structure, const uint8_t *footprint, const int64_t *sshape,
+                    const int64_t *origin, int mode, float cval, tm_stream_t stream);
+int tm_white_tophat(const float *in, float *out, int64_t batch, int ndim, const int64_t *shape,
+                    const float *structure, const uint8_t *footprint, const int64_t *sshape,
+                    const int64_t *origin, int mode, float cval, tm_stream_t stream);
+int tm_black_tophat(const float *in, float *out, int64_t batch, int ndim, const int64_t *shape,
                     const float *structure, const uint8_t *footprint, const int64_t *sshape,
                     const int64_t *origin, int mode, float cval, tm_stream_t stream);
 
@@ -364,11 +386,16 @@ int tm_sinkhorn_logiter(const float *log_a, const float *log_b, const float *M,
  * cost[b] = <P_b, C> and row_err[b] (fp64 [n], for the returned potentials,
  * P never materialised) and iterations (int32 scalar); cost, row_err and
  * iterations may be NULL.  a, b: fp32 (n, d) rows summing to 1; C: fp32
- * (d, d).  workspace: 256-byte aligned, tm_sinkhorn_f32_workspace_size bytes.
+ * (d, d), or NULL for the cost |i - j| of d points on a line (the
+ * reference's default build_cost_matrix((d,)) for p = 1 or 2), which is then
+ * computed where it is used -- no (d, d) matrix is stored or read; the same
+ * NULL is accepted by tm_sinkhorn_plan and tm_sinkhorn_cost_grad.
+ * workspace: 256-byte aligned, tm_sinkhorn_f32_workspace_size bytes
+ * (line_cost = 1 when C is NULL).
  * No counterpart in the reference's extension (it exposes the iterations
  * only). */
 size_t tm_sinkhorn_f32_workspace_size(int64_t n, int64_t d, int log_space, int64_t max_iter,
-                                      int64_t check_every);
+                                      int64_t check_every, int line_cost);
 int tm_sinkhorn_f32_solve(const float *a, const float *b, const float *C, int64_t n, int64_t d,
                           double epsilon, int log_space, int64_t max_iter, double threshold,
                           int64_t check_every, float *log_u, float *log_v, double *cost,

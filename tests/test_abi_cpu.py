@@ -98,9 +98,12 @@ def test_rejects_bad_geometry_without_touching_the_device():
 def test_workspace_sizes():
     lib = _lib.load()
     assert lib.tm_sinkhorn_iter_workspace_size() == 256
-    w = lib.tm_sinkhorn_f32_workspace_size(3, 300, 0, 100, 10)
+    w = lib.tm_sinkhorn_f32_workspace_size(3, 300, 0, 100, 10, 0)
     assert w >= 2 * 300 * 300 * 4 + 2 * 3 * 300 * 4
-    assert lib.tm_sinkhorn_f32_workspace_size(3, 300, 1, 100, 10) < w  # the log form keeps no K
+    assert lib.tm_sinkhorn_f32_workspace_size(3, 300, 1, 100, 10, 0) < w  # the log form keeps no K
+    # the line cost |i - j| is computed in the kernels: no (d, d) matrix in the workspace
+    assert lib.tm_sinkhorn_f32_workspace_size(3, 300, 0, 100, 10, 1) < 300 * 300 * 4
+    assert lib.tm_sinkhorn_f32_workspace_size(3, 300, 1, 100, 10, 1) < 300 * 300 * 4
     assert lib.tm_edt_workspace_size(1, 1, _lib.i64_array([10]), None) == 0
     n2 = lib.tm_edt_workspace_size(4, 3, _lib.i64_array([8, 8, 8]), None)
     assert n2 >= 4 * 512 * (2 + 4)

@@ -17,7 +17,7 @@ def _restore_table():
 
 def test_variant_table_and_validation():
     lib = _lib.load()
-    assert [autotune.variants(op) for op in ("grey_flat2d", "sinkhorn_f32", "edt_3d", "cdt_3d")] == [4, 4, 2, 2]
+    assert [autotune.variants(op) for op in ("grey_flat2d", "sinkhorn_f32", "edt_3d", "cdt_3d")] == [4, 4, 2, 3]
     assert autotune.get_variant("edt_3d", 23) == -1
     autotune.set_variant("edt_3d", 23, 1)
     assert autotune.get_variant("edt_3d", 23) == 1
@@ -43,7 +43,7 @@ def test_cache_round_trip_and_apply(tmp_path):
     assert autotune.load_cache(path) == {"version": 1, "devices": {}}
     data = autotune.load_cache(path)
     data["devices"]["GPU A"] = {"edt_3d": {"23": 1}, "sinkhorn_f32": {"63": 3, "2": 9},
-                                "unknown_op": {"1": 0}, "cdt_3d": {"x": 1}}
+                                "unknown_op": {"1": 0}, "cdt_3d": {"x": 1, "4": 3}}
     autotune.save_cache(data, path)
     with open(path) as f:
         assert json.load(f)["devices"]["GPU A"]["edt_3d"] == {"23": 1}

@@ -237,11 +237,15 @@ def test_edt_shell_patch_and_overflow(cuda, seed):
 
 
 @pytest.mark.parametrize("metric", ["chessboard", "taxicab", "chamfer345"])
-def test_chamfer_far_voxels(cuda, metric):
+@pytest.mark.parametrize("variant", [-1, 2])
+def test_chamfer_far_voxels(cuda, metric, variant):
     """Voxels whose nearest background lies beyond the radius-4 shell's classes are
     searched on the bitmap (the 9^3 block's centre; taxicab and 3-4-5 voxels at
     Bernoulli(0.9)); a unit with many of them (the ball, the all-foreground item) sends
-    its item to the raster passes.  Fast path == raster passes == oracle."""
+    its item to the raster passes.  Fast path == raster passes == oracle, for the
+    work-queue shell kernel (built-in) and the block kernel (autotuner variant 2)."""
+    from torchmorph_gb300 import autotune
+
     r = rng(7)
     shape = (4, 1, 40, 50, 128)
     x = r.random(shape) < 0.9
@@ -250,7 +254,12 @@ def test_chamfer_far_voxels(cuda, metric):
     x[1, 0] |= (zz - 20) ** 2 + (yy - 25) ** 2 + (xx - 64) ** 2 <= 144
     x[2] = True
     t = torch.from_numpy(x).cuda()
-    d_fast, _ = _C.cdt(t, metric, True, False)
+    cls = autotune.work_class("cdt_3d", t.numel())
+    autotune.set_variant("cdt_3d", cls, variant)
+    try:
+        d_fast, _ = _C.cdt(t, metric, True, False)
+    finally:
+        autotune.set_variant("cdt_3d", cls, -1)
     d_ref, _ = _C.cdt(t, metric, True, True)
     np.testing.assert_array_equal(d_fast.cpu().numpy(), d_ref.cpu().numpy())
     d_o, _ = oracle.cdt(x, metric)

@@ -89,13 +89,19 @@ def _check_edt(items, dist_rb, idx):
         off += n
 
 
-@pytest.mark.parametrize("nd", [2, 3])
+@pytest.mark.parametrize("nd,planes", [(2, False), (3, False), (3, True)])
 @pytest.mark.parametrize("p", [0.9, 0.995])
-def test_ragged_edt_vs_oracle(cuda, nd, p):
-    r = rng(10 * nd + int(p * 1000))
+def test_ragged_edt_vs_oracle(cuda, nd, planes, p):
+    """planes: every axis of every 3-D item is at most 180 voxels, so the batch takes the
+    fused plane passes (pass 0 per column, passes 1 + 2 per plane on chip); otherwise the
+    per-line envelope passes (a 300-voxel axis)."""
+    r = rng(10 * nd + int(p * 1000) + planes)
     if nd == 2:
         shapes = [(int(r.integers(1, 200)), int(r.integers(1, 300))) for _ in range(12)]
         shapes += [(1, 1), (1, 77), (300, 2), (40, 41), (33, 700)]  # 700: stack in the workspace
+    elif planes:
+        shapes = [(int(r.integers(1, 50)), int(r.integers(1, 70)), int(r.integers(1, 130))) for _ in range(10)]
+        shapes += [(1, 1, 1), (1, 1, 180), (180, 2, 3), (3, 180, 5), (17, 33, 45), (20, 20, 20), (6, 7, 8)]
     else:
         shapes = [(int(r.integers(1, 30)), int(r.integers(1, 40)), int(r.integers(1, 60))) for _ in range(8)]
         shapes += [(1, 1, 1), (2, 3, 300), (20, 20, 20), (6, 7, 8)]

@@ -223,3 +223,54 @@ def test_grid_barrier_wait_budget_times_out_and_returns(cuda):
     torch.cuda.synchronize()
     assert lib.tm_device_error(1) == 0
     assert torch.equal(again[0], ref[0]) and torch.equal(again[1], ref[1])
+
+
+@pytest.mark.parametrize("log_space", [False, True])
+@pytest.mark.parametrize("n,d", [(3, 96), (20, 301), (5, 1500)])
+def test_line_cost_equals_the_explicit_matrix(cuda, log_space, n, d):
+    """With no cost matrix the FP32 solver computes |i - j| in its kernels: potentials,
+    transport cost, residual, plan and histogram gradients equal, bit for bit, those of a
+    solve given build_cost_matrix((d,)) -- and no (d, d) matrix is allocated."""
+    a, b, _ = _ot_problem(n, d, seed=d)
+    A, B = _f32(a), _f32(b)
+    C = build_cost_matrix((d,), p=2, device="cuda")
+    assert torch.equal(C, build_cost_matrix((d,), p=1, device="cuda"))
+    eps, its = 0.1, 60
+    ref = _C.sinkhorn_f32_solve(A, B, C, eps, its, 0.0, log_space)
+    got = _C.sinkhorn_f32_solve(A, B, None, eps, its, 0.0, log_space)
+    for r, g in zip(ref[:4], got[:4]):
+        assert torch.equal(r, g)
+    assert torch.equal(_C.sinkhorn_plan(ref[0], ref[1], C, eps), _C.sinkhorn_plan(got[0], got[1], None, eps))
+
+    def module_run(cost):
+        x, y = A.clone().requires_grad_(True), B.clone().requires_grad_(True)
+        solver = SinkhornSolver(epsilon=eps, max_iter=its, log_space=log_space, tensor_cores=False)
+        dist = solver(x, y, cost)
+        dist.sum().backward()
+        return dist.detach(), x.grad, y.grad, solver.plan(A, B, cost)
+
+    for r, g in zip(module_run(C), module_run(None)):
+        assert torch.equal(r, g)
+    if d >= 1024:  # where one (d, d) matrix outweighs the (n, d) buffers
+        torch.cuda.synchronize()
+        torch.cuda.reset_peak_memory_stats()
+        base = torch.cuda.memory_allocated()
+        SinkhornSolver(epsilon=eps, max_iter=its, log_space=log_space, tensor_cores=False)(A, B)
+        torch.cuda.synchronize()
+        assert torch.cuda.max_memory_allocated() - base < d * d * 4 // 2
+
+
+def test_line_cost_only_where_it_is_exact(cuda):
+    from torchmorph_gb300.optimal_transport import _line_cost_ok
+
+    A = torch.ones((2, 2896), device="cuda")
+    assert _line_cost_ok(A, 2, False) and _line_cost_ok(A, 1, False)
+    assert not _line_cost_ok(torch.ones((2, 2897), device="cuda"), 2, False)
+    assert _line_cost_ok(torch.ones((2, 2897), device="cuda"), 1, False)
+    assert not _line_cost_ok(A, 3, False)
+    assert not _line_cost_ok(A.double(), 2, False)
+    assert not _line_cost_ok(torch.ones((64, 512), device="cuda"), 2, None)  # tensor-core sizes
+    # the matrix-product evaluation of the distances is exact up to d = 2896
+    C = build_cost_matrix((2896,), p=2, device="cuda")
+    i = torch.arange(2896, device="cuda", dtype=torch.float32)
+    assert torch.equal(C, (i[:, None] - i[None, :]).abs())

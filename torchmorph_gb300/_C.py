@@ -86,20 +86,26 @@ def grey_dilation_cuda(input, structure, footprint, origin, mode, cval):
 _TM_ERR_UNSUPPORTED = 2
 
 
+_COMPOSITES = {"gradient": "tm_grey_gradient", "laplace": "tm_grey_laplace", "opening": "tm_grey_opening",
+               "closing": "tm_grey_closing", "white_tophat": "tm_white_tophat",
+               "black_tophat": "tm_black_tophat"}
+
+
 def grey_composite(kind, input, structure, footprint, origin, mode, cval):
-    """One-pass morphological gradient ("gradient") or laplace ("laplace") of a 2-D batch
-    (tm_grey_gradient / tm_grey_laplace); None when the element is outside the one-pass
-    kernel's limits, so that the caller composes the two operators instead."""
+    """One-pass composite of a batch (tm_grey_gradient, tm_grey_laplace: 2-D items;
+    tm_grey_opening / closing, tm_white_tophat / black_tophat: 1-D or 2-D items with flat
+    boxes up to 33 per axis); None when the element is outside the one-pass kernel's
+    limits, so that the caller composes the operators instead."""
     _require(input.is_cuda and input.is_contiguous() and input.dtype == torch.float32,
              "input must be a contiguous float32 CUDA tensor")
     nd = structure.dim()
     _require(len(origin) == nd and input.dim() == nd + 2, "structure/origin/input dimensions disagree")
-    if nd != 2:
+    name = _COMPOSITES[kind]
+    if nd != 2 and not (nd == 1 and kind not in ("gradient", "laplace")):
         return None
     use_fp = footprint.numel() != 0
     batch, shape = _batch_shape(input)
     out = torch.empty_like(input)
-    name = "tm_grey_gradient" if kind == "gradient" else "tm_grey_laplace"
     lib = _lib.load()
     with torch.cuda.device(input.device):
         st = getattr(lib, name)(
@@ -381,7 +387,8 @@ def sinkhorn_f32_solve(a, b, cost_matrix, epsilon, max_iter, threshold=0.0, log_
                        check_every=10):
     """A whole FP32 Sinkhorn solve on the device (libtmcore tm_sinkhorn_f32_solve).
 
-    a, b: (n, d) float32 CUDA histograms (rows summing to 1); cost_matrix (d, d).
+    a, b: (n, d) float32 CUDA histograms (rows summing to 1); cost_matrix (d, d), or
+    None for the cost |i - j| of d points on a line, computed where it is used.
     Runs max_iter iterations in one launch, or, with threshold > 0, stops on
     the device after the first multiple of `check_every` iterations at which
     every pair's L1 row-marginal residual is <= threshold.  Returns (log_u,
@@ -395,12 +402,14 @@ def sinkhorn_f32_solve(a, b, cost_matrix, epsilon, max_iter, threshold=0.0, log_
     n, d = a.shape
     for t, name in ((a, "a"), (b, "b")):
         _ot_check(t, n * d, name)
-    _ot_check(cost_matrix, d * d, "cost_matrix")
+    if cost_matrix is not None:
+        _ot_check(cost_matrix, d * d, "cost_matrix")
     lib = _lib.load()
     dev = a.device
     check = int(check_every) if threshold > 0 else 0
     with torch.cuda.device(dev):
-        nbytes = lib.tm_sinkhorn_f32_workspace_size(n, d, int(bool(log_space)), int(max_iter), check)
+        nbytes = lib.tm_sinkhorn_f32_workspace_size(n, d, int(bool(log_space)), int(max_iter), check,
+                                                    int(cost_matrix is None))
         ws = _workspace(nbytes, dev)
         log_u = torch.empty((n, d), dtype=torch.float32, device=dev)
         log_v = torch.empty_like(log_u)
@@ -421,7 +430,8 @@ def _plan_args(log_u, log_v, cost_matrix, epsilon):
     n, d = log_u.shape
     for t, name in ((log_u, "log_u"), (log_v, "log_v")):
         _ot_check(t, n * d, name)
-    _ot_check(cost_matrix, d * d, "cost_matrix")
+    if cost_matrix is not None:  # None: the line cost |i - j|
+        _ot_check(cost_matrix, d * d, "cost_matrix")
     return n, d
 
 

@@ -62,7 +62,7 @@ SIGNATURES = {
                                      c_i64, c_void, c_size, c_void]),
     "tm_sinkhorn_logiter": (c_int, [c_void, c_void, c_void, c_void, c_void, c_void, c_i64, c_i64,
                                     c_i64, c_double, c_void, c_size, c_void]),
-    "tm_sinkhorn_f32_workspace_size": (c_size, [c_i64, c_i64, c_int, c_i64, c_i64]),
+    "tm_sinkhorn_f32_workspace_size": (c_size, [c_i64, c_i64, c_int, c_i64, c_i64, c_int]),
     "tm_sinkhorn_f32_solve": (c_int, [c_void, c_void, c_void, c_i64, c_i64, c_double, c_int, c_i64,
                                       c_double, c_i64, c_void, c_void, c_void, c_void, c_void, c_void,
                                       c_size, c_void]),
@@ -86,6 +86,14 @@ SIGNATURES = {
     "tm_grey_gradient": (c_int, [c_void, c_void, c_i64, c_int, I64P, F32P, U8P, I64P, I64P, c_int, c_float,
                                  c_void]),
     "tm_grey_laplace": (c_int, [c_void, c_void, c_i64, c_int, I64P, F32P, U8P, I64P, I64P, c_int, c_float,
+                                c_void]),
+    "tm_grey_opening": (c_int, [c_void, c_void, c_i64, c_int, I64P, F32P, U8P, I64P, I64P, c_int, c_float,
+                                c_void]),
+    "tm_grey_closing": (c_int, [c_void, c_void, c_i64, c_int, I64P, F32P, U8P, I64P, I64P, c_int, c_float,
+                                c_void]),
+    "tm_white_tophat": (c_int, [c_void, c_void, c_i64, c_int, I64P, F32P, U8P, I64P, I64P, c_int, c_float,
+                                c_void]),
+    "tm_black_tophat": (c_int, [c_void, c_void, c_i64, c_int, I64P, F32P, U8P, I64P, I64P, c_int, c_float,
                                 c_void]),
     "tm_grey_dilation_backward": (c_int, [c_void, c_void, c_void, c_i64, c_int, I64P, U8P, I64P, I64P,
                                           c_int, c_void]),

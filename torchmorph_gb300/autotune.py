@@ -10,8 +10,8 @@ indexed by a work class (``tm_tune_*`` in include/torchmorph_gb300.h):
   two CTAs per SM (class from the pair count and the point count);
 * ``edt_3d``        3-D exact EDT: bitmap shell search first, or the separable
   passes alone (class: log2 of the voxel count);
-* ``cdt_3d``        3-D chamfer distances: bitmap shell search first, or the
-  raster passes alone.
+* ``cdt_3d``        3-D chamfer distances: bitmap shell search first (persistent
+  warps on a unit queue, or one CTA per 32-row block), or the raster passes alone.
 
 Every variant of an operator computes bit-identical results, so tuning
 changes speed only.  :func:`tune` times every variant of one call with CUDA

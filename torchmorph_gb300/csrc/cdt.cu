@@ -488,13 +488,15 @@ extern "C" int tm_cdt(const void *input, int in_dtype, int64_t batch, int ndim, 
     cudaStream_t s = (cudaStream_t)stream;
     int *todo = nullptr;
     bool cleared = false;
-    // autotuned variant 1: the raster passes for every item (no shell search)
-    const bool shell = tune_variant(kTuneCdt3D, tune_class(kTuneCdt3D, g.numel, 0)) != 1;
+    // autotuned variants: 1 = the raster passes for every item (no shell search),
+    // 2 = the shell search with one CTA per 32-row block instead of the warp queue
+    const int variant = tune_variant(kTuneCdt3D, tune_class(kTuneCdt3D, g.numel, 0));
+    const bool shell = variant != 1;
     if (shell && cdt_shell_shape(g) && cdt_shell_eligible(g, dist, indices)) {
         // counters first, so that nothing but kernels follows the shell search
         TM_CHECK_CUDA(clear_cdt_counters(ws, pl, s));
         cleared = true;
-        st = cdt_shell_run(input, in_dtype, g, metric, dist, ws + pl.total, &todo, s);
+        st = cdt_shell_run(input, in_dtype, g, metric, dist, ws + pl.total, &todo, s, variant == 2);
         if (st != TM_OK) return st;
     }
     if (in_dtype == TM_F32)

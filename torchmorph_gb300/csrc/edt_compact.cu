@@ -32,6 +32,7 @@
 #include <array>
 #include <cstring>
 #include <mutex>
+#include <utility>
 #include <vector>
 
 #include "edt_internal.cuh"
@@ -82,11 +83,11 @@ __device__ __forceinline__ uint32_t window_key(const uint32_t *w) {
 
 // Widen the search of position q from the first window |q-p| <= K to the
 // exact radius isqrt(best).  G(p) reads the unshifted value for 0 <= p < L.
-// Returns false when the radius exceeds kFar.
+// Returns false when the radius exceeds `far`.
 template <int K, typename GF>
-__device__ __forceinline__ bool widen(int q, int L, GF G, uint32_t &best, int &bp) {
+__device__ __forceinline__ bool widen(int q, int L, GF G, uint32_t &best, int &bp, int far = kFar) {
     const int r = best >= kBig ? L : isqrt_floor(best);
-    if (r > kFar) return false;
+    if (r > far) return false;
     const int lo = q - r < 0 ? 0 : q - r, hi = q + r >= L ? L - 1 : q + r;
     for (int pp = lo; pp < q - K; pp++) {
         const uint32_t v = (uint32_t)((q - pp) * (q - pp)) + G(pp);
@@ -686,9 +687,13 @@ constexpr int kC12PadBot = kNear1 + kQB;
 constexpr int kC12PadX = 4;
 constexpr uint8_t kNoF0 = 255;
 constexpr uint16_t kNoF01 = 0xFFFF;
+// Widest window radius of the fused passes before a line takes its exact envelope:
+// the items reaching these passes are mostly sparse, where wider windows cost
+// O(radius) per voxel while the envelope costs O(1).
+constexpr int kC12Far = 8;
 
 struct C12Smem {
-    int L1, L2, rowp;  // rowp: padded pass-2 row length
+    int L1, L2, rowp;  // rowp: padded pass-2 row length (row rounded up to 4 voxels + both pads)
     size_t tab, f0s, p1, stk, flag, rflag, total;
 };
 
@@ -700,7 +705,7 @@ __host__ __device__ inline C12Smem c12_smem(int L1, int L2) {
     C12Smem m;
     m.L1 = L1;
     m.L2 = L2;
-    m.rowp = L2 + 2 * kC12PadX;
+    m.rowp = (L2 + 3) / 4 * 4 + 2 * kC12PadX;
     size_t off = 0;
     m.tab = off;
     off += kSqrtTab * 4;
@@ -719,13 +724,17 @@ __host__ __device__ inline C12Smem c12_smem(int L1, int L2) {
     return m;
 }
 
-// One plane (block number blk = item * L0 + z) of the fused passes 1 + 2.
-__device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *__restrict__ c1,
+// One (L1 x W) plane of the fused passes 1 + 2: the plane's pass-0 features
+// start at c1 + plane and its outputs at plane in each output (index planes
+// `numel` apart); z is the plane's axis-0 coordinate.  VEC: W % 4 == 0 and
+// 16-byte aligned planes (8-byte loads, 16-byte stores); otherwise every
+// access is scalar, for items packed at any offset.
+template <bool VEC>
+__device__ __forceinline__ void edt_c12_plane(const int64_t plane, const int z, const int L1, const int W,
+                                              const int64_t numel, const int16_t *__restrict__ c1,
                                               float *__restrict__ dist, int32_t *__restrict__ indices,
-                                              int32_t *__restrict__ sqdist, int16_t *__restrict__ gstack,
-                                              const CompactParams &p) {
+                                              int32_t *__restrict__ sqdist) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int L0 = p.L0, L1 = p.L1, W = p.L2;
     const C12Smem sm = c12_smem(L1, W);
     float *tab = reinterpret_cast<float *>(smem_raw + sm.tab);
     uint8_t *f0s = smem_raw + sm.f0s + kC12PadTop * W;  // row y at f0s + y * W, y in -4 .. L1+11
@@ -734,10 +743,7 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
     int *colflag = reinterpret_cast<int *>(smem_raw + sm.flag);
     int *rowflag = reinterpret_cast<int *>(smem_raw + sm.rflag);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int64_t item = blk / L0;
-    const int z = (int)(blk - item * L0);
-    const int64_t plane = item * p.numel_item + (int64_t)z * L1 * W;
-    const int rowp = sm.rowp;
+    const int rowp = sm.rowp, padr = rowp - kC12PadX - W;  // right padding: kC12PadX + round-up
     for (int i = tid; i < kSqrtTab; i += kC12Threads) tab[i] = __fsqrt_rn((float)i);
     // padding: "no site" rows around the f0 plane and columns around each p1 row
     for (int i = tid; i < (kC12PadTop + kC12PadBot) * W; i += kC12Threads) {
@@ -745,17 +751,25 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
         const int y = r < kC12PadTop ? r - kC12PadTop : L1 + r - kC12PadTop;
         f0s[y * W + c] = kNoF0;
     }
-    for (int i = tid; i < L1 * 2 * kC12PadX; i += kC12Threads) {
-        const int y = i / (2 * kC12PadX), k = i % (2 * kC12PadX);
-        p1[y * rowp + (k < kC12PadX ? k : W + k)] = kNoF01;
+    for (int i = tid; i < L1 * (kC12PadX + padr); i += kC12Threads) {
+        const int y = i / (kC12PadX + padr), k = i % (kC12PadX + padr);
+        p1[y * rowp + (k < kC12PadX ? k : kC12PadX + W + (k - kC12PadX))] = kNoF01;
     }
-    // stage the pass-0 features of the plane as bytes, 4 per lane per row
-    for (int i = tid; i < L1 * (W / 4); i += kC12Threads) {
-        const int y = i / (W / 4), c4 = i % (W / 4);
-        const short4 v = *reinterpret_cast<const short4 *>(c1 + plane + (int64_t)y * W + 4 * c4);
-        const uint32_t b0 = v.x < 0 ? kNoF0 : (uint32_t)v.x, b1 = v.y < 0 ? kNoF0 : (uint32_t)v.y;
-        const uint32_t b2 = v.z < 0 ? kNoF0 : (uint32_t)v.z, b3 = v.w < 0 ? kNoF0 : (uint32_t)v.w;
-        reinterpret_cast<uint32_t *>(f0s + y * W)[c4] = b0 | (b1 << 8) | (b2 << 16) | (b3 << 24);
+    if (VEC) {  // stage the pass-0 features of the plane as bytes, 4 per lane per row
+        for (int i = tid; i < L1 * (W / 4); i += kC12Threads) {
+            const int y = i / (W / 4), c4 = i % (W / 4);
+            const short4 v = *reinterpret_cast<const short4 *>(c1 + plane + (int64_t)y * W + 4 * c4);
+            const uint32_t b0 = v.x < 0 ? kNoF0 : (uint32_t)v.x, b1 = v.y < 0 ? kNoF0 : (uint32_t)v.y;
+            const uint32_t b2 = v.z < 0 ? kNoF0 : (uint32_t)v.z, b3 = v.w < 0 ? kNoF0 : (uint32_t)v.w;
+            reinterpret_cast<uint32_t *>(f0s + y * W)[c4] = b0 | (b1 << 8) | (b2 << 16) | (b3 << 24);
+        }
+    } else {
+        // (L2 loads: in the ragged launch other SMs wrote these features after
+        // a grid barrier, so no L1 line may serve them)
+        for (int i = tid; i < L1 * W; i += kC12Threads) {
+            const int16_t v = __ldcg(c1 + plane + i);
+            f0s[i] = v < 0 ? kNoF0 : (uint8_t)v;
+        }
     }
     __syncthreads();
 
@@ -788,7 +802,7 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
                         const uint32_t key = window_key<kNear1>(w + i);
                         uint32_t best = key >> kKeyShift;
                         int bp = q - kNear1 + (int)(key & 31u);
-                        if (best >= (kNear1 + 1) * (kNear1 + 1) && !widen<kNear1>(q, L1, G1, best, bp)) {
+                        if (best >= (kNear1 + 1) * (kNear1 + 1) && !widen<kNear1>(q, L1, G1, best, bp, kC12Far)) {
                             fallback = true;
                         } else {
                             p1[q * rowp + kC12PadX + x] =
@@ -860,7 +874,6 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
     }
 
     // ---- pass 2: rows along axis 2, one warp per row, 4 voxels per lane
-    const int64_t numel = p.numel;
     for (int i = tid; i < L1; i += kC12Threads) rowflag[i] = 0;
     __syncthreads();
     for (int y = warp; y < L1; y += kC12Warps) {
@@ -909,7 +922,10 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
                 const uint32_t key = window_key<kNear2>(w + i + 2);
                 uint32_t best = key >> kKeyShift;
                 int bp = q - kNear2 + (int)(key & 31u);
-                if (best >= (kNear2 + 1) * (kNear2 + 1) && !widen<kNear2>(q, W, G2, best, bp)) fallback = true;
+                // (VEC: q < W always; otherwise the round-up positions have no site
+                // and are neither searched nor written)
+                if (q < W && best >= (kNear2 + 1) * (kNear2 + 1) && !widen<kNear2>(q, W, G2, best, bp, kC12Far))
+                    fallback = true;
                 const uint32_t f = row[bp];
                 dv[i] = dist_of(best, tab);
                 sq[i] = (int32_t)best;
@@ -919,12 +935,26 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
             }
             if (fallback) break;
             const int64_t gi = base + q0;
-            if (dist) *reinterpret_cast<float4 *>(dist + gi) = make_float4(dv[0], dv[1], dv[2], dv[3]);
-            if (sqdist) *reinterpret_cast<int4 *>(sqdist + gi) = make_int4(sq[0], sq[1], sq[2], sq[3]);
-            if (indices) {
-                *reinterpret_cast<int4 *>(indices + gi) = make_int4(i0[0], i0[1], i0[2], i0[3]);
-                *reinterpret_cast<int4 *>(indices + numel + gi) = make_int4(i1[0], i1[1], i1[2], i1[3]);
-                *reinterpret_cast<int4 *>(indices + 2 * numel + gi) = make_int4(i2[0], i2[1], i2[2], i2[3]);
+            if (VEC) {
+                if (dist) *reinterpret_cast<float4 *>(dist + gi) = make_float4(dv[0], dv[1], dv[2], dv[3]);
+                if (sqdist) *reinterpret_cast<int4 *>(sqdist + gi) = make_int4(sq[0], sq[1], sq[2], sq[3]);
+                if (indices) {
+                    *reinterpret_cast<int4 *>(indices + gi) = make_int4(i0[0], i0[1], i0[2], i0[3]);
+                    *reinterpret_cast<int4 *>(indices + numel + gi) = make_int4(i1[0], i1[1], i1[2], i1[3]);
+                    *reinterpret_cast<int4 *>(indices + 2 * numel + gi) = make_int4(i2[0], i2[1], i2[2], i2[3]);
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    if (q0 + i >= W) break;
+                    if (dist) dist[gi + i] = dv[i];
+                    if (sqdist) sqdist[gi + i] = sq[i];
+                    if (indices) {
+                        indices[gi + i] = i0[i];
+                        indices[numel + gi + i] = i1[i];
+                        indices[2 * numel + gi + i] = i2[i];
+                    }
+                }
             }
         }
         if (__any_sync(0xffffffffu, fallback) && lane == 0) rowflag[y] = 1;
@@ -1017,14 +1047,106 @@ __device__ __forceinline__ void edt_c12_block(const int64_t blk, const int16_t *
 // read per plane.
 __global__ void __launch_bounds__(kC12Threads, 3) edt_c12_kernel(const int16_t *__restrict__ c1, float *__restrict__ dist,
                                                               int32_t *__restrict__ indices,
-                                                              int32_t *__restrict__ sqdist,
-                                                              int16_t *__restrict__ gstack, CompactParams p,
+                                                              int32_t *__restrict__ sqdist, CompactParams p,
                                                               const int *__restrict__ todo) {
     pdl_wait();  // launched after pass 0: its features are complete
     const int64_t nblk = p.batch * (int64_t)p.L0;
     for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
-        if (todo && !todo[blk / p.L0]) continue;  // item finished by the shell pass
-        edt_c12_block(blk, c1, dist, indices, sqdist, gstack, p);
+        const int64_t item = blk / p.L0;
+        if (todo && !todo[item]) continue;  // item finished by the shell pass
+        const int z = (int)(blk - item * p.L0);
+        edt_c12_plane<true>(item * p.numel_item + (int64_t)z * p.L1 * p.L2, z, p.L1, p.L2, p.numel, c1, dist, indices,
+                            sqdist);
+        __syncthreads();  // the next plane reuses shared memory
+    }
+}
+
+// ------------------------------------------- ragged batches of 3-D items
+// The fused plane passes over a ragged batch (items packed at any offset,
+// every axis at most kRaggedC12MaxLine): one cooperative launch whose first
+// phase runs pass 0 over the axis-0 columns of every item (one thread per
+// column, adjacent threads on adjacent columns: coalesced), and whose second
+// phase, after a bounded grid barrier, gives the planes of all items to the
+// CTAs in turn (edt_c12_plane with scalar accesses).
+constexpr int kRaggedC12MaxLine = 180;  // the plane code's shared memory stays below 170 KB
+
+struct RaggedC12Args {
+    const void *in;
+    int in_f32;
+    int nitems;
+    const ReItem *items;
+    int64_t cols, total;
+    int16_t *c1;
+    float *dist;
+    int32_t *indices, *sqdist;
+    GridControl *ctl;
+    int *status;
+    long long spin_limit;
+};
+
+__global__ void __launch_bounds__(kC12Threads, 2) ragged_edt3_kernel(RaggedC12Args A) {
+    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+    const ReItem *items = A.items;
+    // pass 0: the nearest background along axis 0 as its position (int16, -1:
+    // none), ties to the lower position; input loads 8 deep per thread
+    for (int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; col < A.cols; col += nthreads) {
+        int lo = 0, hi = A.nitems - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (items[mid].line_begin[0] <= col) lo = mid;
+            else hi = mid - 1;
+        }
+        const ReItem &it = items[lo];
+        const int D = it.shape[0];
+        const int64_t stride = (int64_t)it.shape[1] * it.shape[2];
+        const int64_t base = it.off + (col - it.line_begin[0]);
+        int prev = -1;
+        for (int q0 = 0; q0 < D; q0 += 8) {
+            bool bg[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int64_t p = base + (int64_t)(q0 + u) * stride;
+                bg[u] = q0 + u < D && (A.in_f32 ? static_cast<const float *>(A.in)[p] == 0.0f
+                                                : static_cast<const uint8_t *>(A.in)[p] == 0);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                if (q0 + u >= D) break;
+                if (bg[u]) prev = q0 + u;
+                A.c1[base + (int64_t)(q0 + u) * stride] = (int16_t)prev;
+            }
+        }
+        // backward: the first background after q replaces the forward result only when
+        // strictly nearer (this thread's own stores, read back in program order)
+        int next = -1;
+        for (int q0 = ((D - 1) / 8) * 8; q0 >= 0; q0 -= 8) {
+            int v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) v[u] = q0 + u < D ? A.c1[base + (int64_t)(q0 + u) * stride] : -1;
+#pragma unroll
+            for (int u = 7; u >= 0; u--) {
+                const int q = q0 + u;
+                if (q >= D) continue;
+                if (v[u] == q) next = q;
+                else if (next >= 0 && (v[u] < 0 || next - q < q - v[u]))
+                    A.c1[base + (int64_t)q * stride] = (int16_t)next;
+            }
+        }
+    }
+    if (!grid_barrier_bounded(A.ctl, A.status, A.spin_limit)) return;
+    // passes 1 + 2: one plane of one item per CTA at a time
+    const ReItem &last = items[A.nitems - 1];
+    const int64_t nplanes = (int64_t)last.plane_begin + last.shape[0];
+    for (int64_t k = blockIdx.x; k < nplanes; k += gridDim.x) {
+        int lo = 0, hi = A.nitems - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (items[mid].plane_begin <= k) lo = mid;
+            else hi = mid - 1;
+        }
+        const ReItem &it = items[lo];
+        const int z = (int)(k - it.plane_begin), H = it.shape[1], W = it.shape[2];
+        edt_c12_plane<false>(it.off + (int64_t)z * H * W, z, H, W, A.total, A.c1, A.dist, A.indices, A.sqdist);
         __syncthreads();  // the next plane reuses shared memory
     }
 }
@@ -1372,11 +1494,13 @@ constexpr int kShellCtWarps = 4;
 constexpr unsigned kFarPerUnit = 32;  // voxels beyond the shell searched per 8-row unit at most
 constexpr int kShellCtThreads = 32 * kShellCtWarps;
 constexpr int kShellWarpRows = 8;                        // rows per warp unit (8 rows x 4 words = 32 lanes)
-constexpr int kSwPitch = 6;                              // staged row: 2 zero words, then the row's 4 words
 constexpr int kSwRowsP = kShellWarpRows + 2 * kShellR;   // 16 staged rows per plane
-constexpr int kSwPlaneP = kSwRowsP * kSwPitch;           // 96 words per staged plane
 constexpr int kSwStageRows = (2 * kShellR + 1) * kSwRowsP;  // 144
-constexpr int kSwWords = (2 * kShellR + 1) * kSwPlaneP + 2;  // + zero words read right of the last row
+// Staged rows are the 4 words of the bitmap row with no padding: the 32 lanes
+// of a warp (8 rows x 4 words) read 32 consecutive words -- conflict-free --
+// and a lane masks the word left of word 0 and right of word 3 itself.
+constexpr int kCwPlane = kSwRowsP * 4;                  // 64 words per staged plane
+constexpr int kCwWords = (2 * kShellR + 1) * kCwPlane;  // 576
 
 template <int WW>
 __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uint32_t *__restrict__ bm,
@@ -1388,7 +1512,9 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
     static_assert(kShellWarpRows * WW == 32, "one word per lane");
     constexpr ShellList kL = make_shell_list();
     constexpr int kStageIters = (kSwStageRows + 31) / 32;
-    __shared__ __align__(16) uint32_t bits_all[kShellCtWarps][kSwWords + 2];
+    // 4 words before and after the staged planes: the masked neighbour reads of
+    // the first and last rows stay inside the array
+    __shared__ __align__(16) uint32_t bits_all[kShellCtWarps][kCwWords + 8];
     // per word: bit-planes 0..8 of the resolving offset number (12 words, 16-byte aligned)
     __shared__ __align__(16) uint32_t planes_all[kShellCtWarps][32 * 12];
     __shared__ int2 tab2[kShellN];  // (packed offset, distance as float bits)
@@ -1398,14 +1524,15 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
     // 64-bit work counter after the per-item flags (8-byte aligned), zeroed with them
     unsigned long long *queue = reinterpret_cast<unsigned long long *>(todo + ((p.batch + 1) & ~(int64_t)1));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint32_t *bits = bits_all[warp];
+    uint32_t *bits = bits_all[warp] + 4;
     uint32_t *planes = planes_all[warp];
     pdl_trigger();  // the fallback passes may be scheduled as this grid's CTAs retire
     for (int t = threadIdx.x; t < kShellN; t += kShellCtThreads) {
         const uint32_t c = c_shell.v[t];
         tab2[t] = make_int2((int)c, __float_as_int(__fsqrt_rn((float)(c >> 12))));
     }
-    if (lane < 2) bits[kSwWords - 2 + lane] = 0u;
+    if (lane < 4) bits[-4 + lane] = 0u;
+    else if (lane < 8) bits[kCwWords + lane - 4] = 0u;
     __syncthreads();
     pdl_wait();  // the background bitmap and the zeroed flags / counter are complete
     const int64_t numel = p.numel;
@@ -1432,13 +1559,7 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
 #pragma unroll
         for (int j = 0; j < kStageIters; j++) {
             const int i = lane + 32 * j;
-            if (i < kSwStageRows) {
-                const int kk = i / kSwRowsP, r = i - kk * kSwRowsP;
-                uint2 *dst = reinterpret_cast<uint2 *>(bits + kk * kSwPlaneP + r * kSwPitch);
-                dst[0] = make_uint2(0u, 0u);
-                dst[1] = make_uint2(v[j].x, v[j].y);
-                dst[2] = make_uint2(v[j].z, v[j].w);
-            }
+            if (i < kSwStageRows) reinterpret_cast<uint4 *>(bits)[i] = v[j];  // row i = plane i / 16, row i % 16
         }
         __syncwarp();
         // search: lane = word (row lane / 4, word lane % 4).  The offset number
@@ -1451,7 +1572,8 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
             const int r = lane >> 2, wi = lane & 3;
             const int nb = min(32, W - 32 * wi);
             if (r < nrows) U = nb == 32 ? 0xffffffffu : ((1u << nb) - 1u);
-            const volatile uint32_t *vhere = bits + kShellR * kSwPlaneP + (kShellR + r) * kSwPitch + 2 + wi;
+            const volatile uint32_t *vhere = bits + kShellR * kCwPlane + (kShellR + r) * 4 + wi;
+            const bool has_l = wi != 0, has_r = wi != WW - 1;
             uint32_t P[9] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
             constexpr int kB = 8;
 #pragma unroll
@@ -1462,10 +1584,15 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
 #pragma unroll
                 for (int i = 0; i < kB; i++) {
                     const int t = t0 + i < kShellN ? t0 + i : kShellN - 1;
-                    const int delta = kL.o[t].dz * kSwPlaneP + kL.o[t].dy * kSwPitch + (kL.o[t].dx >= 0 ? 0 : -1);
-                    const int sh = kL.o[t].dx >= 0 ? kL.o[t].dx : 32 + kL.o[t].dx;
+                    const int d = kL.o[t].dz * kCwPlane + kL.o[t].dy * 4, dx = kL.o[t].dx;
                     // volatile: each batch's loads stay behind its exit test
-                    bg[i] = t0 + i < kShellN ? __funnelshift_r(vhere[delta], vhere[delta + 1], sh) : 0u;
+                    uint32_t b = 0u;
+                    if (t0 + i < kShellN) {
+                        if (dx == 0) b = vhere[d];
+                        else if (dx > 0) b = __funnelshift_r(vhere[d], has_r ? vhere[d + 1] : 0u, dx);
+                        else b = __funnelshift_r(has_l ? vhere[d - 1] : 0u, vhere[d], 32 + dx);
+                    }
+                    bg[i] = b;
                     any |= bg[i];
                 }
                 const uint32_t H = any & U;  // resolved in this batch
@@ -1783,6 +1910,205 @@ __global__ void __launch_bounds__(kShellThreads) cdt_shell_kernel(const uint32_t
     }
 }
 
+// The offsets of the chamfer list grouped by row (dz, dy) within each norm
+// class: the three staged words around a lane's word in that row (left
+// neighbour, own, right neighbour) serve every dx of the class in the row.
+struct CdtRow {
+    int dz, dy;
+    int mask;  // bit dx + 4 for each dx of the class in this row
+    int val;   // the class's norm
+    bool last; // last row of its class
+};
+constexpr int kCdtRowMax = 1024;
+struct CdtRowList {
+    int n;
+    CdtRow r[kCdtRowMax];
+};
+
+__host__ __device__ constexpr CdtRowList make_cdt_rows(int metric) {
+    CdtRowList l{};
+    const CdtShellList o = make_cdt_list(metric);
+    for (int c = 0; c < o.nclass; c++) {
+        int mask[81] = {};
+        for (int t = o.cls_begin[c]; t < o.cls_begin[c + 1]; t++)
+            mask[(o.o[t].dz + kShellR) * 9 + (o.o[t].dy + kShellR)] |= 1 << (o.o[t].dx + kShellR);
+        for (int k = 0; k < 81; k++)
+            if (mask[k]) l.r[l.n++] = CdtRow{k / 9 - kShellR, k % 9 - kShellR, mask[k], o.cls_value[c], false};
+        l.r[l.n - 1].last = true;
+    }
+    return l;
+}
+
+template <int MET>
+constexpr CdtRowList kCdtRows = make_cdt_rows(MET);
+
+struct CdtSearch {
+    uint32_t U;               // voxels of the word not resolved yet
+    uint32_t H;               // union of the current class's shifted backgrounds
+    uint32_t P0, P1, P2, P3;  // bit-planes of the resolved voxels' norms
+};
+
+// One row of the row list (a compile-time constant): OR its dx shifts into H
+// and, at the end of a class, resolve the class.  Returns false once every
+// voxel of the word is resolved (the rest of the list is skipped).
+template <int MET, int E>
+__device__ __forceinline__ bool cdt_row_step(const volatile uint32_t *vh, bool has_l, bool has_r, CdtSearch &s) {
+    constexpr CdtRow row = kCdtRows<MET>.r[E];
+    constexpr int d = row.dz * kCwPlane + row.dy * 4;
+    const uint32_t mw = vh[d];
+    uint32_t lw = 0u, rw = 0u;
+    if constexpr ((row.mask & 0x00f) != 0) lw = has_l ? vh[d - 1] : 0u;  // some dx < 0
+    if constexpr ((row.mask & 0x1e0) != 0) rw = has_r ? vh[d + 1] : 0u;  // some dx > 0
+#pragma unroll
+    for (int dx = -kShellR; dx <= kShellR; dx++)
+        if (row.mask & (1 << (dx + kShellR)))
+            s.H |= dx == 0 ? mw : dx > 0 ? __funnelshift_r(mw, rw, dx) : __funnelshift_r(lw, mw, 32 + dx);
+    if constexpr (row.last) {
+        const uint32_t hit = s.H & s.U;
+        s.U &= ~hit;
+        if constexpr ((row.val & 1) != 0) s.P0 |= hit;
+        if constexpr ((row.val & 2) != 0) s.P1 |= hit;
+        if constexpr ((row.val & 4) != 0) s.P2 |= hit;
+        if constexpr ((row.val & 8) != 0) s.P3 |= hit;
+        s.H = 0u;
+        return s.U != 0u;
+    }
+    return true;
+}
+
+template <int MET, int... Es>
+__device__ __forceinline__ void cdt_rows_all(std::integer_sequence<int, Es...>, const volatile uint32_t *vh, bool has_l,
+                                             bool has_r, CdtSearch &s) {
+    (cdt_row_step<MET, Es>(vh, has_l, has_r, s) && ...);  // stops at the first false
+}
+
+// The same search on the EDT shell kernel's work-queue design: persistent
+// warps take 8-row units (one 32-voxel word per lane), stage the 9 x 16
+// bitmap rows they read, and keep each voxel's norm (<= 12) as 4 bit-planes
+// of the word: per norm class, the voxels the class resolves OR into the
+// planes of the class value's set bits, so nothing is stored per voxel until
+// the writing lanes decode four voxels at once.  Staged rows are 4 words with
+// no padding, so the 32 lanes (8 rows x 4 words) read 32 consecutive words --
+// conflict-free -- and a lane masks the words left of word 0 and right of
+// word 3 itself.  Flags: todo[item], todo[batch] as in cdt_shell_kernel; the
+// 64-bit work counter follows them (8-byte aligned), zeroed with them.
+
+template <int MET>
+__global__ void __launch_bounds__(kShellCtThreads) cdt_shell_warp_kernel(const uint32_t *__restrict__ bm,
+                                                                         float *__restrict__ dist,
+                                                                         int *__restrict__ todo, CompactParams p,
+                                                                         float divisor) {
+    constexpr int WW = 4;
+    constexpr int kStageIters = (kSwStageRows + 31) / 32;
+    static_assert(kShellWarpRows * WW == 32, "one word per lane");
+    static_assert(cdt_vmax(MET) < 16, "norms fit four bit-planes");
+    // 4 words before and after the staged planes: the masked neighbour reads of
+    // the first and last rows stay inside the array
+    __shared__ __align__(16) uint32_t bits_all[kShellCtWarps][kCwWords + 8];
+    __shared__ __align__(16) uint4 planes_all[kShellCtWarps][32];
+    const int L0 = p.L0, L1 = p.L1, W = p.L2;
+    const int ybl = (L1 + kShellWarpRows - 1) / kShellWarpRows;
+    const int64_t nunits = p.batch * (int64_t)L0 * ybl;
+    unsigned long long *queue = reinterpret_cast<unsigned long long *>(todo + ((p.batch + 2) & ~(int64_t)1));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t *bits = bits_all[warp] + 4;
+    uint4 *planes = planes_all[warp];
+    pdl_trigger();  // the raster kernel may be scheduled as this grid's CTAs retire
+    if (lane < 4) bits[-4 + lane] = 0u;
+    else if (lane < 8) bits[kCwWords + lane - 4] = 0u;
+    __syncwarp();
+    pdl_wait();  // the background bitmap and the zeroed flags / counter are complete
+    for (;;) {
+        int64_t unit = 0;
+        if (lane == 0) unit = (int64_t)atomicAdd(queue, 1ull);
+        unit = __shfl_sync(~0u, unit, 0);
+        if (unit >= nunits) break;
+        const int64_t item = unit / ((int64_t)L0 * ybl);
+        const int rem = (int)(unit - item * L0 * ybl);
+        const int z = rem / ybl, y0 = (rem % ybl) * kShellWarpRows;
+        const int nrows = min(kShellWarpRows, L1 - y0);
+        const uint32_t *ibm = bm + item * (int64_t)L0 * L1 * WW;
+        uint4 v[kStageIters];
+#pragma unroll
+        for (int j = 0; j < kStageIters; j++) {
+            const int i = lane + 32 * j;
+            const int kk = i / kSwRowsP, r = i - kk * kSwRowsP;
+            const int zz = z - kShellR + kk, yy = y0 - kShellR + r;
+            const bool ok = i < kSwStageRows && (unsigned)zz < (unsigned)L0 && (unsigned)yy < (unsigned)L1;
+            v[j] = ok ? *reinterpret_cast<const uint4 *>(ibm + ((int64_t)zz * L1 + yy) * WW) : make_uint4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int j = 0; j < kStageIters; j++) {
+            const int i = lane + 32 * j;
+            if (i < kSwStageRows) reinterpret_cast<uint4 *>(bits)[i] = v[j];  // row i = plane i / 16, row i % 16
+        }
+        __syncwarp();
+        uint32_t U = 0u;
+        {
+            const int r = lane >> 2, wi = lane & 3;
+            const int nb = min(32, W - 32 * wi);
+            if (r < nrows) U = nb == 32 ? 0xffffffffu : ((1u << nb) - 1u);
+            const volatile uint32_t *vh = bits + kShellR * kCwPlane + (kShellR + r) * 4 + wi;
+            const bool has_l = wi != 0, has_r = wi != WW - 1;
+            // one straight-line pass over the rows of each norm class in turn; at
+            // the end of a class its union resolves the voxels it covers
+            CdtSearch cs{U, 0u, 0u, 0u, 0u, 0u};
+            cdt_rows_all<MET>(std::make_integer_sequence<int, kCdtRows<MET>.n>{}, vh, has_l, has_r, cs);
+            U = cs.U;
+            planes[lane] = make_uint4(cs.P0, cs.P1, cs.P2, cs.P3);
+        }
+        const unsigned nfar = __reduce_add_sync(~0u, (unsigned)__popc(U));
+        if (nfar > kFarPerUnit) {  // many voxels beyond the shell: the item takes the raster passes
+            if (lane == 0) {
+                atomicExch(&todo[item], 1);
+                atomicExch(&todo[p.batch], 1);
+            }
+            continue;
+        }
+        __syncwarp();
+        const int64_t rowbase = item * p.numel_item + ((int64_t)z * L1 + y0) * W;
+        const int x = 4 * lane;
+        if (x < W) {
+            const int b = x & 31;
+            for (int r = 0; r < nrows; r++) {
+                const uint4 q = planes[r * 4 + (x >> 5)];
+                // the norms of voxels x..x+3, one per byte: each plane's nibble
+                // spread to one bit per byte
+                const uint32_t acc = ((((q.x >> b) & 15u) * 0x00204081u) & 0x01010101u) |
+                                     (((((q.y >> b) & 15u) * 0x00204081u) & 0x01010101u) << 1) |
+                                     (((((q.z >> b) & 15u) * 0x00204081u) & 0x01010101u) << 2) |
+                                     (((((q.w >> b) & 15u) * 0x00204081u) & 0x01010101u) << 3);
+                float4 d;
+                // divisor 3 (3-4-5): correctly rounded v / 3 as the raster path computes it
+                d.x = divisor == 1.f ? (float)(acc & 255u) : (float)(acc & 255u) / divisor;
+                d.y = divisor == 1.f ? (float)((acc >> 8) & 255u) : (float)((acc >> 8) & 255u) / divisor;
+                d.z = divisor == 1.f ? (float)((acc >> 16) & 255u) : (float)((acc >> 16) & 255u) / divisor;
+                d.w = divisor == 1.f ? (float)(acc >> 24) : (float)(acc >> 24) / divisor;
+                *reinterpret_cast<float4 *>(dist + rowbase + (int64_t)r * W + x) = d;
+            }
+        }
+        if (nfar) {
+            __syncwarp();  // the unit's stores above come first
+            for (unsigned has = __ballot_sync(~0u, U != 0u); has; has &= has - 1) {
+                const int src = __ffs(has) - 1;
+                for (uint32_t m = __shfl_sync(~0u, U, src); m; m &= m - 1) {
+                    const int yv = y0 + (src >> 2), xv = 32 * (src & 3) + __ffs(m) - 1;
+                    const int best = far_norm_search<MET>(ibm, z, yv, xv, L0, L1, W, lane);
+                    if (lane != 0) continue;
+                    if (best < 0) {  // no background: the raster passes give -1
+                        atomicExch(&todo[item], 1);
+                        atomicExch(&todo[p.batch], 1);
+                    } else {
+                        dist[rowbase + (int64_t)(yv - y0) * W + xv] =
+                            divisor == 1.f ? (float)best : (float)best / divisor;
+                    }
+                }
+            }
+        }
+        __syncwarp();  // bits and planes are free for the next unit
+    }
+}
+
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 }  // namespace
@@ -1951,7 +2277,7 @@ int edt_compact_run(const void *input, int in_dtype, const Geometry &g, float *d
         // launched after pass 0 (whose kernel runs normally when there is no shell search)
         const int64_t grid = todo ? std::min<int64_t>(blocks, wave_ctas(edt_c12_kernel, kC12Threads, smem)) : blocks;
         TM_CHECK_CUDA(launch_pdl(edt_c12_kernel, dim3((unsigned)grid), dim3(kC12Threads), smem, stream,
-                                 (const int16_t *)c1, dist, indices, sqdist, stack1, p, (const int *)todo));
+                                 (const int16_t *)c1, dist, indices, sqdist, p, (const int *)todo));
         TM_LAUNCH_CHECK("edt_c12_kernel");
         return TM_OK;
     }
@@ -2003,11 +2329,13 @@ bool cdt_shell_eligible(const Geometry &g, const float *dist, const int32_t *ind
 
 size_t cdt_shell_workspace(const Geometry &g) {
     const int ww = (int)((g.shape[2] + 31) / 32);
-    return align256((size_t)g.batch * g.shape[0] * g.shape[1] * ww * 4) + align256((size_t)(g.batch + 1) * 4);
+    // per-item flags, the "some item is marked" flag, then the 64-bit work counter
+    return align256((size_t)g.batch * g.shape[0] * g.shape[1] * ww * 4) +
+           align256((size_t)((g.batch + 2) & ~(int64_t)1) * 4 + 8);
 }
 
 int cdt_shell_run(const void *input, int in_dtype, const Geometry &g, int metric, float *dist, unsigned char *ws,
-                  int **todo_out, cudaStream_t stream) {
+                  int **todo_out, cudaStream_t stream, bool block_kernel) {
     CompactParams p;
     std::memset(&p, 0, sizeof(p));
     p.ndim = 3;
@@ -2022,7 +2350,9 @@ int cdt_shell_run(const void *input, int in_dtype, const Geometry &g, int metric
     uint32_t *bm = reinterpret_cast<uint32_t *>(ws);
     int *todo = reinterpret_cast<int *>(ws + align256((size_t)nwords * 4));
     if (g.batch > ((int64_t)1 << 30)) return fail(TM_ERR_TOO_LARGE, "batch too large");
-    const int nclear = (int)g.batch + 1;  // per-item flags and the "any item marked" flag, zeroed by the bitmap kernel
+    // per-item flags, the "any item marked" flag and (8-byte aligned) the warp
+    // kernel's work counter, zeroed by the bitmap kernel
+    const int nclear = (int)((g.batch + 2) & ~(int64_t)1) + 2;
     const unsigned bblocks = (unsigned)std::min<int64_t>(ceil_div(nwords, 256), (int64_t)sm_count() * 16);
     const bool vrow = (p.L2 % 32) == 0 && ((uintptr_t)input & 15) == 0;
     if (in_dtype == TM_F32) {
@@ -2038,15 +2368,80 @@ int cdt_shell_run(const void *input, int in_dtype, const Geometry &g, int metric
     const int64_t blocks = g.batch * (int64_t)p.L0 * ceil_div(p.L1, kShellRows);
     if (blocks >= ((int64_t)1 << 31)) return fail(TM_ERR_TOO_LARGE, "too many blocks");
     const float div = metric == TM_CDT_CHAMFER345 ? 3.0f : 1.0f;
-    auto go = [&](auto kernel) {
-        return launch_pdl(kernel, dim3((unsigned)blocks), dim3(kShellThreads), 0, stream, (const uint32_t *)bm, dist,
-                          todo, p, div);
-    };
-    if (metric == TM_CDT_CHESSBOARD) TM_CHECK_CUDA(go(cdt_shell_kernel<4, 0>));
-    else if (metric == TM_CDT_TAXICAB) TM_CHECK_CUDA(go(cdt_shell_kernel<4, 1>));
-    else TM_CHECK_CUDA(go(cdt_shell_kernel<4, 2>));
-    TM_LAUNCH_CHECK("cdt_shell_kernel");
+    if (block_kernel) {  // one CTA per 32-row block
+        auto go = [&](auto kernel) {
+            return launch_pdl(kernel, dim3((unsigned)blocks), dim3(kShellThreads), 0, stream, (const uint32_t *)bm,
+                              dist, todo, p, div);
+        };
+        if (metric == TM_CDT_CHESSBOARD) TM_CHECK_CUDA(go(cdt_shell_kernel<4, 0>));
+        else if (metric == TM_CDT_TAXICAB) TM_CHECK_CUDA(go(cdt_shell_kernel<4, 1>));
+        else TM_CHECK_CUDA(go(cdt_shell_kernel<4, 2>));
+        TM_LAUNCH_CHECK("cdt_shell_kernel");
+    } else {  // persistent warps on a work queue of 8-row units
+        auto go = [&](auto kernel) -> int {
+            int per_sm = 0;
+            TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kShellCtThreads, 0));
+            const int64_t wunits = g.batch * (int64_t)p.L0 * ceil_div(p.L1, kShellWarpRows);
+            const int64_t grid = std::min<int64_t>((int64_t)(per_sm < 1 ? 1 : per_sm) * sm_count(),
+                                                   ceil_div(wunits, kShellCtWarps));
+            TM_CHECK_CUDA(launch_pdl(kernel, dim3((unsigned)grid), dim3(kShellCtThreads), 0, stream,
+                                     (const uint32_t *)bm, dist, todo, p, div));
+            return TM_OK;
+        };
+        int st;
+        if (metric == TM_CDT_CHESSBOARD) st = go(cdt_shell_warp_kernel<0>);
+        else if (metric == TM_CDT_TAXICAB) st = go(cdt_shell_warp_kernel<1>);
+        else st = go(cdt_shell_warp_kernel<2>);
+        if (st != TM_OK) return st;
+        TM_LAUNCH_CHECK("cdt_shell_warp_kernel");
+    }
     *todo_out = todo;
+    return TM_OK;
+}
+
+int ragged_edt3_max_line() { return kRaggedC12MaxLine; }
+
+int ragged_edt3_run(const void *input, int in_f32, const ReItem *items, int nitems, int64_t cols, int64_t total,
+                    int max_line, int16_t *c1, float *dist, int32_t *indices, int32_t *sqdist, GridControl *ctl,
+                    cudaStream_t stream) {
+    if (max_line < 1 || max_line > kRaggedC12MaxLine)
+        return fail(TM_ERR_UNSUPPORTED, "ragged 3-D planes need axes of at most %d voxels", kRaggedC12MaxLine);
+    RaggedC12Args A{};
+    A.in = input;
+    A.in_f32 = in_f32;
+    A.nitems = nitems;
+    A.items = items;
+    A.cols = cols;
+    A.total = total;
+    A.c1 = c1;
+    A.dist = dist;
+    A.indices = indices;
+    A.sqdist = sqdist;
+    A.ctl = ctl;
+    int st = device_status_word(&A.status);
+    if (st != TM_OK) return st;
+    A.spin_limit = grid_wait_budget();
+    // every plane's regions fit the largest item's layout (each grows with L1 and W)
+    const size_t smem = c12_smem(max_line, max_line).total;
+    static thread_local int cached_dev = -1, cached_per_sm = 0;
+    static thread_local size_t cached_smem = 0;
+    int dev = 0;
+    TM_CHECK_CUDA(cudaGetDevice(&dev));
+    if (cached_dev != dev || cached_smem != smem) {
+        TM_CHECK_CUDA(cudaFuncSetAttribute(ragged_edt3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)c12_smem(kRaggedC12MaxLine, kRaggedC12MaxLine).total));
+        TM_CHECK_CUDA(
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_per_sm, ragged_edt3_kernel, kC12Threads, smem));
+        cached_dev = dev;
+        cached_smem = smem;
+    }
+    if (cached_per_sm < 1) return fail(TM_ERR_UNSUPPORTED, "ragged 3-D EDT kernel does not fit on an SM");
+    const int64_t blocks = (int64_t)cached_per_sm * sm_count();  // one wave: both phases are grid-stride loops
+    TM_CHECK_CUDA(cudaMemsetAsync(ctl, 0, sizeof(GridControl), stream));
+    void *params[] = {&A};
+    TM_CHECK_CUDA(cudaLaunchCooperativeKernel((const void *)ragged_edt3_kernel, dim3((unsigned)blocks),
+                                              dim3(kC12Threads), params, smem, stream));
+    TM_LAUNCH_CHECK("ragged_edt3_kernel");
     return TM_OK;
 }
 

@@ -20,10 +20,16 @@
 // lines up to 256 voxels live in shared memory (interleaved per thread),
 // longer ones in the workspace.  The per-item loop the reference runs on the
 // host (three axis passes with transposes per item) becomes one launch.
+//
+// Batches of 3-D items whose axes are all at most ragged_edt3_max_line()
+// voxels take the uniform operator's fused plane passes instead
+// (edt_compact.cu, ragged_edt3_run): pass 0 as above, then passes 1 + 2 of
+// each (item, z) plane on chip by one CTA, with coalesced row stores -- the
+// same cooperative single launch, and the same results.
 #include <algorithm>
 #include <vector>
 
-#include "tm_tma.cuh"
+#include "edt_internal.cuh"
 
 namespace tmc {
 namespace {
@@ -31,14 +37,6 @@ namespace {
 constexpr int kReThreads = 128;
 constexpr int kReSmemL = 256;  // longest line with its stack in shared memory
 constexpr int32_t kReInf = 0x7fffffff;
-
-struct ReItem {
-    int64_t off;            // first voxel of the item in the packed buffers
-    int shape[3];           // (D, H, W) or (H, W, 1)
-    int pad;
-    int64_t line_begin[3];  // first line of the item along each axis
-};
-static_assert(sizeof(ReItem) == 48, "descriptor layout");
 
 struct RePlanHeader {
     int nitems, ndim;
@@ -48,14 +46,6 @@ struct RePlanHeader {
     int pad[52];
 };
 static_assert(sizeof(RePlanHeader) == 256, "plan header is 256 bytes");
-
-struct ReControl {
-    unsigned barrier_count;
-    unsigned barrier_gen;
-    int abort;
-    int pad[61];
-};
-static_assert(sizeof(ReControl) == 256, "control block is 256 bytes");
 
 struct ReArgs {
     const void *in;
@@ -68,47 +58,14 @@ struct ReArgs {
     int32_t *g[2];
     int32_t *f[2];
     int16_t *gstack;
+    int smem_l;  // longest line whose stack fits the shared region (min(max_line, 256))
     float *dist;
     int32_t *indices;
     int32_t *sqdist;
-    ReControl *ctl;
+    GridControl *ctl;
     int *status;
     long long spin_limit;
 };
-
-__device__ bool re_barrier(ReControl *ctl, int *status, long long spin_limit) {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned *gen = &ctl->barrier_gen;
-        volatile int *abort = &ctl->abort;
-        const unsigned g = *gen;
-        __threadfence();
-        int ok = 1;
-        if (atomicAdd(&ctl->barrier_count, 1u) == gridDim.x - 1) {
-            ctl->barrier_count = 0;
-            __threadfence();
-            atomicAdd(&ctl->barrier_gen, 1u);
-        } else {
-            long long polls = 0;
-            while (*gen == g) {
-                if (*abort || ++polls > spin_limit) {
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        if (!ok) {
-            atomicExch(&ctl->abort, 1);
-            if (status) atomicExch(status, TM_DEV_ERR_TIMEOUT);
-        }
-        __threadfence();
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
 
 // Item of line `line` along `axis` (binary search over the per-axis line starts).
 __device__ __forceinline__ int re_item(const ReArgs &A, int axis, int64_t line) {
@@ -159,7 +116,7 @@ __device__ __forceinline__ void re_write(const ReArgs &A, const ReItem &it, int6
 }
 
 __global__ void __launch_bounds__(kReThreads) ragged_edt_kernel(ReArgs A) {
-    extern __shared__ int16_t re_stack[];  // [kReSmemL][kReThreads]
+    extern __shared__ int16_t re_stack[];  // [smem_l][kReThreads]
     const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
     const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     for (int a = 0; a < A.ndim; a++) {
@@ -179,35 +136,55 @@ __global__ void __launch_bounds__(kReThreads) ragged_edt_kernel(ReArgs A) {
             const int64_t base = it.off + lbase;
             if (a == 0) {  // items have 2 or 3 axes: pass 0 is never the last
                 // nearest background along the line; ties to the lower position.
-                // Forward sweep: the last background at or before q.
+                // Forward sweep: the last background at or before q; the inputs of 8
+                // voxels are loaded before any is used (8 loads in flight per thread).
                 int prev = -1;
-                for (int q = 0; q < L; q++) {
-                    const int64_t p = base + (int64_t)q * inner;
-                    const bool bg = A.in_f32 ? static_cast<const float *>(A.in)[p] == 0.0f
-                                             : static_cast<const uint8_t *>(A.in)[p] == 0;
-                    if (bg) prev = q;
-                    gout[p] = prev < 0 ? kReInf : (q - prev) * (q - prev);
-                    fout[p] = prev < 0 ? -1 : (int32_t)(lbase + (int64_t)prev * inner);
+                for (int q0 = 0; q0 < L; q0 += 8) {
+                    bool bg[8];
+#pragma unroll
+                    for (int u = 0; u < 8; u++) {
+                        const int64_t p = base + (int64_t)(q0 + u) * inner;
+                        bg[u] = q0 + u < L && (A.in_f32 ? static_cast<const float *>(A.in)[p] == 0.0f
+                                                        : static_cast<const uint8_t *>(A.in)[p] == 0);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; u++) {
+                        const int q = q0 + u;
+                        if (q >= L) break;
+                        const int64_t p = base + (int64_t)q * inner;
+                        if (bg[u]) prev = q;
+                        gout[p] = prev < 0 ? kReInf : (q - prev) * (q - prev);
+                        fout[p] = prev < 0 ? -1 : (int32_t)(lbase + (int64_t)prev * inner);
+                    }
                 }
                 // backward sweep: the first background after q, taken only when strictly closer
                 int next = -1;
-                for (int q = L - 1; q >= 0; q--) {
-                    const int64_t p = base + (int64_t)q * inner;
-                    const int32_t gq = gout[p];
-                    if (gq == 0) {
-                        next = q;
-                    } else if (next >= 0) {
-                        const int32_t gn = (next - q) * (next - q);
-                        if (gn < gq) {
-                            gout[p] = gn;
-                            fout[p] = (int32_t)(lbase + (int64_t)next * inner);
+                for (int q0 = ((L - 1) / 8) * 8; q0 >= 0; q0 -= 8) {
+                    int32_t gv[8];
+#pragma unroll
+                    for (int u = 0; u < 8; u++)
+                        gv[u] = q0 + u < L ? gout[base + (int64_t)(q0 + u) * inner] : kReInf;
+#pragma unroll
+                    for (int u = 7; u >= 0; u--) {
+                        const int q = q0 + u;
+                        if (q >= L) continue;
+                        if (gv[u] == 0) {
+                            next = q;
+                        } else if (next >= 0) {
+                            const int32_t gn = (next - q) * (next - q);
+                            if (gn < gv[u]) {
+                                const int64_t p = base + (int64_t)q * inner;
+                                gout[p] = gn;
+                                fout[p] = (int32_t)(lbase + (int64_t)next * inner);
+                            }
                         }
                     }
                 }
                 continue;
             }
-            // lower envelope of the parabolas (q - p)^2 + g(p) over the finite g
-            const bool smem = L <= kReSmemL;
+            // lower envelope of the parabolas (q - p)^2 + g(p) over the finite g;
+            // the two topmost entries (position, g + position^2) stay in registers
+            const bool smem = L <= A.smem_l;
             auto push = [&](int k, int v) {
                 if (smem) re_stack[k * kReThreads + threadIdx.x] = (int16_t)v;
                 else A.gstack[base + (int64_t)k * inner] = (int16_t)v;
@@ -217,46 +194,76 @@ __global__ void __launch_bounds__(kReThreads) ragged_edt_kernel(ReArgs A) {
             };
             // the previous pass's planes were written by other SMs: L2 loads, never a stale L1 line
             auto G = [&](int q) -> int32_t { return __ldcg(gin + base + (int64_t)q * inner); };
-            int k = -1;
-            for (int q = 0; q < L; q++) {
-                const int32_t gq = G(q);
-                if (gq == kReInf) continue;
-                const int64_t Gq = (int64_t)gq + (int64_t)q * q;
-                while (k >= 1) {
-                    const int r = peek(k), pp = peek(k - 1);
-                    const int64_t Gr = (int64_t)G(r) + (int64_t)r * r, Gp = (int64_t)G(pp) + (int64_t)pp * pp;
-                    // pop r when the intersection with q is at or left of the one with pp
-                    if ((Gq - Gr) * (r - pp) <= (Gr - Gp) * (q - r)) k--;
-                    else break;
+            int k = -1, top = 0, sec = 0;
+            int64_t Gtop = 0, Gsec = 0;
+            for (int q0 = 0; q0 < L; q0 += 8) {
+                int32_t gv[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) gv[u] = q0 + u < L ? G(q0 + u) : kReInf;
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int q = q0 + u;
+                    if (gv[u] == kReInf) continue;  // also every q >= L
+                    const int64_t Gq = (int64_t)gv[u] + (int64_t)q * q;
+                    while (k >= 1) {
+                        // pop top when the intersection with q is at or left of the one with sec
+                        if ((Gq - Gtop) * (top - sec) > (Gtop - Gsec) * (q - top)) break;
+                        k--;
+                        top = sec;
+                        Gtop = Gsec;
+                        if (k >= 1) {
+                            sec = peek(k - 1);
+                            Gsec = (int64_t)G(sec) + (int64_t)sec * sec;
+                        }
+                    }
+                    push(++k, q);
+                    sec = top;
+                    Gsec = Gtop;
+                    top = q;
+                    Gtop = Gq;
                 }
-                push(++k, q);
             }
-            int j = 0;
+            // walk the envelope: cur and the next entry with their g in registers
+            int j = 0, cur = 0, nxt = 0;
+            int64_t gcur = 0, gnxt = 0;
+            int32_t fcur = -1;
+            if (k >= 0) {
+                cur = peek(0);
+                gcur = G(cur);
+                fcur = __ldcg(fin + base + (int64_t)cur * inner);
+                if (k >= 1) {
+                    nxt = peek(1);
+                    gnxt = G(nxt);
+                }
+            }
             for (int q = 0; q < L; q++) {
                 const int64_t p = base + (int64_t)q * inner;
-                int32_t fq = -1;
                 int64_t s = kReInf;
                 if (k >= 0) {
+                    s = (int64_t)(q - cur) * (q - cur) + gcur;
                     while (j < k) {
-                        const int x0 = peek(j), x1 = peek(j + 1);
-                        const int64_t a0 = (int64_t)(q - x0) * (q - x0) + G(x0);
-                        const int64_t a1 = (int64_t)(q - x1) * (q - x1) + G(x1);
-                        if (a1 < a0) j++;
-                        else break;
+                        const int64_t sn = (int64_t)(q - nxt) * (q - nxt) + gnxt;
+                        if (!(sn < s)) break;  // ties keep the lower position
+                        j++;
+                        cur = nxt;
+                        gcur = gnxt;
+                        s = sn;
+                        fcur = __ldcg(fin + base + (int64_t)cur * inner);
+                        if (j < k) {
+                            nxt = peek(j + 1);
+                            gnxt = G(nxt);
+                        }
                     }
-                    const int x = peek(j);
-                    s = (int64_t)(q - x) * (q - x) + G(x);
-                    fq = __ldcg(fin + base + (int64_t)x * inner);
                 }
                 if (!last) {
                     gout[p] = s >= kReInf ? kReInf : (int32_t)s;
-                    fout[p] = fq;
+                    fout[p] = k >= 0 ? fcur : -1;
                 } else {
-                    re_write(A, it, p, lbase + (int64_t)q * inner, fq, s);
+                    re_write(A, it, p, lbase + (int64_t)q * inner, k >= 0 ? fcur : -1, s);
                 }
             }
         }
-        if (!last && !re_barrier(A.ctl, A.status, A.spin_limit)) return;
+        if (!last && !grid_barrier_bounded(A.ctl, A.status, A.spin_limit)) return;
     }
 }
 
@@ -282,7 +289,7 @@ extern "C" int tm_ragged_edt_plan(int64_t n_items, int ndim, const int64_t *shap
     std::vector<unsigned char> host(tm_ragged_edt_plan_size(n_items), 0);
     auto *hdr = reinterpret_cast<RePlanHeader *>(host.data());
     auto *items = reinterpret_cast<ReItem *>(host.data() + sizeof(RePlanHeader));
-    int64_t lines[3] = {0, 0, 0}, total = 0, max_line = 0;
+    int64_t lines[3] = {0, 0, 0}, total = 0, max_line = 0, planes = 0;
     for (int64_t i = 0; i < n_items; i++) {
         int64_t n = 1, sq = 0;
         for (int d = 0; d < ndim; d++) {
@@ -299,6 +306,9 @@ extern "C" int tm_ragged_edt_plan(int64_t n_items, int ndim, const int64_t *shap
         if (offsets[i] < 0) return fail(TM_ERR_INVALID_ARGUMENT, "negative offset for item %lld", (long long)i);
         items[i].off = offsets[i];
         for (int d = 0; d < 3; d++) items[i].shape[d] = d < ndim ? (int)shapes[i * ndim + d] : 1;
+        if (planes >= ((int64_t)1 << 31)) return fail(TM_ERR_TOO_LARGE, "more than 2^31 - 1 planes");
+        items[i].plane_begin = (int)planes;
+        planes += shapes[i * ndim];
         for (int d = 0; d < ndim; d++) {
             items[i].line_begin[d] = lines[d];
             lines[d] += n / shapes[i * ndim + d];
@@ -321,7 +331,7 @@ extern "C" size_t tm_ragged_edt_workspace_size(int64_t total, int64_t max_line) 
     using namespace tmc;
     if (total < 1) return 0;
     const size_t n = (size_t)total;
-    return 4 * align256(n * 4) + (max_line > kReSmemL ? align256(n * 2) : 0) + sizeof(ReControl);
+    return 4 * align256(n * 4) + (max_line > kReSmemL ? align256(n * 2) : 0) + sizeof(GridControl);
 }
 
 extern "C" int tm_ragged_edt(const void *input, int in_dtype, const void *plan, size_t plan_bytes, int64_t n_items,
@@ -361,27 +371,36 @@ extern "C" int tm_ragged_edt(const void *input, int in_dtype, const void *plan, 
     size_t off = 4 * align256(n * 4);
     A.gstack = max_line > kReSmemL ? reinterpret_cast<int16_t *>(ws + off) : nullptr;
     if (A.gstack) off += align256(n * 2);
-    A.ctl = reinterpret_cast<ReControl *>(ws + off);
+    A.ctl = reinterpret_cast<GridControl *>(ws + off);
     A.dist = dist;
     A.indices = indices;
     A.sqdist = sqdist;
     int st = device_status_word(&A.status);
     if (st != TM_OK) return st;
     A.spin_limit = grid_wait_budget();
-    const size_t smem = (size_t)kReSmemL * kReThreads * sizeof(int16_t);
+    // the shared stack region holds the longest line's stack (up to 256 entries),
+    // so short lines leave room for more CTAs per SM
+    if (ndim == 3 && max_line <= ragged_edt3_max_line())  // every plane fits on chip
+        return ragged_edt3_run(input, A.in_f32, A.items, A.nitems, A.lines[0], total, (int)max_line,
+                               reinterpret_cast<int16_t *>(A.g[0]), dist, indices, sqdist, A.ctl, s);
+    A.smem_l = (int)std::min<int64_t>(max_line, kReSmemL);
+    const size_t smem = (size_t)A.smem_l * kReThreads * sizeof(int16_t);
     static thread_local int cached_dev = -1, cached_per_sm = 0;
+    static thread_local size_t cached_smem = 0;
     int dev = 0;
     TM_CHECK_CUDA(cudaGetDevice(&dev));
-    if (cached_dev != dev) {
-        TM_CHECK_CUDA(cudaFuncSetAttribute(ragged_edt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (cached_dev != dev || cached_smem != smem) {
+        TM_CHECK_CUDA(cudaFuncSetAttribute(ragged_edt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)((size_t)kReSmemL * kReThreads * sizeof(int16_t))));
         TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_per_sm, ragged_edt_kernel, kReThreads,
                                                                     smem));
         cached_dev = dev;
+        cached_smem = smem;
     }
     if (cached_per_sm < 1) return fail(TM_ERR_UNSUPPORTED, "ragged EDT kernel does not fit on an SM");
     const int64_t blocks =
         std::max<int64_t>(1, std::min<int64_t>((int64_t)cached_per_sm * sm_count(), ceil_div(max_lines, kReThreads)));
-    TM_CHECK_CUDA(cudaMemsetAsync(A.ctl, 0, sizeof(ReControl), s));
+    TM_CHECK_CUDA(cudaMemsetAsync(A.ctl, 0, sizeof(GridControl), s));
     void *params[] = {&A};
     TM_CHECK_CUDA(cudaLaunchCooperativeKernel((const void *)ragged_edt_kernel, dim3((unsigned)blocks),
                                               dim3(kReThreads), params, smem, s));

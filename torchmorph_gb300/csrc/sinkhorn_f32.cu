@@ -51,6 +51,12 @@ __device__ __forceinline__ float ex2(float x) {
     return y;
 }
 
+// Cost of the d points 0, 1, ..., d - 1 on a line, the reference's default
+// cost (build_cost_matrix((d,), p) for p = 1 or 2): |i - j|, exact in float32.
+// A NULL cost matrix selects it; entries are then computed where they are
+// used and no (d, d) matrix is ever stored or read.
+__device__ __forceinline__ float line_cost(int i, int j) { return (float)(i > j ? i - j : j - i); }
+
 struct SkControl {
     unsigned barrier_count;
     unsigned barrier_gen;
@@ -66,6 +72,7 @@ struct SkArgs {
     float *u, *v;                // scalings or log-scalings, updated in place
     int n, d;
     float mscale;                // log form: -log2(e) / eps applied to staged matrix entries
+    float inv_eps;               // scaling form with the line cost: K = exp(-|i - j| * inv_eps)
     int max_iter, check_every;   // check_every = 0: no residual checks
     float threshold;
     double *partial;             // [row blocks][n] residual partial sums
@@ -148,7 +155,17 @@ __device__ void sk_tile(const SkArgs &A, SkStage &st, int i0, int b0, const floa
             const int row = f >> 2, q = f & 3;
             const int i = i0 + row, j = j0 + 4 * q;
             float4 x = make_float4(fill, fill, fill, fill);
-            if (i < d) {
+            if (!mat) {  // the line cost (symmetric: the same for K and K^T)
+                if (i < d) {
+                    float c[4];
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        c[e] = fill;
+                        if (j + e < d) c[e] = LOG ? line_cost(i, j + e) : expf(-line_cost(i, j + e) * A.inv_eps);
+                    }
+                    x = make_float4(c[0], c[1], c[2], c[3]);
+                }
+            } else if (i < d) {
                 const float *src = mat + (size_t)i * d + j;
                 if (A.vec) {
                     if (j < d) x = *reinterpret_cast<const float4 *>(src);
@@ -423,7 +440,7 @@ __global__ void __launch_bounds__(kSkThreads)
         for (int f = tid; f < kSkRows * kSkChunk; f += kSkThreads) {
             const int row = f / kSkChunk, col = f % kSkChunk;
             const int i = i0 + row, j = j0 + col;
-            sc[row * kSkPitch + col] = (i < d && j < d) ? C[(size_t)i * d + j] : 0.0f;
+            sc[row * kSkPitch + col] = (i < d && j < d) ? (C ? C[(size_t)i * d + j] : line_cost(i, j)) : 0.0f;
         }
         for (int f = tid; f < TB * kSkChunk; f += kSkThreads) {
             const int p = f / kSkChunk, col = f % kSkChunk;
@@ -492,12 +509,14 @@ __global__ void sk_plan_kernel(const float *__restrict__ lu, const float *__rest
     for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
         const int b = (int)(row / d), i = (int)(row % d);
         const float x = lu[row];
-        const float *crow = C + (size_t)i * d;
+        const float *crow = C ? C + (size_t)i * d : nullptr;
         const float *vrow = lv + (size_t)b * d;
         float *prow = plan + (size_t)row * d;
         if (vec) {
             for (int j = 4 * threadIdx.x; j < d; j += 4 * blockDim.x) {
-                const float4 c = *reinterpret_cast<const float4 *>(crow + j);
+                const float4 c = crow ? *reinterpret_cast<const float4 *>(crow + j)
+                                      : make_float4(line_cost(i, j), line_cost(i, j + 1), line_cost(i, j + 2),
+                                                    line_cost(i, j + 3));
                 const float4 v = *reinterpret_cast<const float4 *>(vrow + j);
                 float4 o;
                 o.x = expf(__fadd_rn(__fsub_rn(x, __fmul_rn(c.x, inv_eps)), v.x));
@@ -507,7 +526,10 @@ __global__ void sk_plan_kernel(const float *__restrict__ lu, const float *__rest
                 *reinterpret_cast<float4 *>(prow + j) = o;
             }
         } else {
-            for (int j = threadIdx.x; j < d; j += blockDim.x) prow[j] = expf(__fadd_rn(__fsub_rn(x, __fmul_rn(crow[j], inv_eps)), vrow[j]));
+            for (int j = threadIdx.x; j < d; j += blockDim.x) {
+                const float c = crow ? crow[j] : line_cost(i, j);
+                prow[j] = expf(__fadd_rn(__fsub_rn(x, __fmul_rn(c, inv_eps)), vrow[j]));
+            }
         }
     }
 }
@@ -537,7 +559,7 @@ __global__ void __launch_bounds__(kSkThreads)
 #pragma unroll
         for (int s = 0; s < 4; s++) {
             const int i = i0 + ti + 16 * r, j = j0 + tj + 16 * s;
-            mc[r][s] = (i < d && j < d) ? C[(size_t)i * d + j] * mscale : -INFINITY;
+            mc[r][s] = (i < d && j < d) ? (C ? C[(size_t)i * d + j] : line_cost(i, j)) * mscale : -INFINITY;
             acc[r][s] = 0.0f;
         }
     for (int p0 = 0; p0 < n; p0 += kGradPairs) {
@@ -621,16 +643,16 @@ struct SkLayout {
     size_t mat, mat_t, su, sv, partial, err, notconv, ctl, cost_part, err_part, total;
 };
 
-SkLayout sk_layout(int64_t n, int64_t d, bool log_form, int64_t max_iter, int64_t check_every) {
+SkLayout sk_layout(int64_t n, int64_t d, bool log_form, int64_t max_iter, int64_t check_every, bool line) {
     SkLayout L{};
     const size_t dd = (size_t)d * d * sizeof(float), nd = (size_t)n * d * sizeof(float);
     const size_t rblocks = (size_t)ceil_div(d, kSkRows);
     const size_t checks = check_every > 0 ? (size_t)(max_iter / check_every) + 1 : 1;
     size_t off = 0;
     L.mat = off;
-    off += log_form ? 0 : align256(dd);  // K (the log form reads C itself)
+    off += (log_form || line) ? 0 : align256(dd);  // K (the log form reads C itself)
     L.mat_t = off;
-    off += align256(dd);
+    off += line ? 0 : align256(dd);  // the line cost is computed where it is used
     L.su = off;
     off += align256(nd);  // u (scaling) or log a
     L.sv = off;
@@ -729,9 +751,9 @@ extern "C" int tm_sinkhorn_logiter(const float *log_a, const float *log_b, const
 }
 
 extern "C" size_t tm_sinkhorn_f32_workspace_size(int64_t n, int64_t d, int log_space, int64_t max_iter,
-                                                 int64_t check_every) {
+                                                 int64_t check_every, int line_cost) {
     if (n < 1 || d < 1 || max_iter < 0) return 0;
-    return tmc::sk_layout(n, d, log_space != 0, max_iter, check_every).total;
+    return tmc::sk_layout(n, d, log_space != 0, max_iter, check_every, line_cost != 0).total;
 }
 
 extern "C" int tm_sinkhorn_f32_solve(const float *a, const float *b, const float *C, int64_t n, int64_t d,
@@ -740,30 +762,34 @@ extern "C" int tm_sinkhorn_f32_solve(const float *a, const float *b, const float
                                      int32_t *iterations, void *workspace, size_t workspace_bytes,
                                      tm_stream_t stream) {
     using namespace tmc;
-    const void *ptrs[] = {a, b, C, log_u, log_v};
-    const char *names[] = {"a", "b", "C", "log_u", "log_v"};
-    for (int k = 0; k < 5; k++)
+    const void *ptrs[] = {a, b, log_u, log_v};
+    const char *names[] = {"a", "b", "log_u", "log_v"};
+    for (int k = 0; k < 4; k++)
         if (check_ptr(ptrs[k], names[k]) != TM_OK) return TM_ERR_INVALID_ARGUMENT;
     int st = check_nd(n, d);
     if (st != TM_OK) return st;
     if (!(epsilon > 0)) return fail(TM_ERR_INVALID_ARGUMENT, "epsilon must be positive, got %g", epsilon);
     if (max_iter < 1 || max_iter > (1LL << 30)) return fail(TM_ERR_INVALID_ARGUMENT, "max_iter must be in [1, 2^30]");
+    const bool line = C == nullptr;  // the cost of d points on a line, computed where used
     if (threshold < 0) return fail(TM_ERR_INVALID_ARGUMENT, "threshold must be >= 0");
     if (threshold > 0 && check_every < 1) return fail(TM_ERR_INVALID_ARGUMENT, "check_every must be >= 1");
     if (threshold == 0) check_every = 0;
     const bool log_form = log_space != 0;
-    const SkLayout L = sk_layout(n, d, log_form, max_iter, check_every);
+    const SkLayout L = sk_layout(n, d, log_form, max_iter, check_every, line);
     if (!workspace || workspace_bytes < L.total || ((uintptr_t)workspace & 255))
         return fail(TM_ERR_WORKSPACE, "workspace must be 256-byte aligned and hold %zu bytes", L.total);
     cudaStream_t s = (cudaStream_t)stream;
     const size_t nd = (size_t)n * d;
     float *su = ws_at<float>(workspace, L.su), *sv = ws_at<float>(workspace, L.sv);
-    float *mat_t = ws_at<float>(workspace, L.mat_t);
+    float *mat_t = line ? nullptr : ws_at<float>(workspace, L.mat_t);
     const dim3 tgrid((unsigned)ceil_div(d, 32), (unsigned)ceil_div(d, 32)), tblock(32, 8);
     SkArgs A{};
+    A.inv_eps = 1.0f / (float)epsilon;
     if (log_form) {
-        sk_prepare_kernel<false><<<tgrid, tblock, 0, s>>>(C, nullptr, mat_t, (int)d, 0.0f);
-        TM_LAUNCH_CHECK("sk_prepare_kernel");
+        if (!line) {
+            sk_prepare_kernel<false><<<tgrid, tblock, 0, s>>>(C, nullptr, mat_t, (int)d, 0.0f);
+            TM_LAUNCH_CHECK("sk_prepare_kernel");
+        }
         sk_log_kernel<<<grid_for(nd), 256, 0, s>>>(a, su, b, sv, nd);  // log a, log b
         TM_LAUNCH_CHECK("sk_log_kernel");
         sk_fill_kernel<<<grid_for(nd), 256, 0, s>>>(log_u, log_v, nd, 0.0f);
@@ -775,9 +801,11 @@ extern "C" int tm_sinkhorn_f32_solve(const float *a, const float *b, const float
         A.v = log_v;
         A.mscale = (float)(-1.4426950408889634 / epsilon);
     } else {
-        float *K = ws_at<float>(workspace, L.mat);
-        sk_prepare_kernel<true><<<tgrid, tblock, 0, s>>>(C, K, mat_t, (int)d, 1.0f / (float)epsilon);
-        TM_LAUNCH_CHECK("sk_prepare_kernel");
+        float *K = line ? nullptr : ws_at<float>(workspace, L.mat);
+        if (!line) {
+            sk_prepare_kernel<true><<<tgrid, tblock, 0, s>>>(C, K, mat_t, (int)d, 1.0f / (float)epsilon);
+            TM_LAUNCH_CHECK("sk_prepare_kernel");
+        }
         sk_fill_kernel<<<grid_for(nd), 256, 0, s>>>(su, sv, nd, 1.0f);
         TM_LAUNCH_CHECK("sk_fill_kernel");
         A.num_u = a;
@@ -816,9 +844,9 @@ extern "C" int tm_sinkhorn_f32_solve(const float *a, const float *b, const float
 extern "C" int tm_sinkhorn_plan(const float *log_u, const float *log_v, const float *C, int64_t n, int64_t d,
                                 double epsilon, float *plan, tm_stream_t stream) {
     using namespace tmc;
-    const void *ptrs[] = {log_u, log_v, C, plan};
-    const char *names[] = {"log_u", "log_v", "C", "plan"};
-    for (int k = 0; k < 4; k++)
+    const void *ptrs[] = {log_u, log_v, plan};
+    const char *names[] = {"log_u", "log_v", "plan"};
+    for (int k = 0; k < 3; k++)
         if (check_ptr(ptrs[k], names[k]) != TM_OK) return TM_ERR_INVALID_ARGUMENT;
     int st = check_nd(n, d);
     if (st != TM_OK) return st;
@@ -835,9 +863,9 @@ extern "C" int tm_sinkhorn_cost_grad(const float *log_u, const float *log_v, con
                                      const float *grad_distance, int64_t n, int64_t d, double epsilon,
                                      float *grad_C, tm_stream_t stream) {
     using namespace tmc;
-    const void *ptrs[] = {log_u, log_v, C, grad_distance, grad_C};
-    const char *names[] = {"log_u", "log_v", "C", "grad_distance", "grad_C"};
-    for (int k = 0; k < 5; k++)
+    const void *ptrs[] = {log_u, log_v, grad_distance, grad_C};
+    const char *names[] = {"log_u", "log_v", "grad_distance", "grad_C"};
+    for (int k = 0; k < 4; k++)
         if (check_ptr(ptrs[k], names[k]) != TM_OK) return TM_ERR_INVALID_ARGUMENT;
     int st = check_nd(n, d);
     if (st != TM_OK) return st;

@@ -129,7 +129,7 @@ int encode_tensor_map(CUtensorMap *map, CUtensorMapDataType dtype, int rank, con
 // --------------------------------------------------------------- autotuning
 // Variant table: (operator, work class) -> variant, -1 = built-in choice.
 constexpr int kTuneClasses = 64;
-static const int kTuneVariants[kTuneOps] = {4, 4, 2, 2};
+static const int kTuneVariants[kTuneOps] = {4, 4, 2, 3};
 static std::atomic<int> g_tune[kTuneOps][kTuneClasses];
 static std::once_flag g_tune_once;
 

@@ -33,6 +33,57 @@ constexpr long long kSpinLimit = 1LL << 26;
 // tensor-core work in flight always use kSpinLimit.
 long long grid_wait_budget();
 
+// Control block of a cooperative launch whose CTAs meet at grid barriers;
+// zeroed before the launch.
+struct GridControl {
+    unsigned count;  // CTAs arrived at the current barrier
+    unsigned gen;    // barriers completed
+    int abort;       // set by a CTA whose wait gave up: every CTA leaves
+    int pad[61];
+};
+static_assert(sizeof(GridControl) == 256, "control block is 256 bytes");
+
+// Barrier of all CTAs of a cooperative launch (all co-resident).  The last
+// CTA to arrive resets the count and advances the generation; the others
+// poll the generation at most spin_limit times.  A wait that gives up (or
+// sees another CTA's abort) sets the abort flag and TM_DEV_ERR_TIMEOUT in
+// `status`; the barrier then returns false in every CTA that reaches it, and
+// the caller returns.  Writes before the barrier are visible to loads after
+// it that bypass L1 (__ldcg, or data this CTA has not cached).
+__device__ inline bool grid_barrier_bounded(GridControl *ctl, int *status, long long spin_limit) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = &ctl->gen;
+        volatile int *abort = &ctl->abort;
+        const unsigned g = *gen;
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(&ctl->count, 1u) == gridDim.x - 1) {
+            ctl->count = 0;
+            __threadfence();
+            atomicAdd(&ctl->gen, 1u);
+        } else {
+            long long polls = 0;
+            while (*gen == g) {
+                if (*abort || ++polls > spin_limit) {
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        if (!ok) {
+            atomicExch(&ctl->abort, 1);
+            if (status) atomicExch(status, TM_DEV_ERR_TIMEOUT);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }

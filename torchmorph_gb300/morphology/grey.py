@@ -143,9 +143,22 @@ def grey_dilation(input, size=None, footprint=None, structure=None, output=None,
                             operation="dilation", differentiable=differentiable)
 
 
+def _fused(kind, input, output, differentiable, size, footprint, structure, mode, cval, origin):
+    """The one-pass composite of 1-D / 2-D items with flat boxes (None elsewhere, and
+    for differentiable calls, which compose the operators)."""
+    validate_bcs_input(input)
+    validate_output(input, output)
+    if differentiable and input.requires_grad and torch.is_grad_enabled():
+        return None
+    return _one_pass(kind, input, size, footprint, structure, mode, cval, origin)
+
+
 def grey_opening(input, size=None, footprint=None, structure=None, output=None, mode="reflect",
                  cval=0.0, origin=0, *, differentiable=False) -> Tensor:
-    """Grey opening: dilation of the erosion."""
+    """Grey opening: dilation of the erosion (1-D / 2-D flat boxes: one pass)."""
+    res = _fused("opening", input, output, differentiable, size, footprint, structure, mode, cval, origin)
+    if res is not None:
+        return _finish(res, output)
     kw = _element_kwargs(size, footprint, structure, mode, cval, origin)
     return grey_dilation(grey_erosion(input, differentiable=differentiable, **kw), output=output,
                          differentiable=differentiable, **kw)
@@ -153,7 +166,10 @@ def grey_opening(input, size=None, footprint=None, structure=None, output=None, 
 
 def grey_closing(input, size=None, footprint=None, structure=None, output=None, mode="reflect",
                  cval=0.0, origin=0, *, differentiable=False) -> Tensor:
-    """Grey closing: erosion of the dilation."""
+    """Grey closing: erosion of the dilation (1-D / 2-D flat boxes: one pass)."""
+    res = _fused("closing", input, output, differentiable, size, footprint, structure, mode, cval, origin)
+    if res is not None:
+        return _finish(res, output)
     kw = _element_kwargs(size, footprint, structure, mode, cval, origin)
     return grey_erosion(grey_dilation(input, differentiable=differentiable, **kw), output=output,
                         differentiable=differentiable, **kw)
@@ -188,18 +204,20 @@ def morphological_gradient(input, size=None, footprint=None, structure=None, out
 
 def white_tophat(input, size=None, footprint=None, structure=None, output=None, mode="reflect",
                  cval=0.0, origin=0) -> Tensor:
-    """Input minus its grey opening."""
-    validate_bcs_input(input)
-    validate_output(input, output)
+    """Input minus its grey opening (1-D / 2-D flat boxes: one pass)."""
+    res = _fused("white_tophat", input, output, False, size, footprint, structure, mode, cval, origin)
+    if res is not None:
+        return _finish(res, output)
     opened = grey_opening(input, **_element_kwargs(size, footprint, structure, mode, cval, origin))
     return _finish(input.detach().float() - opened, output)
 
 
 def black_tophat(input, size=None, footprint=None, structure=None, output=None, mode="reflect",
                  cval=0.0, origin=0) -> Tensor:
-    """Grey closing minus the input."""
-    validate_bcs_input(input)
-    validate_output(input, output)
+    """Grey closing minus the input (1-D / 2-D flat boxes: one pass)."""
+    res = _fused("black_tophat", input, output, False, size, footprint, structure, mode, cval, origin)
+    if res is not None:
+        return _finish(res, output)
     closed = grey_closing(input, **_element_kwargs(size, footprint, structure, mode, cval, origin))
     return _finish(closed - input.detach().float(), output)
 

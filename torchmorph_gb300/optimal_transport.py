@@ -67,6 +67,21 @@ def _use_tensor_cores(a: Tensor, cost_matrix: Tensor, tensor_cores) -> bool:
     return bool(tensor_cores)
 
 
+# Largest d for which build_cost_matrix((d,), p=2) is exactly |i - j| in float32 (its
+# matrix-product evaluation keeps i^2 + j^2 below 2^24); p = 1 is exact for every d.
+_LINE_EXACT_P2 = 2896
+
+
+def _line_cost_ok(a: Tensor, p, tensor_cores) -> bool:
+    """The FP32 device solver takes the default cost (points 0 .. d-1 on a line) without a
+    matrix when it equals build_cost_matrix((d,), p) bit for bit."""
+    d = a.shape[1]
+    if not _on_device(a) or p not in (1, 2) or (p == 2 and d > _LINE_EXACT_P2):
+        return False
+    eye = torch.empty((d, d), device="meta")  # shape only: the tensor-core choice needs no values
+    return not _use_tensor_cores(a, eye, tensor_cores)
+
+
 def _device_solve(a, b, cost_matrix, epsilon, max_iter, threshold, log_space, tensor_cores):
     """One libtmcore call: the whole solve, its transport cost and residual."""
     from . import _C
@@ -190,18 +205,26 @@ class SinkhornSolver(nn.Module):
 
     def data_preprocess(self, source, target, cost_matrix: Optional[Tensor] = None):
         """Validate (n, d) inputs, clamp negatives and normalise each row to unit mass."""
+        return self._preprocess(source, target, cost_matrix, build=True)
+
+    def _preprocess(self, source, target, cost_matrix, build):
+        """data_preprocess; with build=False and no cost_matrix, the returned cost is None
+        when the device solver computes the default line cost itself."""
         if source.ndim != 2 or source.shape != target.shape:
             raise ValueError("source and target must be (n, d) tensors of the same shape.")
         if not source.is_floating_point():
             raise ValueError("source and target must be floating-point tensors.")
         d = source.shape[1]
-        if cost_matrix is None:
+        if cost_matrix is None and not build and _line_cost_ok(source, self.p, self.tensor_cores):
+            pass
+        elif cost_matrix is None:
             cost_matrix = build_cost_matrix((d,), self.p, source.device)
         elif cost_matrix.shape != (d, d):
             raise ValueError(
                 f"cost_matrix must have shape ({d}, {d}), got {tuple(cost_matrix.shape)}."
             )
-        cost_matrix = cost_matrix.to(device=source.device, dtype=source.dtype).contiguous()
+        if cost_matrix is not None:
+            cost_matrix = cost_matrix.to(device=source.device, dtype=source.dtype).contiguous()
         source = source.clamp(min=0)
         target = target.clamp(min=0)
         source = source / source.sum(dim=-1, keepdim=True).clamp(min=1e-12)
@@ -224,10 +247,11 @@ class SinkhornSolver(nn.Module):
                 (r is None and t is None) or (r is not None and r() is t) for r, t in zip(last[1], inputs)):
             return last[3]
         with torch.no_grad():
-            a, b, c = a.detach(), b.detach(), cost_matrix.detach()
+            a, b = a.detach(), b.detach()
+            c = None if cost_matrix is None else cost_matrix.detach()
             if _on_device(a):
                 result = _device_solve(a, b, c, self.epsilon, self.max_iter, self.threshold, self.log_space,
-                                       _use_tensor_cores(a, c, self.tensor_cores))
+                                       c is not None and _use_tensor_cores(a, c, self.tensor_cores))
             else:
                 if self.tensor_cores:
                     _use_tensor_cores(a, c, True)  # raises: tensor cores need CUDA float32
@@ -241,7 +265,7 @@ class SinkhornSolver(nn.Module):
     def forward(self, source: Tensor, target: Tensor, cost_matrix: Optional[Tensor] = None):
         """(n,) transport distances <P, C> between the rows of source and target."""
         inputs = (source, target, cost_matrix)
-        a, b, c = self.data_preprocess(source, target, cost_matrix)
+        a, b, c = self._preprocess(source, target, cost_matrix, build=False)
         sol = self._solve(inputs, a, b, c)
         return _SinkhornDistance.apply(a, b, c, self.epsilon, sol.log_u, sol.log_v, sol.cost)
 
@@ -252,7 +276,7 @@ class SinkhornSolver(nn.Module):
         between the plan's row sums and the source histogram, in float64 -- and
         ``iterations`` (an int; reading it synchronises with the device)."""
         inputs = (source, target, cost_matrix)
-        source, target, cost_matrix = self.data_preprocess(source, target, cost_matrix)
+        source, target, cost_matrix = self._preprocess(source, target, cost_matrix, build=False)
         sol = self._solve(inputs, source, target, cost_matrix)
         if sol.cost is not None:
             distance, row_err = sol.cost.to(source.dtype), sol.row_err
@@ -272,7 +296,7 @@ class SinkhornSolver(nn.Module):
         reference's operations and rounding; CUDA float32 plans are written by one
         kernel pass."""
         inputs = (source, target, cost_matrix)
-        source, target, cost_matrix = self.data_preprocess(source, target, cost_matrix)
+        source, target, cost_matrix = self._preprocess(source, target, cost_matrix, build=False)
         sol = self._solve(inputs, source, target, cost_matrix)
         return _plan(sol.log_u, sol.log_v, cost_matrix, self.epsilon)
 
@@ -280,7 +304,7 @@ class SinkhornSolver(nn.Module):
     def potentials(self, source: Tensor, target: Tensor, cost_matrix: Optional[Tensor] = None):
         """Centred dual potentials (f, g), each (n, d)."""
         inputs = (source, target, cost_matrix)
-        source, target, cost_matrix = self.data_preprocess(source, target, cost_matrix)
+        source, target, cost_matrix = self._preprocess(source, target, cost_matrix, build=False)
         sol = self._solve(inputs, source, target, cost_matrix)
         f = self.epsilon * sol.log_u
         g = self.epsilon * sol.log_v
