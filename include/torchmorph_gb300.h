@@ -205,6 +205,22 @@ int tm_binary_dilation(const uint8_t *in, uint8_t *out, int64_t batch, int ndim,
                        const int64_t *shape, const uint8_t *structure, const int64_t *sshape,
                        const int64_t *origin, int border_value, tm_stream_t stream);
 
+/* One-pass binary opening / closing (one iteration, no mask) of 1-D or 2-D
+ * items on bit-packed tiles: the first operator over the tile grown by the
+ * second's halo stays on chip, positions outside the item read border_value
+ * in both operators -- equal to the reference's two calls
+ * (torchmorph/morphology/binary.py:231-290).  Arguments as for
+ * tm_binary_erosion; TM_ERR_UNSUPPORTED when a structure offset reaches
+ * beyond 16 rows or 32 columns, where the caller composes the operators.
+ * 1-D / 2-D tm_binary_erosion / tm_binary_dilation with elements other than
+ * full boxes run on the same bit tiles. */
+int tm_binary_opening(const uint8_t *in, uint8_t *out, int64_t batch, int ndim, const int64_t *shape,
+                      const uint8_t *structure, const int64_t *sshape, const int64_t *origin,
+                      int border_value, tm_stream_t stream);
+int tm_binary_closing(const uint8_t *in, uint8_t *out, int64_t batch, int ndim, const int64_t *shape,
+                      const uint8_t *structure, const int64_t *sshape, const int64_t *origin,
+                      int border_value, tm_stream_t stream);
+
 /* ------------------------------------------------------------------- edt --
  * Replaces edt_cuda (torchmorph/csrc/torchmorph.cpp:35-40,
  * torchmorph/csrc/edt_kernel.cu:904-958).
@@ -292,6 +308,14 @@ int tm_ragged_binary_erosion(const uint8_t *in, uint8_t *out, const void *plan, 
 int tm_ragged_binary_dilation(const uint8_t *in, uint8_t *out, const void *plan, size_t plan_bytes,
                               int64_t n_items, const uint8_t *structure, const int64_t *sshape,
                               const int64_t *origin, int border_value, tm_stream_t stream);
+/* Ragged binary operators run on bit-packed tiles (as tm_binary_opening);
+ * the opening / closing in one pass. */
+int tm_ragged_binary_opening(const uint8_t *in, uint8_t *out, const void *plan, size_t plan_bytes,
+                             int64_t n_items, const uint8_t *structure, const int64_t *sshape,
+                             const int64_t *origin, int border_value, tm_stream_t stream);
+int tm_ragged_binary_closing(const uint8_t *in, uint8_t *out, const void *plan, size_t plan_bytes,
+                             int64_t n_items, const uint8_t *structure, const int64_t *sshape,
+                             const int64_t *origin, int border_value, tm_stream_t stream);
 
 /* Ragged batches of 3-D volumes (volume i: depths[i] x heights[i] x
  * widths[i] elements from element offsets[i]).  Each operator is ONE

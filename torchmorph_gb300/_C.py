@@ -191,6 +191,22 @@ def _binary(fn_name, input, structure, origin, border_value, out=None):
     return out
 
 
+def binary_composite(kind, input, structure, origin, border_value):
+    """One-pass binary opening / closing (one iteration) of 1-D / 2-D items on bit-packed
+    tiles (tm_binary_opening / tm_binary_closing); None when the structure is beyond the
+    kernel's limits, so that the caller composes the operators."""
+    name = {"opening": "tm_binary_opening", "closing": "tm_binary_closing"}[kind]
+    if structure.dim() > 2:
+        return None
+    out = torch.empty_like(input)
+    try:
+        return _binary(name, input, structure, origin, border_value, out)
+    except _lib.TorchmorphError as e:
+        if e.status == _TM_ERR_UNSUPPORTED:
+            return None
+        raise
+
+
 def binary_erosion_cuda(input, structure, origin, border_value):
     """N-dimensional fused binary erosion (reference binary_kernel.cu:252-261)."""
     return _binary("tm_binary_erosion", input, structure, origin, border_value)

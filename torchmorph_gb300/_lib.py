@@ -42,6 +42,10 @@ SIGNATURES = {
                                   c_void]),
     "tm_binary_dilation": (c_int, [c_void, c_void, c_i64, c_int, I64P, U8P, I64P, I64P, c_int,
                                    c_void]),
+    "tm_binary_opening": (c_int, [c_void, c_void, c_i64, c_int, I64P, U8P, I64P, I64P, c_int,
+                                  c_void]),
+    "tm_binary_closing": (c_int, [c_void, c_void, c_i64, c_int, I64P, U8P, I64P, I64P, c_int,
+                                  c_void]),
     "tm_edt_workspace_size": (c_size, [c_i64, c_int, I64P, F32P]),
     "tm_edt": (c_int, [c_void, c_int, c_i64, c_int, I64P, F32P, c_void, c_void, c_void, c_void,
                        c_size, c_void]),
@@ -130,6 +134,10 @@ SIGNATURES = {
                                          c_void]),
     "tm_ragged_binary_dilation": (c_int, [c_void, c_void, c_void, c_size, c_i64, U8P, I64P, I64P, c_int,
                                           c_void]),
+    "tm_ragged_binary_opening": (c_int, [c_void, c_void, c_void, c_size, c_i64, U8P, I64P, I64P, c_int,
+                                         c_void]),
+    "tm_ragged_binary_closing": (c_int, [c_void, c_void, c_void, c_size, c_i64, U8P, I64P, I64P, c_int,
+                                         c_void]),
 }
 
 TM_F32 = 0

@@ -1,0 +1,430 @@
+// Binary morphology of 1-D / 2-D items on bit-packed tiles (GB300, sm_103a):
+// erosion, dilation, and the opening / closing fused into one pass.
+//
+// The reference runs one byte per voxel through a tap loop, and its opening /
+// closing are two full launches with the intermediate image in HBM
+// (torchmorph/morphology/binary.py:231-290, csrc/binary_kernel.cu:56-127).
+// Here one CTA of 128 threads owns a 32 x 128 output tile (the ragged plan's
+// tile, ragged.cu) and keeps its input region as 32-voxel words:
+//  * staging: a warp reads 32 consecutive bytes of a row (one per lane,
+//    coalesced) and __ballot_sync packs them into one word; positions outside
+//    the item read border_value;
+//  * one operator on words: out = AND (erosion) / OR (dilation) over the taps
+//    of the 32-voxel row segment shifted by the tap -- one funnel shift and one
+//    logic operation per tap for 32 voxels;
+//  * fused opening / closing: the first operator over the tile grown by the
+//    second one's halo, kept in shared memory, positions outside the item set
+//    to border_value (the reference's intermediate image is read with
+//    border_value outside the item), then the second operator;
+//  * output: each lane writes one byte of a row segment (32 consecutive bytes
+//    per warp store).
+// Taps follow the reference's offsets (erosion reads x + d, dilation x - d,
+// d = k - (size // 2 + origin)); erosion with no taps inside the item still
+// ANDs border_value, exactly as the per-voxel loop does.  Limits: every tap
+// within 16 rows and 32 columns of the output, at most 1024 taps per
+// operator.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "bitmorph.cuh"
+#include "tile_queue.cuh"
+
+namespace tmc {
+namespace {
+
+constexpr int kBTileH = 32, kBTileW = 128, kBWords = kBTileW / 32;  // 4 words per tile row
+constexpr int kBThreads = kBTileH * kBWords;                           // one output word per thread
+constexpr int kBMaxTaps = 1024;
+constexpr int kBMaxDy = 16, kBMaxDx = 32;
+
+struct BitTaps {
+    int n;
+    int hy, hx;  // largest |dy| and |dx| of the read offsets
+    int8_t dy[kBMaxTaps], dx[kBMaxTaps];
+};
+
+struct BitOps {
+    BitTaps op[2];  // read offsets of the first and (fused) second operator
+    int nops;       // 1 or 2
+    int or1, or2;   // operator k is a dilation (OR) rather than an erosion (AND)
+    int border;     // border_value, 0 or 1
+};
+
+struct BitItem {  // the layout of ragged.cu's plan descriptors
+    int64_t off;
+    int H, W;
+    int tile_begin;
+    int tiles_x;
+    int pad[2];
+};
+
+struct BitPlanHeader {
+    int queue;
+    int ntiles;
+    int nitems;
+    int pad[61];
+};
+
+struct BitUniform {
+    int64_t batch;
+    int H, W;
+    int tiles_x, tiles_item;
+};
+
+__host__ __device__ inline int floor32(int v) { return v >= 0 ? v / 32 : -((-v + 31) / 32); }
+
+// Word ranges of a tile (word j of a row = columns x0 + 32 j .. + 31).  An
+// operator with column reach hx that computes words clo .. chi reads words
+// clo + floor32(-hx) .. chi + floor32(hx) + 1 (the + 1: the funnel shift's
+// high word).
+struct BitGeom {
+    int HY, srows, sjlo, sld;  // staged input: rows y0 - HY .., words sjlo .. sjlo + sld - 1
+    int irows, ijlo, ild;      // first operator's result (fused): rows y0 - hy2 .., words ijlo ..
+};
+
+__host__ __device__ inline BitGeom bit_geom(const BitOps &ops) {
+    const bool fused = ops.nops == 2;
+    const int hy1 = ops.op[0].hy, hx1 = ops.op[0].hx;
+    const int hy2 = fused ? ops.op[1].hy : 0, hx2 = fused ? ops.op[1].hx : 0;
+    int clo = 0, chi = kBWords - 1;  // words the first operator computes
+    if (fused) {
+        clo = floor32(-hx2);
+        chi = kBWords - 1 + floor32(hx2) + 1;
+    }
+    BitGeom g;
+    g.irows = kBTileH + 2 * hy2;
+    g.ijlo = clo;
+    g.ild = chi - clo + 1;
+    g.HY = hy1 + hy2;
+    g.srows = kBTileH + 2 * g.HY;
+    g.sjlo = clo + floor32(-hx1);
+    g.sld = chi + floor32(hx1) + 1 - g.sjlo + 1;
+    return g;
+}
+
+// One operator over a word array: out word (r, w) for rows r < nrows, words
+// wlo <= w <= whi of the output region; `src` holds rows with row offset
+// `srow` (source row of output row r and tap dy: r + srow + dy) and words from
+// `sjlo` (ld words per row).
+__device__ __forceinline__ uint32_t bit_op(const uint32_t *src, int ld, int sjlo, int srow, int r, int w,
+                                           const BitTaps &t, bool is_or) {
+    uint32_t acc = is_or ? 0u : ~0u;
+    for (int k = 0; k < t.n; k++) {
+        const int dx = t.dx[k];
+        const int q = floor32(dx), sh = dx - 32 * q;
+        const uint32_t *row = src + (r + srow + t.dy[k]) * ld + (w - sjlo + q);
+        const uint32_t v = sh ? __funnelshift_r(row[0], row[1], sh) : row[0];
+        acc = is_or ? (acc | v) : (acc & v);
+    }
+    return acc;
+}
+
+__global__ void __launch_bounds__(kBThreads) bitmorph_kernel(const uint8_t *__restrict__ in, uint8_t *__restrict__ out,
+                                                             BitPlanHeader *hdr, const BitItem *__restrict__ items,
+                                                             BitUniform u, const __grid_constant__ BitOps ops) {
+    extern __shared__ __align__(16) uint32_t bsm[];
+    __shared__ int s_slot[2];
+    __shared__ int s_tb[kQueueCache];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    TileQueue<BitItem> q{hdr ? &hdr->queue : nullptr, hdr ? hdr->ntiles : 0, hdr ? hdr->nitems : 0, items, s_tb,
+                         s_slot, 0};
+    if (hdr) q.init();
+    const BitTaps &t1 = ops.op[0];
+    const BitTaps &t2 = ops.op[1];
+    const bool fused = ops.nops == 2;
+    const int hy2 = fused ? t2.hy : 0;
+    const BitGeom g = bit_geom(ops);
+    const int HY = g.HY, srows = g.srows, sjlo = g.sjlo, sld = g.sld;
+    const int irows = g.irows, ijlo = g.ijlo, ild = g.ild;
+    uint32_t *S = bsm;
+    uint32_t *I = bsm + srows * sld;
+    const uint32_t bvw = ops.border ? ~0u : 0u;
+    const int64_t ntiles = hdr ? 0 : u.batch * (int64_t)u.tiles_item;
+    for (int64_t k = blockIdx.x;; k += gridDim.x) {
+        int lt, H, W, tiles_x;
+        int64_t off;
+        if (hdr) {
+            __syncthreads();  // the previous tile's readers are done with s_slot and the buffers
+            if (!q.take()) break;
+            const BitItem &v = items[s_slot[1]];
+            lt = s_slot[0] - v.tile_begin;
+            off = v.off;
+            H = v.H;
+            W = v.W;
+            tiles_x = v.tiles_x;
+        } else {
+            if (k >= ntiles) break;
+            __syncthreads();
+            const int64_t item = k / u.tiles_item;
+            lt = (int)(k - item * u.tiles_item);
+            H = u.H;
+            W = u.W;
+            off = item * (int64_t)H * W;
+            tiles_x = u.tiles_x;
+        }
+        const int ty = lt / tiles_x, tx = lt - ty * tiles_x;
+        const int y0 = ty * kBTileH, x0 = tx * kBTileW;
+        const uint8_t *src = in + off;
+        // ---- stage: one ballot per 32 bytes, 8 words of a row in flight per lane
+        for (int rw = warp; rw < srows; rw += kBThreads / 32) {
+            const int y = y0 - HY + rw;
+            const bool yin = (unsigned)y < (unsigned)H;
+            const uint8_t *row = src + (int64_t)y * W;
+            for (int j0 = 0; j0 < sld; j0 += 8) {
+                uint8_t b[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const int x = x0 + 32 * (sjlo + j0 + j) + lane;
+                    b[j] = (yin && (unsigned)x < (unsigned)W) ? row[x] : (uint8_t)ops.border;
+                }
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const uint32_t word = __ballot_sync(~0u, b[j] != 0);
+                    if (j0 + j < sld && lane == 0) S[rw * sld + j0 + j] = word;
+                }
+            }
+        }
+        __syncthreads();
+        uint32_t res = 0u;
+        const int r = tid / kBWords, w = tid % kBWords;
+        if (!fused) {
+            res = bit_op(S, sld, sjlo, HY, r, w, t1, ops.or1);
+        } else {
+            // first operator over the intermediate region, outside the item = border_value
+            for (int e = tid; e < irows * ild; e += kBThreads) {
+                const int ir = e / ild, iw = ijlo + e % ild;
+                const int y = y0 - hy2 + ir;
+                uint32_t v = bit_op(S, sld, sjlo, t1.hy, ir, iw, t1, ops.or1);
+                if ((unsigned)y >= (unsigned)H) {
+                    v = bvw;
+                } else {
+                    const int xb = x0 + 32 * iw;  // column of bit 0
+                    uint32_t inside = 0u;
+                    if (xb >= 0 && xb + 32 <= W) inside = ~0u;
+                    else if (xb + 32 > 0 && xb < W) {
+                        const int lo = max(0, -xb), hi = min(32, W - xb);  // bits lo .. hi-1 inside
+                        inside = (hi >= 32 ? ~0u : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
+                    }
+                    v = (v & inside) | (bvw & ~inside);
+                }
+                I[ir * ild + (iw - ijlo)] = v;
+            }
+            __syncthreads();
+            res = bit_op(I, ild, ijlo, hy2, r, w, t2, ops.or2);
+        }
+        // ---- output: lane writes byte `lane` of each of its warp's words
+        uint8_t *dst = out + off;
+        const int wr0 = warp * (32 / kBWords);  // first tile row of this warp
+#pragma unroll
+        for (int q = 0; q < 32; q++) {  // (row in warp, word) pairs, one per source lane
+            const uint32_t word = __shfl_sync(~0u, res, q);
+            const int y = y0 + wr0 + q / kBWords, x = x0 + 32 * (q % kBWords) + lane;
+            if (y < H && x < W) dst[(int64_t)y * W + x] = (uint8_t)((word >> lane) & 1u);
+        }
+    }
+}
+
+size_t bitmorph_smem(const BitOps &ops) {
+    const BitGeom g = bit_geom(ops);
+    size_t words = (size_t)g.srows * g.sld;
+    if (ops.nops == 2) words += (size_t)g.irows * g.ild;
+    return words * 4;
+}
+
+// Read offsets of one operator on an (kh, kw) structure (1-D items: kh = 1).
+int bit_taps(const uint8_t *structure, int kh, int kw, int oy, int ox, bool dilation, BitTaps *t) {
+    std::memset(t, 0, sizeof(BitTaps));
+    const int cy = kh / 2 + oy, cx = kw / 2 + ox;
+    for (int a = 0; a < kh; a++)
+        for (int b = 0; b < kw; b++) {
+            if (!structure[a * kw + b]) continue;
+            int dy = a - cy, dx = b - cx;
+            if (dilation) {
+                dy = -dy;
+                dx = -dx;
+            }
+            if (dy < -kBMaxDy || dy > kBMaxDy || dx < -kBMaxDx || dx > kBMaxDx || t->n >= kBMaxTaps) return 0;
+            t->dy[t->n] = (int8_t)dy;
+            t->dx[t->n] = (int8_t)dx;
+            t->hy = std::max(t->hy, std::abs(dy));
+            t->hx = std::max(t->hx, std::abs(dx));
+            t->n++;
+        }
+    return t->n > 0;
+}
+
+int bit_grid(size_t smem, int *grid) {
+    struct Entry {
+        size_t smem;
+        int dev, ctas;
+    };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
+    int dev = 0;
+    TM_CHECK_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    for (const Entry &e : cache)
+        if (e.smem == smem && e.dev == dev) {
+            *grid = e.ctas;
+            return TM_OK;
+        }
+    int per_sm = 0;
+    TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bitmorph_kernel, kBThreads, smem));
+    if (per_sm < 1) return fail(TM_ERR_UNSUPPORTED, "bit tile does not fit on an SM");
+    cache.push_back({smem, dev, per_sm * sm_count()});
+    *grid = per_sm * sm_count();
+    return TM_OK;
+}
+
+// kind: 0 erosion, 1 dilation, 2 opening, 3 closing.
+int build_bitops(int kind, const uint8_t *structure, int kh, int kw, int oy, int ox, int border, BitOps *ops) {
+    std::memset(ops, 0, sizeof(BitOps));
+    const bool first_dil = kind == 1 || kind == 3;
+    if (!bit_taps(structure, kh, kw, oy, ox, first_dil, &ops->op[0])) return 0;
+    ops->or1 = first_dil;
+    ops->nops = kind >= 2 ? 2 : 1;
+    if (ops->nops == 2) {
+        if (!bit_taps(structure, kh, kw, oy, ox, !first_dil, &ops->op[1])) return 0;
+        ops->or2 = !first_dil;
+    }
+    ops->border = border ? 1 : 0;
+    return 1;
+}
+
+}  // namespace
+
+// 1-D / 2-D binary morphology on bit tiles.  Sets *done = false (launching
+// nothing) when the structure is beyond the kernel's limits.
+int bitmorph_uniform(int kind, const uint8_t *in, uint8_t *out, int64_t batch, int ndim, const int64_t *shape,
+                     const uint8_t *structure, const int64_t *sshape, const int64_t *origin, int border,
+                     cudaStream_t s, bool *done) {
+    *done = false;
+    if (ndim != 1 && ndim != 2) return TM_OK;
+    const int64_t H = ndim == 2 ? shape[0] : 1, W = shape[ndim - 1];
+    if (H < 1 || W < 1 || H * W >= ((int64_t)1 << 31) || sshape[0] > 255 || sshape[ndim - 1] > 255) return TM_OK;
+    const int kh = ndim == 2 ? (int)sshape[0] : 1, kw = (int)sshape[ndim - 1];
+    const int oy = ndim == 2 ? (int)origin[0] : 0, ox = (int)origin[ndim - 1];
+    BitOps ops;
+    if (!build_bitops(kind, structure, kh, kw, oy, ox, border, &ops)) return TM_OK;
+    BitUniform u;
+    u.batch = batch;
+    u.H = (int)H;
+    u.W = (int)W;
+    u.tiles_x = (int)ceil_div(W, kBTileW);
+    const int64_t tiles_item = ceil_div(H, kBTileH) * (int64_t)u.tiles_x;
+    if (tiles_item >= ((int64_t)1 << 31)) return TM_OK;
+    u.tiles_item = (int)tiles_item;
+    const size_t smem = bitmorph_smem(ops);
+    int grid = 0, st;
+    if ((st = bit_grid(smem, &grid)) != TM_OK) return st;
+    const int64_t blocks = std::min<int64_t>((int64_t)grid, batch * tiles_item);
+    if (blocks > 0)
+        bitmorph_kernel<<<(unsigned)blocks, kBThreads, smem, s>>>(in, out, nullptr, nullptr, u, ops);
+    TM_LAUNCH_CHECK("bitmorph_kernel");
+    *done = true;
+    return TM_OK;
+}
+
+// Ragged batches of 2-D images (the plan of tm_ragged_plan: 128 x 32 tiles).
+int bitmorph_ragged(int kind, const uint8_t *in, uint8_t *out, const void *plan, const uint8_t *structure,
+                    const int64_t *sshape, const int64_t *origin, int border, cudaStream_t s, bool *done) {
+    *done = false;
+    if (sshape[0] > 255 || sshape[1] > 255) return TM_OK;
+    BitOps ops;
+    if (!build_bitops(kind, structure, (int)sshape[0], (int)sshape[1], (int)origin[0], (int)origin[1], border, &ops))
+        return TM_OK;
+    const size_t smem = bitmorph_smem(ops);
+    int grid = 0, st;
+    if ((st = bit_grid(smem, &grid)) != TM_OK) return st;
+    auto *hdr = static_cast<BitPlanHeader *>(const_cast<void *>(plan));
+    auto *items = reinterpret_cast<const BitItem *>(static_cast<const unsigned char *>(plan) + sizeof(BitPlanHeader));
+    TM_CHECK_CUDA(cudaMemsetAsync(&hdr->queue, 0, sizeof(int), s));
+    BitUniform u{};
+    bitmorph_kernel<<<(unsigned)grid, kBThreads, smem, s>>>(in, out, hdr, items, u, ops);
+    TM_LAUNCH_CHECK("bitmorph_kernel");
+    *done = true;
+    return TM_OK;
+}
+
+}  // namespace tmc
+
+namespace {
+
+int check_binary_args(const uint8_t *in, const uint8_t *out, const uint8_t *structure, const int64_t *sshape,
+                      const int64_t *origin, int nd) {
+    using namespace tmc;
+    if (!in || !out || !structure || !sshape || !origin) return fail(TM_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (in == out) return fail(TM_ERR_INVALID_ARGUMENT, "output must not alias the input");
+    for (int d = 0; d < nd; d++) {
+        if (sshape[d] < 1 || sshape[d] > 255)
+            return fail(TM_ERR_UNSUPPORTED, "structure sizes must be 1..255, got %lld", (long long)sshape[d]);
+        if (origin[d] < -(sshape[d] / 2) || origin[d] > (sshape[d] - 1) / 2)
+            return fail(TM_ERR_INVALID_ARGUMENT, "invalid origin");
+    }
+    return TM_OK;
+}
+
+int uniform_open(int kind, const uint8_t *in, uint8_t *out, int64_t batch, int ndim, const int64_t *shape,
+                 const uint8_t *structure, const int64_t *sshape, const int64_t *origin, int border_value,
+                 tm_stream_t stream) {
+    using namespace tmc;
+    if (ndim != 1 && ndim != 2) return fail(TM_ERR_UNSUPPORTED, "fused binary opening / closing: 1-D or 2-D items");
+    if (batch < 1 || !shape) return fail(TM_ERR_INVALID_ARGUMENT, "empty batch or NULL shape");
+    for (int d = 0; d < ndim; d++)
+        if (shape[d] < 1) return fail(TM_ERR_INVALID_ARGUMENT, "empty item");
+    int st = check_binary_args(in, out, structure, sshape, origin, ndim);
+    if (st != TM_OK) return st;
+    bool done = false;
+    st = bitmorph_uniform(kind, in, out, batch, ndim, shape, structure, sshape, origin, border_value,
+                          (cudaStream_t)stream, &done);
+    if (st != TM_OK) return st;
+    if (!done)
+        return fail(TM_ERR_UNSUPPORTED, "structure beyond the fused kernel (taps within 16 rows / 32 columns)");
+    return TM_OK;
+}
+
+int ragged_open(int kind, const uint8_t *in, uint8_t *out, const void *plan, size_t plan_bytes, int64_t n_items,
+                const uint8_t *structure, const int64_t *sshape, const int64_t *origin, int border_value,
+                tm_stream_t stream) {
+    using namespace tmc;
+    if (!plan || n_items < 1) return fail(TM_ERR_INVALID_ARGUMENT, "NULL plan or empty batch");
+    if (plan_bytes < sizeof(BitPlanHeader) + (size_t)n_items * sizeof(BitItem))
+        return fail(TM_ERR_WORKSPACE, "ragged plan buffer too small for %lld images", (long long)n_items);
+    if (((uintptr_t)plan & 255) != 0) return fail(TM_ERR_INVALID_ARGUMENT, "ragged plan must be 256-byte aligned");
+    int st = check_binary_args(in, out, structure, sshape, origin, 2);
+    if (st != TM_OK) return st;
+    bool done = false;
+    st = bitmorph_ragged(kind, in, out, plan, structure, sshape, origin, border_value, (cudaStream_t)stream, &done);
+    if (st != TM_OK) return st;
+    if (!done)
+        return fail(TM_ERR_UNSUPPORTED, "structure beyond the fused kernel (taps within 16 rows / 32 columns)");
+    return TM_OK;
+}
+
+}  // namespace
+
+extern "C" int tm_binary_opening(const uint8_t *in, uint8_t *out, int64_t batch, int ndim, const int64_t *shape,
+                                 const uint8_t *structure, const int64_t *sshape, const int64_t *origin,
+                                 int border_value, tm_stream_t stream) {
+    return uniform_open(2, in, out, batch, ndim, shape, structure, sshape, origin, border_value, stream);
+}
+
+extern "C" int tm_binary_closing(const uint8_t *in, uint8_t *out, int64_t batch, int ndim, const int64_t *shape,
+                                 const uint8_t *structure, const int64_t *sshape, const int64_t *origin,
+                                 int border_value, tm_stream_t stream) {
+    return uniform_open(3, in, out, batch, ndim, shape, structure, sshape, origin, border_value, stream);
+}
+
+extern "C" int tm_ragged_binary_opening(const uint8_t *in, uint8_t *out, const void *plan, size_t plan_bytes,
+                                        int64_t n_items, const uint8_t *structure, const int64_t *sshape,
+                                        const int64_t *origin, int border_value, tm_stream_t stream) {
+    return ragged_open(2, in, out, plan, plan_bytes, n_items, structure, sshape, origin, border_value, stream);
+}
+
+extern "C" int tm_ragged_binary_closing(const uint8_t *in, uint8_t *out, const void *plan, size_t plan_bytes,
+                                        int64_t n_items, const uint8_t *structure, const int64_t *sshape,
+                                        const int64_t *origin, int border_value, tm_stream_t stream) {
+    return ragged_open(3, in, out, plan, plan_bytes, n_items, structure, sshape, origin, border_value, stream);
+}

@@ -1573,7 +1573,9 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
             const int nb = min(32, W - 32 * wi);
             if (r < nrows) U = nb == 32 ? 0xffffffffu : ((1u << nb) - 1u);
             const volatile uint32_t *vhere = bits + kShellR * kCwPlane + (kShellR + r) * 4 + wi;
-            const bool has_l = wi != 0, has_r = wi != WW - 1;
+            // neighbour words are always inside the staged array (pads at both ends);
+            // these masks zero the words left of word 0 and right of word 3
+            const uint32_t ml = wi != 0 ? ~0u : 0u, mr = wi != WW - 1 ? ~0u : 0u;
             uint32_t P[9] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
             constexpr int kB = 8;
 #pragma unroll
@@ -1589,8 +1591,8 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
                     uint32_t b = 0u;
                     if (t0 + i < kShellN) {
                         if (dx == 0) b = vhere[d];
-                        else if (dx > 0) b = __funnelshift_r(vhere[d], has_r ? vhere[d + 1] : 0u, dx);
-                        else b = __funnelshift_r(has_l ? vhere[d - 1] : 0u, vhere[d], 32 + dx);
+                        else if (dx > 0) b = __funnelshift_r(vhere[d], vhere[d + 1] & mr, dx);
+                        else b = __funnelshift_r(vhere[d - 1] & ml, vhere[d], 32 + dx);
                     }
                     bg[i] = b;
                     any |= bg[i];
@@ -1952,13 +1954,15 @@ struct CdtSearch {
 // and, at the end of a class, resolve the class.  Returns false once every
 // voxel of the word is resolved (the rest of the list is skipped).
 template <int MET, int E>
-__device__ __forceinline__ bool cdt_row_step(const volatile uint32_t *vh, bool has_l, bool has_r, CdtSearch &s) {
+__device__ __forceinline__ bool cdt_row_step(const volatile uint32_t *vh, uint32_t ml, uint32_t mr, CdtSearch &s) {
     constexpr CdtRow row = kCdtRows<MET>.r[E];
     constexpr int d = row.dz * kCwPlane + row.dy * 4;
     const uint32_t mw = vh[d];
     uint32_t lw = 0u, rw = 0u;
-    if constexpr ((row.mask & 0x00f) != 0) lw = has_l ? vh[d - 1] : 0u;  // some dx < 0
-    if constexpr ((row.mask & 0x1e0) != 0) rw = has_r ? vh[d + 1] : 0u;  // some dx > 0
+    // the neighbour words are always inside the staged array (pads at both ends);
+    // the lane's masks zero the words left of word 0 and right of word 3
+    if constexpr ((row.mask & 0x00f) != 0) lw = vh[d - 1] & ml;  // some dx < 0
+    if constexpr ((row.mask & 0x1e0) != 0) rw = vh[d + 1] & mr;  // some dx > 0
 #pragma unroll
     for (int dx = -kShellR; dx <= kShellR; dx++)
         if (row.mask & (1 << (dx + kShellR)))
@@ -1977,9 +1981,9 @@ __device__ __forceinline__ bool cdt_row_step(const volatile uint32_t *vh, bool h
 }
 
 template <int MET, int... Es>
-__device__ __forceinline__ void cdt_rows_all(std::integer_sequence<int, Es...>, const volatile uint32_t *vh, bool has_l,
-                                             bool has_r, CdtSearch &s) {
-    (cdt_row_step<MET, Es>(vh, has_l, has_r, s) && ...);  // stops at the first false
+__device__ __forceinline__ void cdt_rows_all(std::integer_sequence<int, Es...>, const volatile uint32_t *vh, uint32_t ml,
+                                             uint32_t mr, CdtSearch &s) {
+    (cdt_row_step<MET, Es>(vh, ml, mr, s) && ...);  // stops at the first false
 }
 
 // The same search on the EDT shell kernel's work-queue design: persistent
@@ -2049,11 +2053,11 @@ __global__ void __launch_bounds__(kShellCtThreads) cdt_shell_warp_kernel(const u
             const int nb = min(32, W - 32 * wi);
             if (r < nrows) U = nb == 32 ? 0xffffffffu : ((1u << nb) - 1u);
             const volatile uint32_t *vh = bits + kShellR * kCwPlane + (kShellR + r) * 4 + wi;
-            const bool has_l = wi != 0, has_r = wi != WW - 1;
+            const uint32_t ml = wi != 0 ? ~0u : 0u, mr = wi != WW - 1 ? ~0u : 0u;
             // one straight-line pass over the rows of each norm class in turn; at
             // the end of a class its union resolves the voxels it covers
             CdtSearch cs{U, 0u, 0u, 0u, 0u, 0u};
-            cdt_rows_all<MET>(std::make_integer_sequence<int, kCdtRows<MET>.n>{}, vh, has_l, has_r, cs);
+            cdt_rows_all<MET>(std::make_integer_sequence<int, kCdtRows<MET>.n>{}, vh, ml, mr, cs);
             U = cs.U;
             planes[lane] = make_uint4(cs.P0, cs.P1, cs.P2, cs.P3);
         }

@@ -86,6 +86,14 @@ constexpr int kTileW = 128;
 constexpr int kTileH = 32;
 constexpr int kFlatThreads = 256;
 constexpr int kRun = 8;
+// Row pitch of the row-pass buffer: odd, so that threads writing the same
+// column of consecutive rows hit different banks.
+constexpr int kRowsPitch = kTileW + 1;
+
+// Row pitch of a staged tile for a window of kw columns: room for full runs
+// past the last column, made odd so that consecutive rows start in different
+// banks (the row pass gives consecutive rows to consecutive threads).
+__host__ __device__ inline int stage_pitch(int kw) { return (kTileW + kw - 1 + (kRun - 1)) | 1; }
 
 struct Flat2DParams {
     int H, W;        // item size (1-D items use H = 1)
@@ -132,7 +140,7 @@ __device__ __forceinline__ void window_run(const T *src, int step, int k, T *res
 
 // Row pass then column pass of one staged tile: `tile` points at the first
 // input column the tile needs (row stride ld), `rows` receives the row-pass
-// result (RH x kTileW); outputs go to dst at (y0.., x0..).
+// result (RH x kTileW at pitch kRowsPitch); outputs go to dst at (y0.., x0..).
 template <typename T, bool MAX>
 __device__ __forceinline__ void flat_tile_compute(const T *tile, int ld, T *rows, const Flat2DParams &p, T *dst,
                                                   int x0, int y0) {
@@ -146,16 +154,20 @@ __device__ __forceinline__ void flat_tile_compute(const T *tile, int ld, T *rows
             const T *src = tile + r * ld + c;
             T acc = src[0];
             for (int t = 1; t < p.kw; t++) acc = Op::combine(acc, src[t]);
-            rows[r * kTileW + c] = acc;
+            rows[r * kRowsPitch + c] = acc;
         }
     } else {
         const int runs_per_row = kTileW / kRun;
+        // an odd row stride: consecutive threads take the same run of consecutive
+        // rows (conflict-free); otherwise consecutive runs of one row
+        const bool by_rows = (ld & 1) != 0;
         for (int w = threadIdx.x; w < RH * runs_per_row; w += kFlatThreads) {
-            int r = w / runs_per_row, c = (w % runs_per_row) * kRun;
+            const int r = by_rows ? w % RH : w / runs_per_row;
+            const int c = (by_rows ? w / RH : w % runs_per_row) * kRun;
             T res[kRun];
             window_run<T, MAX>(tile + r * ld + c, 1, p.kw, res);
 #pragma unroll
-            for (int j = 0; j < kRun; j++) rows[r * kTileW + c + j] = res[j];
+            for (int j = 0; j < kRun; j++) rows[r * kRowsPitch + c + j] = res[j];
         }
     }
     __syncthreads();
@@ -166,7 +178,7 @@ __device__ __forceinline__ void flat_tile_compute(const T *tile, int ld, T *rows
         // kTileH is a multiple of kRun, so the run reads rows
         // r .. r + kRun + kh - 2 <= RH - 1: always inside the row buffer
         T res[kRun];
-        window_run<T, MAX>(rows + r * kTileW + c, kTileW, p.kh, res);
+        window_run<T, MAX>(rows + r * kRowsPitch + c, kRowsPitch, p.kh, res);
         if (gx < p.W) {
 #pragma unroll
             for (int j = 0; j < kRun; j++) {

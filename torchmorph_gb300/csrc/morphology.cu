@@ -22,6 +22,7 @@
 #include <cstring>
 #include <vector>
 
+#include "bitmorph.cuh"
 #include "morph_tile.cuh"
 #include "tm_common.cuh"
 #include "tm_tma.cuh"
@@ -38,9 +39,9 @@ __global__ void __launch_bounds__(kFlatThreads) flat2d_kernel(const T *__restric
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int RH = kTileH + p.kh - 1;      // loaded rows
     const int RW = kTileW + p.kw - 1;      // loaded columns
-    const int RWp = RW + (kRun - 1);       // padded so full runs never read past a row
+    const int RWp = stage_pitch(p.kw);     // padded so full runs never read past a row; odd
     T *tile = reinterpret_cast<T *>(smem_raw);
-    T *rows = tile + RH * RWp;             // row-pass result, RH x kTileW (+ pad)
+    T *rows = tile + RH * RWp;             // row-pass result, RH x kTileW at pitch kRowsPitch
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = kFlatThreads / 32;
     const T cval = (T)p.cval;
@@ -147,7 +148,7 @@ __global__ void __launch_bounds__(kFlatThreads) flat2d_tma_kernel(const __grid_c
     const size_t buf_bytes = round_up((size_t)RH * tp.bw * sizeof(T), 1024);
     T *buf[2] = {reinterpret_cast<T *>(smem_raw), reinterpret_cast<T *>(smem_raw + buf_bytes)};
     T *rows = reinterpret_cast<T *>(smem_raw + 2 * buf_bytes);
-    const size_t rows_bytes = KH == 0 ? round_up((size_t)RH * kTileW * sizeof(T), 16) : 0;
+    const size_t rows_bytes = KH == 0 ? round_up((size_t)RH * kRowsPitch * sizeof(T), 16) : 0;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + 2 * buf_bytes + rows_bytes);
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
@@ -307,8 +308,8 @@ struct Tap {
 // border ring when the TMA kernel takes the interior), then the TMA kernel.
 template <typename T, bool MAX, int KH, int KW>
 int launch_flat2d(const T *in, T *out, Flat2DParams p, int64_t batch, int sms, cudaStream_t stream) {
-    const int RH = kTileH + p.kh - 1, RWp = kTileW + p.kw - 1 + (kRun - 1);
-    const size_t rows_bytes = KH == 0 ? (size_t)RH * kTileW * sizeof(T) : 0;
+    const int RH = kTileH + p.kh - 1, RWp = stage_pitch(p.kw);
+    const size_t rows_bytes = KH == 0 ? (size_t)RH * kRowsPitch * sizeof(T) : 0;
     const size_t smem = (size_t)RH * RWp * sizeof(T) + rows_bytes;
     if (smem > 48 * 1024)
         TM_CHECK_CUDA(cudaFuncSetAttribute(flat2d_kernel<T, MAX, KH, KW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -361,7 +362,7 @@ int launch_flat2d(const T *in, T *out, Flat2DParams p, int64_t batch, int sms, c
     st = device_status_word(&status);
     if (st != TM_OK) return st;
     const size_t tsmem = 2 * round_up((size_t)RH * tp.bw * sizeof(T), 1024) +
-                         (KH == 0 ? round_up((size_t)RH * kTileW * sizeof(T), 16) : 0) + 2 * sizeof(uint64_t) + 1024;
+                         (KH == 0 ? round_up((size_t)RH * kRowsPitch * sizeof(T), 16) : 0) + 2 * sizeof(uint64_t) + 1024;
     if (tsmem > 220 * 1024) return fail(TM_ERR_UNSUPPORTED, "TMA tile does not fit in shared memory");
     // attribute + occupancy depend only on the instantiation and the smem size: cache the last answer
     static thread_local size_t cached_smem = 0;
@@ -433,6 +434,16 @@ int run_morphology(const T *in, T *out, int64_t batch, int ndim, const int64_t *
         return fail(TM_ERR_INVALID_ARGUMENT, "footprint must contain at least one active position");
     const bool box = (int64_t)taps.size() == stotal && uniform;
     const int sms = sm_count();
+    if constexpr (sizeof(T) == 1) {
+        // binary, 1-D / 2-D, elements other than full boxes (the default cross,
+        // footprints): bit-packed tiles
+        if (!box && ndim <= 2) {
+            bool done = false;
+            st = bitmorph_uniform(MAX ? 1 : 0, in, out, batch, ndim, shape, footprint, sshape, origin, cval != 0.0f,
+                                  stream, &done);
+            if (st != TM_OK || done) return st;
+        }
+    }
 
     if (box && ndim <= 2) {
         Flat2DParams p;
@@ -451,8 +462,8 @@ int run_morphology(const T *in, T *out, int64_t batch, int ndim, const int64_t *
         p.sval = first_val;
         if (p.kh > 4096 || p.kw > 4096) goto stencil;  // tile would not fit on chip
         {
-            const int RH = kTileH + p.kh - 1, RW = kTileW + p.kw - 1 + (kRun - 1);
-            if ((size_t)RH * RW * sizeof(T) + (size_t)RH * kTileW * sizeof(T) > 200 * 1024) goto stencil;
+            const int RH = kTileH + p.kh - 1, RW = stage_pitch(p.kw);
+            if ((size_t)RH * RW * sizeof(T) + (size_t)RH * kRowsPitch * sizeof(T) > 200 * 1024) goto stencil;
             if (p.kh == 3 && p.kw == 3) return launch_flat2d<T, MAX, 3, 3>(in, out, p, batch, sms, stream);
             if (p.kh == 5 && p.kw == 5) return launch_flat2d<T, MAX, 5, 5>(in, out, p, batch, sms, stream);
             if (p.kh == 1 && p.kw == 3) return launch_flat2d<T, MAX, 1, 3>(in, out, p, batch, sms, stream);

@@ -23,7 +23,9 @@
 #include <mutex>
 #include <vector>
 
+#include "bitmorph.cuh"
 #include "morph_tile.cuh"
+#include "tile_queue.cuh"
 #include "tm_common.cuh"
 
 namespace tmc {
@@ -60,26 +62,6 @@ struct RaggedTaps {
     int8_t dy[kMaxTaps], dx[kMaxTaps];
     float val[kMaxTaps];
 };
-
-// Thread 0 takes the next tile and finds its image; -1 when the queue is empty.
-__device__ __forceinline__ void next_tile(PlanHeader *hdr, const RaggedItem *items, int *s_slot) {
-    if (threadIdx.x == 0) {
-        const int t = atomicAdd(&hdr->queue, 1);
-        int item = -1;
-        if (t < hdr->ntiles) {
-            int lo = 0, hi = hdr->nitems - 1;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (items[mid].tile_begin <= t) lo = mid;
-                else hi = mid - 1;
-            }
-            item = lo;
-        }
-        s_slot[0] = t;
-        s_slot[1] = item;
-    }
-    __syncthreads();
-}
 
 // Stage rows [gy0, gy0 + RH) x columns [gx0, gx0 + RW) of one image into
 // shared memory (row stride ld), mapping out-of-image coordinates.  Warp w
@@ -141,14 +123,15 @@ __global__ void __launch_bounds__(kFlatThreads) ragged_flat_kernel(const T *__re
                                                                    RaggedWindow w) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_slot[2];
+    __shared__ int s_tb[kQueueCache];
     const int RH = kTileH + w.kh - 1, RW = kTileW + w.kw - 1;
-    const int RWp = RW + (kRun - 1);
+    const int RWp = stage_pitch(w.kw);
     T *tile = reinterpret_cast<T *>(smem_raw);
     T *rows = tile + RH * RWp;
-    for (;;) {
-        next_tile(hdr, items, s_slot);
+    TileQueue<RaggedItem> q{&hdr->queue, hdr->ntiles, hdr->nitems, items, s_tb, s_slot, 0};
+    q.init();
+    while (q.take()) {
         const int t = s_slot[0], item = s_slot[1];
-        if (item < 0) break;
         const RaggedItem it = items[item];
         const int local = t - it.tile_begin;
         const int ty = local / it.tiles_x, tx = local - ty * it.tiles_x;
@@ -184,13 +167,14 @@ __global__ void __launch_bounds__(kFlatThreads) ragged_taps_kernel(const T *__re
     using Op = MorphOp<T, MAX>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_slot[2];
+    __shared__ int s_tb[kQueueCache];
     const int RH = kTileH + taps.ext_y, RW = kTileW + taps.ext_x;
     const int ld = P ? P : RW;
     T *tile = reinterpret_cast<T *>(smem_raw);
-    for (;;) {
-        next_tile(hdr, items, s_slot);
+    TileQueue<RaggedItem> q{&hdr->queue, hdr->ntiles, hdr->nitems, items, s_tb, s_slot, 0};
+    q.init();
+    while (q.take()) {
         const int t = s_slot[0], item = s_slot[1];
-        if (item < 0) break;
         const RaggedItem it = items[item];
         const int local = t - it.tile_begin;
         const int ty = local / it.tiles_x, tx = local - ty * it.tiles_x;
@@ -278,8 +262,8 @@ int persistent_grid(K kernel, size_t smem, int *grid) {
 template <typename T, bool MAX, int KH, int KW>
 int launch_ragged_flat(const T *in, T *out, PlanHeader *hdr, const RaggedItem *items, const RaggedWindow &w,
                        cudaStream_t s) {
-    const int RH = kTileH + w.kh - 1, RWp = kTileW + w.kw - 1 + (kRun - 1);
-    const size_t smem = (size_t)RH * RWp * sizeof(T) + (KH == 0 ? (size_t)RH * kTileW * sizeof(T) : 0);
+    const int RH = kTileH + w.kh - 1, RWp = stage_pitch(w.kw);
+    const size_t smem = (size_t)RH * RWp * sizeof(T) + (KH == 0 ? (size_t)RH * kRowsPitch * sizeof(T) : 0);
     auto kernel = ragged_flat_kernel<T, MAX, KH, KW>;
     int grid = 0;
     int st = persistent_grid(kernel, smem, &grid);
@@ -307,6 +291,11 @@ int run_ragged(const T *in, T *out, const void *plan, size_t plan_bytes, int64_t
             return fail(TM_ERR_UNSUPPORTED, "ragged structure sizes must be 1..255, got %lld", (long long)sshape[d]);
         if (origin[d] < -(sshape[d] / 2) || origin[d] > (sshape[d] - 1) / 2)
             return fail(TM_ERR_INVALID_ARGUMENT, "invalid origin");
+    }
+    if constexpr (sizeof(T) == 1) {  // binary: bit-packed tiles (the same plan)
+        bool done = false;
+        const int st = bitmorph_ragged(MAX ? 1 : 0, in, out, plan, footprint, sshape, origin, cval != 0.0f, s, &done);
+        if (st != TM_OK || done) return st;
     }
     auto *hdr = static_cast<PlanHeader *>(const_cast<void *>(plan));
     auto *items = reinterpret_cast<const RaggedItem *>(static_cast<const unsigned char *>(plan) + sizeof(PlanHeader));

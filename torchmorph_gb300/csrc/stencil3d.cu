@@ -5,9 +5,10 @@
 // 256 threads from a staged copy of its input region -- the tile grown by the
 // footprint's extent on each axis, out-of-item coordinates mapped with the
 // reference's border modes (torchmorph/csrc/grey_kernel.cu:63-97) -- so every
-// input voxel is read from HBM once per tile instead of once per tap.  Each
-// thread owns one (y, x) column of the tile and walks the taps over shared
-// memory for its 4 voxels; the taps (offsets and values, up to 1024) sit in
+// input voxel is read from HBM once per tile instead of once per tap.  Flat
+// boxes are reduced separably (x through shared memory, y and z in
+// registers); other elements: each thread owns one (y, x) column of the tile
+// and walks the taps over shared memory for its 4 voxels; the taps (offsets and values, up to 1024) sit in
 // the launch parameters, their shared-memory offsets are computed once per
 // CTA.  Erosion reads x + delta, dilation x - delta, delta = k - (size // 2 +
 // origin), with min(v - s) / max(v + s) as in the reference's kernel
@@ -24,6 +25,7 @@
 #include <vector>
 
 #include "morph_tile.cuh"
+#include "tile_queue.cuh"
 
 namespace tmc {
 namespace {
@@ -66,8 +68,67 @@ struct Uniform3 {  // a uniform batch: `batch` items of D x H x W
     int tiles_x, tiles_xy, tiles_item;
 };
 
-template <typename T, bool MAX>
-__global__ void __launch_bounds__(kT3Threads) stencil3d_kernel(const T *__restrict__ in, T *__restrict__ out,
+// Stage the tile's input region, (z, y) rows of RX elements: each warp takes
+// 4 rows at a time and every lane loads its 2 columns of all 4 rows (8 loads
+// in flight) before storing any; a row's border mapping is computed once.
+// Interior tiles read straight rows; others map every coordinate with the
+// border mode.
+template <typename T>
+__device__ __forceinline__ void stage3d(const T *__restrict__ src, T *tile, int D, int H, int W, int gz0, int gy0,
+                                        int gx0, int RZ, int RY, int RX, int mode, T cval) {
+    constexpr int kRows = 4, kCols = 2;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool interior = gz0 >= 0 && gy0 >= 0 && gx0 >= 0 && gz0 + RZ <= D && gy0 + RY <= H && gx0 + RX <= W;
+    const int nrows = RZ * RY;
+    for (int row0 = warp * kRows; row0 < nrows; row0 += kRows * (kT3Threads / 32)) {
+        int64_t base[kRows];  // element offset of the row's first staged column (mapped row), or -1
+#pragma unroll
+        for (int k = 0; k < kRows; k++) {
+            const int row = row0 + k;
+            const int rz = row / RY, ry = row - rz * RY;
+            int mz = gz0 + rz, my = gy0 + ry;
+            if (!interior) {
+                mz = map_coord(mz, D, mode);
+                my = map_coord(my, H, mode);
+            }
+            base[k] = (row < nrows && mz >= 0 && my >= 0) ? ((int64_t)mz * H + my) * W : -1;
+        }
+        for (int c0 = 0; c0 < RX; c0 += 32 * kCols) {
+            T v[kRows][kCols];
+#pragma unroll
+            for (int k = 0; k < kRows; k++)
+#pragma unroll
+                for (int j = 0; j < kCols; j++) {
+                    const int rx = c0 + lane + 32 * j;
+                    v[k][j] = cval;
+                    if (base[k] >= 0 && rx < RX) {
+                        int mx = gx0 + rx;
+                        if (!interior) mx = map_coord(mx, W, mode);
+                        if (mx >= 0) v[k][j] = src[base[k] + mx];
+                    }
+                }
+#pragma unroll
+            for (int k = 0; k < kRows; k++)
+#pragma unroll
+                for (int j = 0; j < kCols; j++) {
+                    const int rx = c0 + lane + 32 * j;
+                    if (row0 + k < nrows && rx < RX) tile[(row0 + k) * RX + rx] = v[k][j];
+                }
+        }
+    }
+}
+
+constexpr int kSepMaxZ = 9;  // flat boxes up to 9 deep take the separable path
+
+// SEP: the element is a full box with one structure value s (flat), at most
+// kSepMaxZ deep: the min / max is taken along x into a shared buffer, then
+// each thread takes it along y for every staged z and along z in registers,
+// and applies s once -- erosion min(v) - s, dilation max(v) + s, equal to the
+// per-tap min(v - s) / max(v + s) because rounding is monotone (accumulators
+// start at the identity, so NaN inputs are skipped exactly as the tap loop
+// skips them).  Otherwise every thread loops over the taps.
+template <typename T, bool MAX, bool SEP>
+__global__ void __launch_bounds__(kT3Threads, 6) stencil3d_kernel(const T *__restrict__ in, T *__restrict__ out,
                                                                Plan3Header *hdr, const Vol3Item *__restrict__ items,
                                                                Uniform3 u, const __grid_constant__ Taps3 taps,
                                                                int mode, float cval_f) {
@@ -78,11 +139,19 @@ __global__ void __launch_bounds__(kT3Threads) stencil3d_kernel(const T *__restri
     const int n = taps.n;
     int *soff = reinterpret_cast<int *>(smem3);
     T *tile = reinterpret_cast<T *>(smem3 + (((size_t)n * 4 + 15) & ~(size_t)15));
+    // SEP: x-reduced rows, (rz, ry) x kT3X
+    T *xr = reinterpret_cast<T *>(smem3 + (((size_t)n * 4 + 15) & ~(size_t)15) +
+                                  (((size_t)rz_n * ryx * sizeof(T) + 15) & ~(size_t)15));
     __shared__ int s_slot[2];
+    __shared__ int s_tb[kQueueCache];
     const int tid = threadIdx.x;
-    for (int t = tid; t < n; t += kT3Threads)
-        soff[t] = (taps.off[0][t] - taps.lo[0]) * ryx + (taps.off[1][t] - taps.lo[1]) * RX +
-                  (taps.off[2][t] - taps.lo[2]);
+    TileQueue<Vol3Item> q{hdr ? &hdr->queue : nullptr, hdr ? hdr->ntiles : 0, hdr ? hdr->nitems : 0, items, s_tb,
+                          s_slot, 0};
+    if (hdr) q.init();
+    if (!SEP)
+        for (int t = tid; t < n; t += kT3Threads)
+            soff[t] = (taps.off[0][t] - taps.lo[0]) * ryx + (taps.off[1][t] - taps.lo[1]) * RX +
+                      (taps.off[2][t] - taps.lo[2]);
     const T cval = (T)cval_f;
     const int y = tid / kT3X, x = tid % kT3X;
     const int64_t ntiles = hdr ? (int64_t)0 : u.batch * (int64_t)u.tiles_item;
@@ -92,23 +161,7 @@ __global__ void __launch_bounds__(kT3Threads) stencil3d_kernel(const T *__restri
         int D, H, W, tiles_x, tiles_xy;
         if (hdr) {  // ragged: the next tile from the plan's queue
             __syncthreads();  // the previous tile's readers are done with s_slot and the tile
-            if (tid == 0) {
-                const int t = atomicAdd(&hdr->queue, 1);
-                int it = -1;
-                if (t < hdr->ntiles) {
-                    int lo = 0, hi = hdr->nitems - 1;
-                    while (lo < hi) {
-                        const int mid = (lo + hi + 1) >> 1;
-                        if (items[mid].tile_begin <= t) lo = mid;
-                        else hi = mid - 1;
-                    }
-                    it = lo;
-                }
-                s_slot[0] = t;
-                s_slot[1] = it;
-            }
-            __syncthreads();
-            if (s_slot[1] < 0) break;
+            if (!q.take()) break;
             const Vol3Item &v = items[s_slot[1]];
             lt = s_slot[0] - v.tile_begin;
             off = v.off;
@@ -132,26 +185,40 @@ __global__ void __launch_bounds__(kT3Threads) stencil3d_kernel(const T *__restri
         const int tz = lt / tiles_xy, rem = lt - tz * tiles_xy;
         const int ty = rem / tiles_x, tx = rem - ty * tiles_x;
         const int z0 = tz * kT3Z, y0 = ty * kT3Y, x0 = tx * kT3X;
-        const int gz0 = z0 + taps.lo[0], gy0 = y0 + taps.lo[1], gx0 = x0 + taps.lo[2];
-        const T *src = in + off;
-        const int total = rz_n * ryx;
-        const bool interior = gz0 >= 0 && gy0 >= 0 && gx0 >= 0 && gz0 + rz_n <= D && gy0 + RY <= H && gx0 + RX <= W;
-        if (interior) {
-            for (int i = tid; i < total; i += kT3Threads) {
-                const int rz = i / ryx, r2 = i - rz * ryx, ry = r2 / RX, rx = r2 - ry * RX;
-                tile[i] = src[((int64_t)(gz0 + rz) * H + (gy0 + ry)) * W + (gx0 + rx)];
-            }
-        } else {
-            for (int i = tid; i < total; i += kT3Threads) {
-                const int rz = i / ryx, r2 = i - rz * ryx, ry = r2 / RX, rx = r2 - ry * RX;
-                const int mz = map_coord(gz0 + rz, D, mode), my = map_coord(gy0 + ry, H, mode),
-                          mx = map_coord(gx0 + rx, W, mode);
-                tile[i] = (mz < 0 || my < 0 || mx < 0) ? cval : src[((int64_t)mz * H + my) * W + mx];
-            }
-        }
+        stage3d(in + off, tile, D, H, W, z0 + taps.lo[0], y0 + taps.lo[1], x0 + taps.lo[2], rz_n, RY, RX, mode, cval);
         __syncthreads();
-        if (y0 + y < H && x0 + x < W) {
-            const int zn = min(kT3Z, D - z0);
+        const int zn = min(kT3Z, D - z0);
+        if (SEP) {
+            const int kx = taps.ext[2] + 1, ky = taps.ext[1] + 1, kz = taps.ext[0] + 1;
+            for (int i = tid; i < rz_n * RY * kT3X; i += kT3Threads) {  // along x
+                const int row = i / kT3X, c = i - row * kT3X;
+                const T *t = tile + row * RX + c;
+                T acc = Op::identity();
+                for (int dx = 0; dx < kx; dx++) acc = Op::combine(acc, t[dx]);
+                xr[i] = acc;
+            }
+            __syncthreads();
+            if (y0 + y < H && x0 + x < W) {
+                T a[kT3Z + kSepMaxZ - 1];
+#pragma unroll
+                for (int rz = 0; rz < kT3Z + kSepMaxZ - 1; rz++) {  // along y, every staged z
+                    T acc = Op::identity();
+                    if (rz < rz_n)
+                        for (int dy = 0; dy < ky; dy++) acc = Op::combine(acc, xr[(rz * RY + y + dy) * kT3X + x]);
+                    a[rz] = acc;
+                }
+                const float sval = taps.val[0];
+#pragma unroll
+                for (int z = 0; z < kT3Z; z++) {  // along z
+                    if (z >= zn) break;
+                    T acc = Op::identity();
+#pragma unroll
+                    for (int dz = 0; dz < kSepMaxZ; dz++)
+                        if (dz < kz) acc = Op::combine(acc, a[z + dz]);
+                    out[off + ((int64_t)(z0 + z) * H + (y0 + y)) * W + (x0 + x)] = Op::apply(acc, sval);
+                }
+            }
+        } else if (y0 + y < H && x0 + x < W) {
             for (int z = 0; z < zn; z++) {
                 const T *base = tile + z * ryx + y * RX + x;
                 T acc = Op::identity();
@@ -162,9 +229,19 @@ __global__ void __launch_bounds__(kT3Threads) stencil3d_kernel(const T *__restri
     }
 }
 
+// A full box with one structure value, at most kSepMaxZ deep.
+bool taps3_separable(const Taps3 &taps) {
+    const int kz = taps.ext[0] + 1, ky = taps.ext[1] + 1, kx = taps.ext[2] + 1;
+    if (kz > kSepMaxZ || taps.n != kz * ky * kx) return false;
+    for (int t = 1; t < taps.n; t++)
+        if (taps.val[t] != taps.val[0]) return false;
+    return true;
+}
+
 size_t stencil3d_smem(const Taps3 &taps, size_t elem) {
-    return (((size_t)taps.n * 4 + 15) & ~(size_t)15) +
-           (size_t)(kT3Z + taps.ext[0]) * (kT3Y + taps.ext[1]) * (kT3X + taps.ext[2]) * elem;
+    const size_t rz = kT3Z + taps.ext[0], ry = kT3Y + taps.ext[1];
+    const size_t tile = (rz * ry * (kT3X + taps.ext[2]) * elem + 15) & ~(size_t)15;
+    return (((size_t)taps.n * 4 + 15) & ~(size_t)15) + tile + (taps3_separable(taps) ? rz * ry * kT3X * elem : 0);
 }
 
 // Taps of a 3-D element (torchmorph/csrc/grey_kernel.cu:271-291).
@@ -212,7 +289,7 @@ int build_taps3(const float *structure, const uint8_t *footprint, const int64_t 
 // CTAs of one wave for a tile size (cached per device and size).  The
 // dynamic shared-memory attribute is set to the largest tile this kernel
 // takes, so a cached size never falls below a later launch's.
-template <typename T, bool MAX>
+template <typename T, bool MAX, bool SEP>
 int grid_for_kernel(size_t smem, int *grid) {
     struct Entry {
         size_t smem;
@@ -228,13 +305,29 @@ int grid_for_kernel(size_t smem, int *grid) {
             *grid = e.ctas;
             return TM_OK;
         }
-    auto kernel = stencil3d_kernel<T, MAX>;
+    auto kernel = stencil3d_kernel<T, MAX, SEP>;
     TM_CHECK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxStencil3Smem));
     int per_sm = 0;
     TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kT3Threads, smem));
     if (per_sm < 1) return fail(TM_ERR_UNSUPPORTED, "3-D tile does not fit on an SM");
     cache.push_back({smem, dev, per_sm * sm_count()});
     *grid = per_sm * sm_count();
+    return TM_OK;
+}
+
+// One launch of the tile kernel: `blocks` CTAs (at most one wave; -1: one
+// wave), the separable variant for flat boxes.
+template <typename T, bool MAX>
+int launch3d(bool sep, int64_t blocks, size_t smem, const T *in, T *out, Plan3Header *hdr, const Vol3Item *items,
+             const Uniform3 &u, const Taps3 &taps, int mode, float cval, cudaStream_t s) {
+    int grid = 0, st;
+    if (sep) st = grid_for_kernel<T, MAX, true>(smem, &grid);
+    else st = grid_for_kernel<T, MAX, false>(smem, &grid);
+    if (st != TM_OK) return st;
+    const unsigned g = (unsigned)(blocks < 0 ? grid : std::min<int64_t>(blocks, grid));
+    if (sep) stencil3d_kernel<T, MAX, true><<<g, kT3Threads, smem, s>>>(in, out, hdr, items, u, taps, mode, cval);
+    else stencil3d_kernel<T, MAX, false><<<g, kT3Threads, smem, s>>>(in, out, hdr, items, u, taps, mode, cval);
+    TM_LAUNCH_CHECK("stencil3d_kernel");
     return TM_OK;
 }
 
@@ -255,15 +348,11 @@ int run_ragged3d(const T *in, T *out, const void *plan, size_t plan_bytes, int64
     if (st != TM_OK) return st;
     const size_t smem = stencil3d_smem(taps, sizeof(T));
     if (smem > kMaxStencil3Smem) return fail(TM_ERR_UNSUPPORTED, "3-D structure too large for the shared-memory tile");
-    int grid = 0;
-    if ((st = grid_for_kernel<T, MAX>(smem, &grid)) != TM_OK) return st;
     auto *hdr = static_cast<Plan3Header *>(const_cast<void *>(plan));
     auto *items = reinterpret_cast<const Vol3Item *>(static_cast<const unsigned char *>(plan) + sizeof(Plan3Header));
     TM_CHECK_CUDA(cudaMemsetAsync(&hdr->queue, 0, sizeof(int), s));
     Uniform3 u{};
-    stencil3d_kernel<T, MAX><<<grid, kT3Threads, smem, s>>>(in, out, hdr, items, u, taps, mode, cval);
-    TM_LAUNCH_CHECK("stencil3d_kernel");
-    return TM_OK;
+    return launch3d<T, MAX>(taps3_separable(taps), -1, smem, in, out, hdr, items, u, taps, mode, cval, s);
 }
 
 }  // namespace
@@ -297,12 +386,9 @@ int stencil3d_uniform(const T *in, T *out, int64_t batch, const int64_t *shape, 
     const int64_t tiles_item = (int64_t)u.tiles_xy * ceil_div(u.D, kT3Z);
     if (tiles_item >= ((int64_t)1 << 31)) return TM_OK;
     u.tiles_item = (int)tiles_item;
-    int grid = 0;
-    if ((st = grid_for_kernel<T, MAX>(smem, &grid)) != TM_OK) return st;
-    const int64_t blocks = std::min<int64_t>(batch * tiles_item, (int64_t)grid);
-    stencil3d_kernel<T, MAX><<<(unsigned)blocks, kT3Threads, smem, s>>>(in, out, nullptr, nullptr, u, taps, mode,
-                                                                          cval);
-    TM_LAUNCH_CHECK("stencil3d_kernel");
+    if ((st = launch3d<T, MAX>(taps3_separable(taps), batch * tiles_item, smem, in, out, nullptr, nullptr, u, taps,
+                               mode, cval, s)) != TM_OK)
+        return st;
     *done = true;
     return TM_OK;
 }

@@ -144,15 +144,47 @@ def binary_hit_or_miss(input, structure1=None, structure2=None, output=None, ori
     return result
 
 
+def _one_pass(kind, input, structure, iterations, mask, output, border_value, origin):
+    """The one-pass opening / closing of 1-D / 2-D items (one iteration, no mask) on
+    bit-packed tiles; None where the reference's composition of two operators runs."""
+    if iterations != 1 or mask is not None:
+        return None
+    nd = validate_bcs_input(input)
+    validate_output(input, output)
+    if nd > 2:
+        return None
+    if structure is None:
+        structure = generate_binary_structure(nd, 1)
+    structure = _normalize_structure(structure, nd)
+    origin = _normalize_origin(origin, nd)
+    _validate_origin(origin, structure)
+    if not bool(structure.any()):
+        return None
+    x = input if input.dtype == torch.bool and input.is_contiguous() else (input != 0).contiguous()
+    res = _C.binary_composite(kind, x, structure, list(origin), bool(border_value))
+    if res is None:
+        return None
+    if output is not None:
+        output.copy_(res)
+        return output
+    return res
+
+
 def binary_opening(input, structure=None, iterations=1, mask=None, output=None, border_value=False,
                    origin=0) -> Tensor:
-    """Erosion followed by dilation."""
+    """Erosion followed by dilation (1-D / 2-D, one iteration: one pass)."""
+    res = _one_pass("opening", input, structure, iterations, mask, output, border_value, origin)
+    if res is not None:
+        return res
     x = binary_erosion(input, structure, iterations, mask, None, border_value, origin)
     return binary_dilation(x, structure, iterations, mask, output, border_value, origin)
 
 
 def binary_closing(input, structure=None, iterations=1, mask=None, output=None, border_value=False,
                    origin=0) -> Tensor:
-    """Dilation followed by erosion."""
+    """Dilation followed by erosion (1-D / 2-D, one iteration: one pass)."""
+    res = _one_pass("closing", input, structure, iterations, mask, output, border_value, origin)
+    if res is not None:
+        return res
     x = binary_dilation(input, structure, iterations, mask, None, border_value, origin)
     return binary_erosion(x, structure, iterations, mask, output, border_value, origin)

@@ -30,6 +30,8 @@ from . import _lib
 from .morphology.grey import _MODE_MAP, _resolve_element
 from .morphology.structure import _normalize_origin, _validate_origin, generate_binary_structure
 
+_TM_ERR_UNSUPPORTED = 2  # tm_status of a call outside a kernel's limits
+
 
 class RaggedBatch:
     """Items of different shapes (all 2-D or all 3-D) packed in one contiguous 1-D CUDA buffer."""
@@ -254,11 +256,25 @@ def binary_dilation(batch: RaggedBatch, structure=None, border_value=False, orig
 
 
 def binary_opening(batch, structure=None, border_value=False, origin=0):
+    """Per-item binary opening; 2-D items in one pass on bit-packed tiles."""
+    if batch.ndim == 2:
+        try:
+            return _binary("tm_ragged_binary_opening", batch, structure, border_value, origin, None)
+        except _lib.TorchmorphError as e:
+            if e.status != _TM_ERR_UNSUPPORTED:
+                raise
     return binary_dilation(binary_erosion(batch, structure, border_value, origin), structure, border_value,
                            origin)
 
 
 def binary_closing(batch, structure=None, border_value=False, origin=0):
+    """Per-item binary closing; 2-D items in one pass on bit-packed tiles."""
+    if batch.ndim == 2:
+        try:
+            return _binary("tm_ragged_binary_closing", batch, structure, border_value, origin, None)
+        except _lib.TorchmorphError as e:
+            if e.status != _TM_ERR_UNSUPPORTED:
+                raise
     return binary_erosion(binary_dilation(batch, structure, border_value, origin), structure, border_value,
                           origin)
 
