@@ -382,6 +382,21 @@ def grey_lines(args, dev, stream, hbm_peak):
         "us_per_call": round(t1 * 1e6, 1), "Gvoxel/s": round(nv / t1 / 1e9, 3),
         "frac_of_hbm": round(8 * nv / t1 / 1e9 / hbm_peak, 4),
         "two_operators_us": round(t2 * 1e6, 1), "speedup_vs_two_operators": round(t2 / t1, 2)}
+    # opening and white top-hat 3x3: one pass vs the reference's composition (two operator
+    # launches, and a subtraction for the top-hat)
+    for name, fn, comp in (
+            ("opening", lambda x: tm.grey_opening(x, size=3),
+             lambda x: _C.grey_dilation_cuda(_C.grey_erosion_cuda(x, st3, fp0, [0, 0], 1, 0.0), st3, fp0,
+                                             [0, 0], 1, 0.0)),
+            ("white_tophat", lambda x: tm.white_tophat(x, size=3),
+             lambda x: x - _C.grey_dilation_cuda(_C.grey_erosion_cuda(x, st3, fp0, [0, 0], 1, 0.0), st3, fp0,
+                                                 [0, 0], 1, 0.0))):
+        t1 = time_device(fn, xs, steps, args.warmup, stream) / steps
+        t2 = time_device(comp, xs, steps, args.warmup, stream) / steps
+        out[f"grey_{name}_3x3_8x4096x4096_one_pass"] = {
+            "us_per_call": round(t1 * 1e6, 1), "Gvoxel/s": round(nv / t1 / 1e9, 3),
+            "frac_of_hbm": round(8 * nv / t1 / 1e9 / hbm_peak, 4),
+            "composition_us": round(t2 * 1e6, 1), "speedup_vs_composition": round(t2 / t1, 2)}
     return out
 
 

@@ -74,3 +74,27 @@ def test_elements_outside_the_one_pass_kernel_compose(cuda):
     assert torch.equal(got, tm.grey_dilation(tm.grey_erosion(x, footprint=fp), footprint=fp))
     assert _C.grey_composite("closing", x, torch.zeros(35, 3), torch.empty(0, dtype=torch.bool), [0, 0], 1,
                              0.0) is None
+
+
+@pytest.mark.parametrize("kind", ["opening", "closing", "white_tophat", "black_tophat"])
+@pytest.mark.parametrize("size", [(3, 3), (5, 5)])
+@pytest.mark.parametrize("mode", ["reflect", "constant", "wrap"])
+def test_register_walkers_on_large_items(cuda, kind, size, mode):
+    """3 x 3 and 5 x 5 windows: outputs whose footprint lies inside the item come from the
+    register walkers (32-column strips, 64-row blocks, warp shuffles), the rest from the
+    tile kernel; both with a structure value and every origin, equal to the composition."""
+    r = rng(hash((kind, size, mode)) % 1000)
+    x = torch.from_numpy(r.random((2, 1, 300, 700)).astype(np.float32)).cuda()
+    codes = {"constant": 0, "reflect": 1, "nearest": 2, "mirror": 3, "wrap": 4}
+    k = size[0]
+    for oy in range(-(k // 2), (k - 1) // 2 + 1):
+        for ox in (-(k // 2), 0, (k - 1) // 2):
+            st = torch.full(size, 0.125)
+            got = _C.grey_composite(kind, x, st, torch.empty(0, dtype=torch.bool), [oy, ox], codes[mode], 0.3)
+            kw = dict(structure=st, mode=mode, cval=0.3, origin=(oy, ox))
+            if kind in ("opening", "white_tophat"):
+                op = tm.grey_dilation(tm.grey_erosion(x, **kw), **kw)
+            else:
+                op = tm.grey_erosion(tm.grey_dilation(x, **kw), **kw)
+            exp = x - op if kind == "white_tophat" else (op - x if kind == "black_tophat" else op)
+            assert torch.equal(got, exp), (oy, ox)

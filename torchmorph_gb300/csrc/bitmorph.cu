@@ -167,24 +167,44 @@ __global__ void __launch_bounds__(kBThreads) bitmorph_kernel(const uint8_t *__re
         const int ty = lt / tiles_x, tx = lt - ty * tiles_x;
         const int y0 = ty * kBTileH, x0 = tx * kBTileW;
         const uint8_t *src = in + off;
-        // ---- stage: one ballot per 32 bytes, 8 words of a row in flight per lane
-        for (int rw = warp; rw < srows; rw += kBThreads / 32) {
-            const int y = y0 - HY + rw;
-            const bool yin = (unsigned)y < (unsigned)H;
-            const uint8_t *row = src + (int64_t)y * W;
-            for (int j0 = 0; j0 < sld; j0 += 8) {
-                uint8_t b[8];
+        // ---- stage: every lane packs one 32-voxel word from the 8 (or 9, when the
+        // row segment is not 4-byte aligned) aligned 4-byte words that hold its 32
+        // bytes -- all its loads in flight at once.  Words reaching past the item's
+        // columns are packed by the whole warp instead: one byte per lane and a ballot.
+        const int nwords = srows * sld;
+        for (int e0 = warp * 32; e0 < nwords; e0 += kBThreads) {
+            const int e = e0 + lane;
+            const int rw = e / sld, j = e - rw * sld;
+            const int y = y0 - HY + rw, xs = x0 + 32 * (sjlo + j);
+            const bool valid = e < nwords;
+            const bool yin = valid && (unsigned)y < (unsigned)H;
+            const bool full = yin && xs >= 0 && xs + 32 <= W;
+            uint32_t word = bvw;
+            if (full) {
+                const uintptr_t a = reinterpret_cast<uintptr_t>(src + (int64_t)y * W + xs);
+                const uint32_t *w4 = reinterpret_cast<const uint32_t *>(a & ~(uintptr_t)3);
+                const int sh = (int)(a & 3) * 8;
+                uint32_t v[9];
 #pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    const int x = x0 + 32 * (sjlo + j0 + j) + lane;
-                    b[j] = (yin && (unsigned)x < (unsigned)W) ? row[x] : (uint8_t)ops.border;
-                }
+                for (int i = 0; i < 8; i++) v[i] = __ldg(w4 + i);
+                v[8] = sh ? __ldg(w4 + 8) : 0u;  // holds byte 31 exactly when the segment is unaligned
+                word = 0u;
 #pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    const uint32_t word = __ballot_sync(~0u, b[j] != 0);
-                    if (j0 + j < sld && lane == 0) S[rw * sld + j0 + j] = word;
+                for (int i = 0; i < 8; i++) {
+                    const uint32_t q = sh ? __funnelshift_r(v[i], v[i + 1], sh) : v[i];  // bytes 4i .. 4i+3, 0 or 1
+                    word |= ((q * 0x01020408u) >> 24) << (4 * i);
                 }
             }
+            // words partly outside the item's columns: the warp packs them one by one
+            for (unsigned part = __ballot_sync(~0u, yin && !full); part; part &= part - 1) {
+                const int src_lane = __ffs(part) - 1;
+                const int py = __shfl_sync(~0u, y, src_lane), pxs = __shfl_sync(~0u, xs, src_lane);
+                const int x = pxs + lane;
+                const bool inside = (unsigned)x < (unsigned)W;
+                const uint32_t bits = __ballot_sync(~0u, inside ? src[(int64_t)py * W + x] != 0 : ops.border != 0);
+                if (lane == src_lane) word = bits;
+            }
+            if (valid) S[e] = word;
         }
         __syncthreads();
         uint32_t res = 0u;

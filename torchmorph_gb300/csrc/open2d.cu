@@ -23,6 +23,7 @@
 // max(x) + s, rounded as the reference's per-tap x -/+ s (both are monotone
 // in x).  Top-hats: white = x - opening, black = closing - x, float32 as the
 // reference's torch subtraction.
+#include <algorithm>
 #include <cstring>
 
 #include "morph_tile.cuh"
@@ -41,6 +42,9 @@ struct Open2DParams {
     int mode;
     float cval, sval;
     int64_t batch;
+    // outputs computed by open2d_walk_kernel (the tile kernel skips them):
+    // rows ry0 <= y < ry1, columns rx0 <= x < rx1 of every item (empty when ry0 >= ry1)
+    int ry0, ry1, rx0, rx1;
 };
 
 enum { kTophatNone = 0, kTophatWhite = 1, kTophatBlack = 2 };
@@ -81,80 +85,215 @@ __global__ void __launch_bounds__(kOThreads) open2d_kernel(const float *__restri
     const int y0 = (rem / tiles_x) * kOTileH, x0 = (rem % tiles_x) * kOTileW;
     const float *src = in + item * (int64_t)p.H * p.W;
     float *dst = out + item * (int64_t)p.H * p.W;
-    const int tid = threadIdx.x;
+    if (y0 >= p.ry0 && y0 + kOTileH <= p.ry1 && x0 >= p.rx0 && x0 + kOTileW <= p.rx1) return;  // the walkers' part
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int kWarps = kOThreads / 32;
     const int iy0 = y0 + p.lo2y + p.lo1y, ix0 = x0 + p.lo2x + p.lo1x;  // item position of s0[0]
     const int my0 = y0 + p.lo2y, mx0 = x0 + p.lo2x;                    // item position of s1[0]
-    // stage the input region with the border mapping
-    for (int i = tid; i < RH0 * RW0; i += kOThreads) {
-        const int r = i / RW0, c = i - r * RW0;
-        const int yy = map_coord(iy0 + r, p.H, p.mode), xx = map_coord(ix0 + c, p.W, p.mode);
-        s0[i] = (yy < 0 || xx < 0) ? p.cval : src[(int64_t)yy * p.W + xx];
+    // stage the input region, a warp per row and every load of a row chunk in
+    // flight before its stores; the border mapping only for tiles that need it
+    const bool interior = iy0 >= 0 && ix0 >= 0 && iy0 + RH0 <= p.H && ix0 + RW0 <= p.W;
+    constexpr int kNC = 5;
+    for (int r = warp; r < RH0; r += kWarps) {
+        const int yy = interior ? iy0 + r : map_coord(iy0 + r, p.H, p.mode);
+        const float *row = src + (int64_t)(yy < 0 ? 0 : yy) * p.W;
+        for (int c0 = 0; c0 < RW0; c0 += 32 * kNC) {
+            float v[kNC];
+#pragma unroll
+            for (int j = 0; j < kNC; j++) {
+                const int c = c0 + lane + 32 * j;
+                v[j] = p.cval;
+                if (c < RW0) {
+                    const int xx = interior ? ix0 + c : map_coord(ix0 + c, p.W, p.mode);
+                    if (yy >= 0 && xx >= 0) v[j] = row[xx];
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < kNC; j++) {
+                const int c = c0 + lane + 32 * j;
+                if (c < RW0) s0[r * RW0 + c] = v[j];
+            }
+        }
     }
     __syncthreads();
     // first operator: row pass (RH0 x RW1), then column pass (RH1 x RW1)
-    for (int i = tid; i < RH0 * RW1; i += kOThreads) {
-        const int r = i / RW1, c = i - r * RW1;
-        const float *row = s0 + r * RW0 + c;
-        float acc = row[0];
-        for (int j = 1; j < p.kw; j++) acc = Op1::combine(acc, row[j]);
-        rowb[i] = acc;
-    }
+    for (int r = warp; r < RH0; r += kWarps)
+        for (int c = lane; c < RW1; c += 32) {
+            const float *row = s0 + r * RW0 + c;
+            float acc = row[0];
+            for (int j = 1; j < p.kw; j++) acc = Op1::combine(acc, row[j]);
+            rowb[r * RW1 + c] = acc;
+        }
     __syncthreads();
-    for (int i = tid; i < RH1 * RW1; i += kOThreads) {
-        const int r = i / RW1, c = i - r * RW1;
-        const float *col = rowb + r * RW1 + c;
-        float acc = col[0];
-        for (int j = 1; j < p.kh; j++) acc = Op1::combine(acc, col[j * RW1]);
-        s1[i] = Op1::apply(acc, p.sval);
-    }
+    for (int r = warp; r < RH1; r += kWarps)
+        for (int c = lane; c < RW1; c += 32) {
+            const float *col = rowb + r * RW1 + c;
+            float acc = col[0];
+            for (int j = 1; j < p.kh; j++) acc = Op1::combine(acc, col[j * RW1]);
+            s1[r * RW1 + c] = Op1::apply(acc, p.sval);
+        }
     __syncthreads();
     // the intermediate image's own border: positions outside the item take cval
-    // or the value at the mapped position (inside the item)
-    for (int i = tid; i < RH1 * RW1; i += kOThreads) {
-        const int r = i / RW1, c = i - r * RW1;
-        const int yy = my0 + r, xx = mx0 + c;
-        if ((unsigned)yy < (unsigned)p.H && (unsigned)xx < (unsigned)p.W) continue;
-        const int my = map_coord(yy, p.H, p.mode), mx = map_coord(xx, p.W, p.mode);
-        float v;
-        if (my < 0 || mx < 0) {
-            v = p.cval;
-        } else {
-            const int rr = my - my0, cc = mx - mx0;
-            v = ((unsigned)rr < (unsigned)RH1 && (unsigned)cc < (unsigned)RW1) ? s1[rr * RW1 + cc]
-                                                                               : first_at<MAX1>(src, p, my, mx);
-        }
-        rowb[i] = v;  // staged apart: every in-item value above stays readable
+    // or the value at the mapped position (inside the item); nothing to do when
+    // the whole intermediate region lies inside the item
+    if (!(my0 >= 0 && mx0 >= 0 && my0 + RH1 <= p.H && mx0 + RW1 <= p.W)) {
+        for (int r = warp; r < RH1; r += kWarps)
+            for (int c = lane; c < RW1; c += 32) {
+                const int yy = my0 + r, xx = mx0 + c;
+                if ((unsigned)yy < (unsigned)p.H && (unsigned)xx < (unsigned)p.W) continue;
+                const int my = map_coord(yy, p.H, p.mode), mx = map_coord(xx, p.W, p.mode);
+                float v;
+                if (my < 0 || mx < 0) {
+                    v = p.cval;
+                } else {
+                    const int rr = my - my0, cc = mx - mx0;
+                    v = ((unsigned)rr < (unsigned)RH1 && (unsigned)cc < (unsigned)RW1)
+                            ? s1[rr * RW1 + cc]
+                            : first_at<MAX1>(src, p, my, mx);
+                }
+                rowb[r * RW1 + c] = v;  // staged apart: every in-item value above stays readable
+            }
+        __syncthreads();
+        for (int r = warp; r < RH1; r += kWarps)
+            for (int c = lane; c < RW1; c += 32) {
+                const int yy = my0 + r, xx = mx0 + c;
+                if (!((unsigned)yy < (unsigned)p.H && (unsigned)xx < (unsigned)p.W)) s1[r * RW1 + c] = rowb[r * RW1 + c];
+            }
+        __syncthreads();
     }
-    __syncthreads();
-    for (int i = tid; i < RH1 * RW1; i += kOThreads) {
-        const int r = i / RW1, c = i - r * RW1;
-        const int yy = my0 + r, xx = mx0 + c;
-        if (!((unsigned)yy < (unsigned)p.H && (unsigned)xx < (unsigned)p.W)) s1[i] = rowb[i];
-    }
-    __syncthreads();
     // second operator: row pass (RH1 x 128), then the column pass to the outputs
-    for (int i = tid; i < RH1 * kOTileW; i += kOThreads) {
-        const int r = i / kOTileW, c = i - r * kOTileW;
-        const float *row = s1 + r * RW1 + c;
-        float acc = row[0];
-        for (int j = 1; j < p.kw; j++) acc = Op2::combine(acc, row[j]);
-        rowb[r * kOTileW + c] = acc;
-    }
-    __syncthreads();
-    for (int i = tid; i < kOTileH * kOTileW; i += kOThreads) {
-        const int r = i / kOTileW, c = i - r * kOTileW;
-        const int yy = y0 + r, xx = x0 + c;
-        if (yy >= p.H || xx >= p.W) continue;
-        const float *col = rowb + r * kOTileW + c;
-        float acc = col[0];
-        for (int j = 1; j < p.kh; j++) acc = Op2::combine(acc, col[j * kOTileW]);
-        float v = Op2::apply(acc, p.sval);
-        if (TOPHAT != kTophatNone) {
-            const float x = s0[(yy - iy0) * RW0 + (xx - ix0)];  // the input at (yy, xx)
-            v = TOPHAT == kTophatWhite ? x - v : v - x;
+    for (int r = warp; r < RH1; r += kWarps)
+        for (int c = lane; c < kOTileW; c += 32) {
+            const float *row = s1 + r * RW1 + c;
+            float acc = row[0];
+            for (int j = 1; j < p.kw; j++) acc = Op2::combine(acc, row[j]);
+            rowb[r * kOTileW + c] = acc;
         }
-        dst[(int64_t)yy * p.W + xx] = v;
+    __syncthreads();
+    for (int r = warp; r < kOTileH; r += kWarps) {
+        const int yy = y0 + r;
+        if (yy >= p.H) break;
+        const bool row_in = yy >= p.ry0 && yy < p.ry1;
+        for (int c = lane; c < kOTileW; c += 32) {
+            const int xx = x0 + c;
+            if (xx >= p.W) break;
+            if (row_in && xx >= p.rx0 && xx < p.rx1) continue;  // written by the walkers
+            const float *col = rowb + r * kOTileW + c;
+            float acc = col[0];
+            for (int j = 1; j < p.kh; j++) acc = Op2::combine(acc, col[j * kOTileW]);
+            float v = Op2::apply(acc, p.sval);
+            if (TOPHAT != kTophatNone) {
+                const float x = s0[(yy - iy0) * RW0 + (xx - ix0)];  // the input at (yy, xx)
+                v = TOPHAT == kTophatWhite ? x - v : v - x;
+            }
+            dst[(int64_t)yy * p.W + xx] = v;
+        }
     }
+}
+
+// Outputs whose whole input footprint (and the intermediate values they use)
+// lie inside the item, for compile-time KH x KW windows: each warp owns a strip
+// of 32 - (KW - 1) output columns and walks kWalkRows rows down it.  Lane l
+// holds the intermediate column x0 + lo2x + l: per input row it takes the first
+// operator's row window from L1-cached loads (the loads of 8 input rows in
+// flight together), the column window over the last KH rows in registers; the
+// second operator's row window for output column x0 + l reads lanes l .. l + KW - 1
+// by warp shuffles, its column window is again a register window.  No border
+// mapping anywhere: the rectangle excludes every output that would need it.
+constexpr int kWalkRows = 64;
+constexpr int kWalkChunk = 8;  // input rows whose loads are in flight together
+
+template <bool MAX1, int TOPHAT, int KH, int KW>
+__global__ void __launch_bounds__(256) open2d_walk_kernel(const float *__restrict__ in, float *__restrict__ out,
+                                                          Open2DParams p) {
+    using Op1 = MorphOp<float, MAX1>;
+    using Op2 = MorphOp<float, !MAX1>;
+    static_assert(KW <= 16 && KH >= 1, "window");
+    constexpr int kSW = 32 - (KW - 1);  // output columns per strip
+    const int lane = threadIdx.x & 31;
+    const int strips = (p.rx1 - p.rx0 + kSW - 1) / kSW, rblocks = (p.ry1 - p.ry0 + kWalkRows - 1) / kWalkRows;
+    const int64_t per_item = (int64_t)strips * rblocks;
+    const int64_t ntasks = p.batch * per_item;
+    for (int64_t task = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); task < ntasks;
+         task += (int64_t)gridDim.x * (blockDim.x / 32)) {
+        const int64_t item = task / per_item;
+        const int rem = (int)(task - item * per_item);
+        const int sx = rem % strips, by = rem / strips;
+        const int x0 = p.rx0 + kSW * sx, ya = p.ry0 + kWalkRows * by;
+        const int yb = min(ya + kWalkRows, p.ry1);
+        const float *src = in + item * (int64_t)p.H * p.W;
+        float *dst = out + item * (int64_t)p.H * p.W;
+        // Every column an output of the rectangle uses reads input columns
+        // c + lo1x .. c + lo1x + KW - 1 inside the item; columns no output uses
+        // (right of the rectangle) are clamped into that range, so every load stays
+        // inside the item and the values that matter are unchanged.
+        const int ci = min(x0 + p.lo2x + lane, p.W - KW - p.lo1x);
+        const int i0 = ya + p.lo2y;  // first intermediate row
+        float h1[KH];  // the first operator's row results of the last KH input rows
+        float v2[KH];  // the second operator's row results of the last KH intermediate rows
+        auto row1 = [&](int y) {  // first operator's row window at input row y
+            const float *r = src + (int64_t)y * p.W + ci + p.lo1x;
+            float acc = __ldg(r);
+#pragma unroll
+            for (int j = 1; j < KW; j++) acc = Op1::combine(acc, __ldg(r + j));
+            return acc;
+        };
+#pragma unroll
+        for (int k = 0; k < KH - 1; k++) h1[k] = row1(i0 + p.lo1y + k);
+        const int nint = (yb - ya) + KH - 1;            // intermediate rows to produce
+        const int ylast = i0 + p.lo1y + nint + KH - 2;  // last input row read
+        for (int t0 = 0; t0 < nint; t0 += kWalkChunk) {
+            float ra[kWalkChunk];  // rows past the end repeat the last row
+#pragma unroll
+            for (int u = 0; u < kWalkChunk; u++) ra[u] = row1(min(i0 + p.lo1y + t0 + u + KH - 1, ylast));
+#pragma unroll
+            for (int u = 0; u < kWalkChunk; u++) {
+                const int t = t0 + u;
+                if (t >= nint) break;
+                h1[KH - 1] = ra[u];
+                float iv = h1[0];
+#pragma unroll
+                for (int k = 1; k < KH; k++) iv = Op1::combine(iv, h1[k]);
+                iv = Op1::apply(iv, p.sval);
+#pragma unroll
+                for (int k = 0; k < KH - 1; k++) h1[k] = h1[k + 1];
+                float acc = iv;
+#pragma unroll
+                for (int j = 1; j < KW; j++) acc = Op2::combine(acc, __shfl_down_sync(~0u, iv, j));
+                v2[KH - 1] = acc;
+                if (t >= KH - 1) {  // output row ya + t - (KH - 1)
+                    float o = v2[0];
+#pragma unroll
+                    for (int k = 1; k < KH; k++) o = Op2::combine(o, v2[k]);
+                    o = Op2::apply(o, p.sval);
+                    const int y = ya + t - (KH - 1), x = x0 + lane;
+                    if (lane < kSW && x < p.rx1) {
+                        if (TOPHAT != kTophatNone) {
+                            const float xv = __ldg(src + (int64_t)y * p.W + x);
+                            o = TOPHAT == kTophatWhite ? xv - o : o - xv;
+                        }
+                        dst[(int64_t)y * p.W + x] = o;
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < KH - 1; k++) v2[k] = v2[k + 1];
+            }
+        }
+    }
+}
+
+// The rectangle of outputs the walkers can take (see open2d_walk_kernel).
+void walk_rect(Open2DParams &p) {
+    // output y reads intermediate rows y + lo2y .. y + lo2y + kh - 1 (all inside the item)
+    // and those read input rows + lo1y .. + lo1y + kh - 1 (all inside the item)
+    auto range = [](int lo1, int lo2, int k, int n, int &a, int &b) {
+        a = std::max(-lo2, -(lo2 + lo1));
+        b = std::min(n - (lo2 + k - 1), n - (lo2 + lo1 + 2 * k - 2));
+        if (b < a) b = a;
+    };
+    range(p.lo1y, p.lo2y, p.kh, p.H, p.ry0, p.ry1);
+    range(p.lo1x, p.lo2x, p.kw, p.W, p.rx0, p.rx1);
+    if (p.ry1 <= p.ry0 || p.rx1 <= p.rx0) p.ry0 = p.ry1 = p.rx0 = p.rx1 = 0;
 }
 
 size_t open2d_smem(int kh, int kw) {
@@ -209,6 +348,18 @@ int run_open2d(const float *in, float *out, int64_t batch, int ndim, const int64
     p.cval = cval;
     p.sval = sval;
     p.batch = batch;
+    p.ry0 = p.ry1 = p.rx0 = p.rx1 = 0;
+    const bool walk = ndim == 2 && ((p.kh == 3 && p.kw == 3) || (p.kh == 5 && p.kw == 5));
+    if (walk) walk_rect(p);
+    if (p.ry1 > p.ry0) {
+        const int sw = 32 - (p.kw - 1);
+        const int64_t tasks = batch * (int64_t)((p.rx1 - p.rx0 + sw - 1) / sw) *
+                              ((p.ry1 - p.ry0 + kWalkRows - 1) / kWalkRows);
+        const int64_t blocks = std::min<int64_t>(ceil_div(tasks, 8), (int64_t)sm_count() * 8);
+        if (p.kh == 3) open2d_walk_kernel<MAX1, TOPHAT, 3, 3><<<(unsigned)blocks, 256, 0, s>>>(in, out, p);
+        else open2d_walk_kernel<MAX1, TOPHAT, 5, 5><<<(unsigned)blocks, 256, 0, s>>>(in, out, p);
+        TM_LAUNCH_CHECK("open2d_walk_kernel");
+    }
     const size_t smem = open2d_smem(p.kh, p.kw);
     auto kernel = open2d_kernel<MAX1, TOPHAT>;
     if (smem > 48 * 1024)
