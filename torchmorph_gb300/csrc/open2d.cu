@@ -45,6 +45,8 @@ struct Open2DParams {
     // outputs computed by open2d_walk_kernel (the tile kernel skips them):
     // rows ry0 <= y < ry1, columns rx0 <= x < rx1 of every item (empty when ry0 >= ry1)
     int ry0, ry1, rx0, rx1;
+    // tiles (32 x 128) inside that rectangle: tile rows [tr0, tr1), columns [tc0, tc1)
+    int tr0, tr1, tc0, tc1;
 };
 
 enum { kTophatNone = 0, kTophatWhite = 1, kTophatBlack = 2 };
@@ -80,12 +82,27 @@ __global__ void __launch_bounds__(kOThreads) open2d_kernel(const float *__restri
     float *rowb = s0 + RH0 * RW0;     // row pass of either operator, RH0 x RW1
     float *s1 = rowb + RH0 * RW1;     // intermediate, RH1 x RW1
     const int tiles_x = (p.W + kOTileW - 1) / kOTileW, tiles_y = (p.H + kOTileH - 1) / kOTileH;
-    const int64_t item = blockIdx.x / ((int64_t)tiles_x * tiles_y);
-    const int rem = (int)(blockIdx.x - item * (int64_t)tiles_x * tiles_y);
-    const int y0 = (rem / tiles_x) * kOTileH, x0 = (rem % tiles_x) * kOTileW;
+    // this CTA's tile: the k-th of the item's tiles that the walkers do not cover
+    // entirely (tile rows [tr0, tr1) and columns [tc0, tc1) are theirs)
+    const int ring = tiles_x * tiles_y - (p.tr1 - p.tr0) * (p.tc1 - p.tc0);
+    const int64_t item = blockIdx.x / ring;
+    int k = (int)(blockIdx.x - item * ring), ty, tx;
+    const int top = p.tr0 * tiles_x, side = p.tc0 + (tiles_x - p.tc1);
+    if (k < top) {
+        ty = k / tiles_x;
+        tx = k % tiles_x;
+    } else if ((k -= top) < (p.tr1 - p.tr0) * side) {
+        ty = p.tr0 + k / side;
+        tx = k % side;
+        if (tx >= p.tc0) tx += p.tc1 - p.tc0;
+    } else {
+        k -= (p.tr1 - p.tr0) * side;
+        ty = p.tr1 + k / tiles_x;
+        tx = k % tiles_x;
+    }
+    const int y0 = ty * kOTileH, x0 = tx * kOTileW;
     const float *src = in + item * (int64_t)p.H * p.W;
     float *dst = out + item * (int64_t)p.H * p.W;
-    if (y0 >= p.ry0 && y0 + kOTileH <= p.ry1 && x0 >= p.rx0 && x0 + kOTileW <= p.rx1) return;  // the walkers' part
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int kWarps = kOThreads / 32;
     const int iy0 = y0 + p.lo2y + p.lo1y, ix0 = x0 + p.lo2x + p.lo1x;  // item position of s0[0]
@@ -195,13 +212,14 @@ __global__ void __launch_bounds__(kOThreads) open2d_kernel(const float *__restri
 // lie inside the item, for compile-time KH x KW windows: each warp owns a strip
 // of 32 - (KW - 1) output columns and walks kWalkRows rows down it.  Lane l
 // holds the intermediate column x0 + lo2x + l: per input row it takes the first
-// operator's row window from L1-cached loads (the loads of 8 input rows in
-// flight together), the column window over the last KH rows in registers; the
+// operator's row window from L1-cached loads (the loads of the next 8 input rows
+// in flight while the current 8 are used), the column window over the last KH
+// rows in registers; the
 // second operator's row window for output column x0 + l reads lanes l .. l + KW - 1
 // by warp shuffles, its column window is again a register window.  No border
 // mapping anywhere: the rectangle excludes every output that would need it.
 constexpr int kWalkRows = 64;
-constexpr int kWalkChunk = 8;  // input rows whose loads are in flight together
+constexpr int kWalkChunk = 8;  // input rows per chunk (two chunks of loads in flight)
 
 template <bool MAX1, int TOPHAT, int KH, int KW>
 __global__ void __launch_bounds__(256) open2d_walk_kernel(const float *__restrict__ in, float *__restrict__ out,
@@ -242,10 +260,20 @@ __global__ void __launch_bounds__(256) open2d_walk_kernel(const float *__restric
         for (int k = 0; k < KH - 1; k++) h1[k] = row1(i0 + p.lo1y + k);
         const int nint = (yb - ya) + KH - 1;            // intermediate rows to produce
         const int ylast = i0 + p.lo1y + nint + KH - 2;  // last input row read
-        for (int t0 = 0; t0 < nint; t0 += kWalkChunk) {
-            float ra[kWalkChunk];  // rows past the end repeat the last row
+        // the loads of the next chunk are issued before the current chunk is used
+        // (two chunks in flight); rows past the end repeat the last row
+        float nxt[kWalkChunk];
 #pragma unroll
-            for (int u = 0; u < kWalkChunk; u++) ra[u] = row1(min(i0 + p.lo1y + t0 + u + KH - 1, ylast));
+        for (int u = 0; u < kWalkChunk; u++) nxt[u] = row1(min(i0 + p.lo1y + u + KH - 1, ylast));
+        for (int t0 = 0; t0 < nint; t0 += kWalkChunk) {
+            float ra[kWalkChunk];
+#pragma unroll
+            for (int u = 0; u < kWalkChunk; u++) ra[u] = nxt[u];
+            if (t0 + kWalkChunk < nint) {
+#pragma unroll
+                for (int u = 0; u < kWalkChunk; u++)
+                    nxt[u] = row1(min(i0 + p.lo1y + t0 + kWalkChunk + u + KH - 1, ylast));
+            }
 #pragma unroll
             for (int u = 0; u < kWalkChunk; u++) {
                 const int t = t0 + u;
@@ -360,13 +388,24 @@ int run_open2d(const float *in, float *out, int64_t batch, int ndim, const int64
         else open2d_walk_kernel<MAX1, TOPHAT, 5, 5><<<(unsigned)blocks, 256, 0, s>>>(in, out, p);
         TM_LAUNCH_CHECK("open2d_walk_kernel");
     }
+    // tiles entirely inside the walkers' rectangle are skipped by the tile kernel
+    const int tiles_x = (int)ceil_div(p.W, kOTileW), tiles_y = (int)ceil_div(p.H, kOTileH);
+    p.tr0 = p.tr1 = p.tc0 = p.tc1 = 0;
+    if (p.ry1 > p.ry0) {
+        p.tr0 = (int)ceil_div(p.ry0, kOTileH);
+        p.tr1 = std::max(p.tr0, p.ry1 / kOTileH);
+        p.tc0 = (int)ceil_div(p.rx0, kOTileW);
+        p.tc1 = std::max(p.tc0, p.rx1 / kOTileW);
+        if (p.tr1 == p.tr0 || p.tc1 == p.tc0) p.tr0 = p.tr1 = p.tc0 = p.tc1 = 0;
+    }
     const size_t smem = open2d_smem(p.kh, p.kw);
     auto kernel = open2d_kernel<MAX1, TOPHAT>;
     if (smem > 48 * 1024)
         TM_CHECK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int64_t tiles = batch * ceil_div(p.W, kOTileW) * ceil_div(p.H, kOTileH);
+    const int64_t ring = (int64_t)tiles_x * tiles_y - (int64_t)(p.tr1 - p.tr0) * (p.tc1 - p.tc0);
+    const int64_t tiles = batch * ring;
     if (tiles >= ((int64_t)1 << 31)) return fail(TM_ERR_TOO_LARGE, "too many tiles");
-    kernel<<<(unsigned)tiles, kOThreads, smem, s>>>(in, out, p);
+    if (tiles > 0) kernel<<<(unsigned)tiles, kOThreads, smem, s>>>(in, out, p);
     TM_LAUNCH_CHECK("open2d_kernel");
     return TM_OK;
 }
