@@ -255,48 +255,6 @@ __device__ void cdt_finalize(const int32_t *dt, const int32_t *ft, float *__rest
     }
 }
 
-struct CdtControl {
-    unsigned barrier_count;
-    unsigned barrier_gen;
-    int abort;
-    int pad[61];
-};
-static_assert(sizeof(CdtControl) == 256, "control block is 256 bytes");
-
-__device__ bool cdt_barrier(CdtControl *ctl, int *status, long long spin_limit) {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned *gen = &ctl->barrier_gen;
-        volatile int *abort = &ctl->abort;
-        const unsigned g = *gen;
-        __threadfence();
-        int ok = 1;
-        if (atomicAdd(&ctl->barrier_count, 1u) == gridDim.x - 1) {
-            ctl->barrier_count = 0;
-            __threadfence();
-            atomicAdd(&ctl->barrier_gen, 1u);
-        } else {
-            long long polls = 0;
-            while (*gen == g) {
-                if (*abort || ++polls > spin_limit) {
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        if (!ok) {
-            atomicExch(&ctl->abort, 1);
-            if (status) atomicExch(status, TM_DEV_ERR_TIMEOUT);
-        }
-        __threadfence();
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
-
 struct CdtRasterArgs {
     const void *in;
     int32_t *dt, *ft;
@@ -307,7 +265,7 @@ struct CdtRasterArgs {
     float divisor;
     const int *todo;  // per-item flags of the shell search (NULL: every item)
     const int *any;   // flag after them: some item is marked
-    CdtControl *ctl;
+    GridControl *ctl;
     int *status;
     long long spin_limit;
 };
@@ -321,16 +279,16 @@ template <typename In>
 __global__ void __launch_bounds__(kCdtThreads, 1) cdt_raster_kernel(CdtRasterArgs a, CdtParams p, CdtOffsets offs) {
     if (a.any && !*(volatile const int *)a.any) return;  // uniform: every CTA leaves
     cdt_count(a.cnt, p);
-    if (!cdt_barrier(a.ctl, a.status, a.spin_limit)) return;
+    if (!grid_barrier_bounded(a.ctl, gridDim.x, a.status, a.spin_limit)) return;
     if (blockIdx.x == 0) cdt_scan(a.cnt, a.woff, p.T);
     cdt_init(static_cast<const In *>(a.in), a.dt, a.ft, a.numel, p.numel_item, a.todo);
-    if (!cdt_barrier(a.ctl, a.status, a.spin_limit)) return;
+    if (!grid_barrier_bounded(a.ctl, gridDim.x, a.status, a.spin_limit)) return;
     cdt_scatter(a.woff, a.cur, a.order, p);
-    if (!cdt_barrier(a.ctl, a.status, a.spin_limit)) return;
+    if (!grid_barrier_bounded(a.ctl, gridDim.x, a.status, a.spin_limit)) return;
     // an item's two passes run on the same CTA: no grid barrier between them
     cdt_pass<false>(a.dt, a.ft, a.order, a.woff, p, offs, a.todo);
     cdt_pass<true>(a.dt, a.ft, a.order, a.woff, p, offs, a.todo);
-    if (!cdt_barrier(a.ctl, a.status, a.spin_limit)) return;
+    if (!grid_barrier_bounded(a.ctl, gridDim.x, a.status, a.spin_limit)) return;
     cdt_finalize(a.dt, a.ft, a.dist, a.indices, a.numel, p.numel_item, p.ndim, p, a.divisor, a.todo);
 }
 
@@ -361,7 +319,7 @@ CdtPlan plan_cdt(const Geometry &g) {
     pl.cur_off = o;
     o += align256((size_t)pl.T * 4);
     pl.ctl_off = o;  // the raster launch's barrier block, right after the counters
-    o += sizeof(CdtControl);
+    o += sizeof(GridControl);
     pl.total = o;
     return pl;
 }
@@ -369,7 +327,7 @@ CdtPlan plan_cdt(const Geometry &g) {
 // Zero the wavefront counters and the barrier block of the raster launch
 // (contiguous in the workspace: one memset).
 cudaError_t clear_cdt_counters(unsigned char *ws, const CdtPlan &pl, cudaStream_t stream) {
-    return cudaMemsetAsync(ws + pl.cnt_off, 0, pl.ctl_off + sizeof(CdtControl) - pl.cnt_off, stream);
+    return cudaMemsetAsync(ws + pl.cnt_off, 0, pl.ctl_off + sizeof(GridControl) - pl.cnt_off, stream);
 }
 
 template <typename In>
@@ -421,7 +379,7 @@ int run_cdt(const In *in, const Geometry &g, int metric, float *dist, int32_t *i
     a.woff = reinterpret_cast<int *>(ws + pl.woff_off);
     a.cnt = reinterpret_cast<int *>(ws + pl.cnt_off);
     a.cur = reinterpret_cast<int *>(ws + pl.cur_off);
-    a.ctl = reinterpret_cast<CdtControl *>(ws + pl.ctl_off);
+    a.ctl = reinterpret_cast<GridControl *>(ws + pl.ctl_off);
     a.dist = dist;
     a.indices = indices;
     a.numel = g.numel;

@@ -1133,7 +1133,7 @@ __global__ void __launch_bounds__(kC12Threads, 2) ragged_edt3_kernel(RaggedC12Ar
             }
         }
     }
-    if (!grid_barrier_bounded(A.ctl, A.status, A.spin_limit)) return;
+    if (!grid_barrier_bounded(A.ctl, gridDim.x, A.status, A.spin_limit)) return;
     // passes 1 + 2: one plane of one item per CTA at a time
     const ReItem &last = items[A.nitems - 1];
     const int64_t nplanes = (int64_t)last.plane_begin + last.shape[0];

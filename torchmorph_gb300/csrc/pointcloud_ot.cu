@@ -97,41 +97,6 @@ struct PcArgs {
     long long spin_limit;  // polls a barrier wait may take (tm_set_grid_wait_budget)
 };
 
-// Bounded grid barrier (sense by generation).  Returns false when it gave up
-// or another CTA aborted.
-__device__ bool grid_barrier(PcControl *ctl, unsigned nblocks, int *status, long long spin_limit) {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned *gen = &ctl->barrier_gen;
-        volatile int *abort = &ctl->abort;
-        const unsigned g = *gen;
-        __threadfence();
-        int ok = 1;
-        if (atomicAdd(&ctl->barrier_count, 1u) == nblocks - 1) {
-            ctl->barrier_count = 0;
-            __threadfence();
-            atomicAdd(&ctl->barrier_gen, 1u);
-        } else {
-            long long polls = 0;
-            while (*gen == g) {
-                if (*abort || ++polls > spin_limit) {
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        if (!ok) {
-            atomicExch(&ctl->abort, 1);
-            if (status) atomicExch(status, TM_DEV_ERR_TIMEOUT);
-        }
-        __threadfence();
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
 
 __device__ __forceinline__ int find_problem(const PcProblem *prob, int nprob, int tile, bool rows) {
     int lo = 0, hi = nprob - 1;
@@ -313,7 +278,7 @@ __global__ void __launch_bounds__(kPcThreads) pc_sinkhorn_kernel(PcArgs a) {
                         (tile - P.row_tile0) * kPcTile, P.n, P.m, a.eps, make_float3(P.ox, P.oy, P.oz), nullptr,
                         nullptr, s_part);
         }
-        if (!grid_barrier(a.ctl, nblocks, a.status, a.spin_limit)) return;
+        if (!grid_barrier_bounded(a.ctl, nblocks, a.status, a.spin_limit)) return;
         const bool check = ((it + 1) % a.check_every == 0) || it + 1 == a.max_iter;
         // g-update over the column tiles (+ the column-marginal error on check iterations)
         const int ncol = *(volatile int *)&a.ctl->n_col_list;
@@ -340,7 +305,7 @@ __global__ void __launch_bounds__(kPcThreads) pc_sinkhorn_kernel(PcArgs a) {
                 if (threadIdx.x == 0) atomicAdd(&a.err[p], s_err);
             }
         }
-        if (!grid_barrier(a.ctl, nblocks, a.status, a.spin_limit)) return;
+        if (!grid_barrier_bounded(a.ctl, nblocks, a.status, a.spin_limit)) return;
         if (check) {
             if (blockIdx.x == 0) {
                 for (int p = threadIdx.x; p < a.nprob; p += kPcThreads) {
@@ -355,7 +320,7 @@ __global__ void __launch_bounds__(kPcThreads) pc_sinkhorn_kernel(PcArgs a) {
                 rebuild_lists(a, s_scan);
                 __threadfence();
             }
-            if (!grid_barrier(a.ctl, nblocks, a.status, a.spin_limit)) return;
+            if (!grid_barrier_bounded(a.ctl, nblocks, a.status, a.spin_limit)) return;
             if (*(volatile int *)&a.ctl->n_active <= 0) {
                 it++;
                 break;

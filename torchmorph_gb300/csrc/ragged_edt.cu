@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(kReThreads) ragged_edt_kernel(ReArgs A) {
                 }
             }
         }
-        if (!last && !grid_barrier_bounded(A.ctl, A.status, A.spin_limit)) return;
+        if (!last && !grid_barrier_bounded(A.ctl, gridDim.x, A.status, A.spin_limit)) return;
     }
 }
 

@@ -84,41 +84,6 @@ struct SkArgs {
     bool vec;                    // d % 4 == 0 and 16-byte aligned operands: float4 staging
 };
 
-// Bounded grid barrier (generation counter).  Returns false when this CTA gave
-// up or another CTA aborted; the caller then leaves the kernel.
-__device__ bool sk_grid_barrier(SkControl *ctl, int *status, long long spin_limit) {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned *gen = &ctl->barrier_gen;
-        volatile int *abort = &ctl->abort;
-        const unsigned g = *gen;
-        __threadfence();
-        int ok = 1;
-        if (atomicAdd(&ctl->barrier_count, 1u) == gridDim.x - 1) {
-            ctl->barrier_count = 0;
-            __threadfence();
-            atomicAdd(&ctl->barrier_gen, 1u);
-        } else {
-            long long polls = 0;
-            while (*gen == g) {
-                if (*abort || ++polls > spin_limit) {
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        if (!ok) {
-            atomicExch(&ctl->abort, 1);
-            if (status) atomicExch(status, TM_DEV_ERR_TIMEOUT);
-        }
-        __threadfence();
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
 
 struct SkStage {
     float mat[2][kSkRows * kSkPitch];
@@ -332,7 +297,7 @@ __global__ void __launch_bounds__(kSkThreads, 2) sk_solve_kernel(SkArgs A) {
             sk_tile<LOG, MB>(A, st, rb * kSkRows, pb * TB, A.num_u, A.mat, A.v, A.u,
                              checking ? A.partial + (size_t)rb * A.n : nullptr);
         }
-        if (!sk_grid_barrier(A.ctl, A.status, A.spin_limit)) return;
+        if (!grid_barrier_bounded(A.ctl, gridDim.x, A.status, A.spin_limit)) return;
         if (checking) {  // per-pair residual sums, one warp per pair, fixed order
             const int warps = gridDim.x * (kSkThreads / 32);
             const int lane = threadIdx.x & 31;
@@ -351,7 +316,7 @@ __global__ void __launch_bounds__(kSkThreads, 2) sk_solve_kernel(SkArgs A) {
             const int rb = t / pair_blocks, pb = t % pair_blocks;
             sk_tile<LOG, MB>(A, st, rb * kSkRows, pb * TB, A.num_v, A.mat_t, A.u, A.v, nullptr);
         }
-        if (!sk_grid_barrier(A.ctl, A.status, A.spin_limit)) return;
+        if (!grid_barrier_bounded(A.ctl, gridDim.x, A.status, A.spin_limit)) return;
         if (checking) {
             const bool stop = *((volatile int *)&A.notconv[check]) == 0;
             check++;

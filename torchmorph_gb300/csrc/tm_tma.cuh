@@ -34,35 +34,38 @@ constexpr long long kSpinLimit = 1LL << 26;
 long long grid_wait_budget();
 
 // Control block of a cooperative launch whose CTAs meet at grid barriers;
-// zeroed before the launch.
+// zeroed before the launch.  Kernels with more launch-wide state keep their
+// own 256-byte block with the same first three fields.
 struct GridControl {
-    unsigned count;  // CTAs arrived at the current barrier
-    unsigned gen;    // barriers completed
-    int abort;       // set by a CTA whose wait gave up: every CTA leaves
+    unsigned barrier_count;  // CTAs arrived at the current barrier
+    unsigned barrier_gen;    // barriers completed
+    int abort;               // set by a CTA whose wait gave up: every CTA leaves
     int pad[61];
 };
 static_assert(sizeof(GridControl) == 256, "control block is 256 bytes");
 
-// Barrier of all CTAs of a cooperative launch (all co-resident).  The last
-// CTA to arrive resets the count and advances the generation; the others
-// poll the generation at most spin_limit times.  A wait that gives up (or
-// sees another CTA's abort) sets the abort flag and TM_DEV_ERR_TIMEOUT in
+// Barrier of the `nblocks` CTAs of a cooperative launch (all co-resident).
+// The last CTA to arrive resets the count and advances the generation; the
+// others poll the generation at most spin_limit times.  A wait that gives up
+// (or sees another CTA's abort) sets the abort flag and TM_DEV_ERR_TIMEOUT in
 // `status`; the barrier then returns false in every CTA that reaches it, and
 // the caller returns.  Writes before the barrier are visible to loads after
 // it that bypass L1 (__ldcg, or data this CTA has not cached).
-__device__ inline bool grid_barrier_bounded(GridControl *ctl, int *status, long long spin_limit) {
+// Ctl: a control block with barrier_count, barrier_gen and abort.
+template <typename Ctl>
+__device__ inline bool grid_barrier_bounded(Ctl *ctl, unsigned nblocks, int *status, long long spin_limit) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned *gen = &ctl->gen;
+        volatile unsigned *gen = &ctl->barrier_gen;
         volatile int *abort = &ctl->abort;
         const unsigned g = *gen;
         __threadfence();
         int ok = 1;
-        if (atomicAdd(&ctl->count, 1u) == gridDim.x - 1) {
-            ctl->count = 0;
+        if (atomicAdd(&ctl->barrier_count, 1u) == nblocks - 1) {
+            ctl->barrier_count = 0;
             __threadfence();
-            atomicAdd(&ctl->gen, 1u);
+            atomicAdd(&ctl->barrier_gen, 1u);
         } else {
             long long polls = 0;
             while (*gen == g) {
