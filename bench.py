@@ -400,16 +400,16 @@ def grey_lines(args, dev, stream, hbm_peak):
     return out
 
 
-def secondary(args, dev, stream, hbm_peak):
-    """Grey/binary dilation, chamfer and Sinkhorn lines (rank 0 only)."""
+def binary_lines(args, dev, stream, hbm_peak):
+    """Binary dilation 3x3 box at 8 x 256^2 (L2 resident) and, HBM resident at 8 x 4096^2
+    (bit-packed tiles), erosion with the default cross and the one-pass opening."""
     import torch
 
     import torchmorph_gb300 as tm
     from torchmorph_gb300 import _C
 
-    out = grey_lines(args, dev, stream, hbm_peak)
+    out = {}
     g = torch.Generator(device="cpu").manual_seed(1)
-
     xb = (torch.rand((8, 1, 256, 256), generator=g) > 0.5).to(dev)
     box = torch.ones((3, 3), dtype=torch.bool)
 
@@ -420,6 +420,24 @@ def secondary(args, dev, stream, hbm_peak):
     t = time_device(bstep, [xb], steps, args.warmup, stream)
     out["binary_dilation_3x3_8x256x256"] = {"Gvoxel/s": round(xb.numel() / (t / steps) / 1e9, 3),
                                             "us_per_call": round(t / steps * 1e6, 2)}
+    # HBM-resident binary lines (bit-packed tiles): erosion with the default cross and the
+    # one-pass opening, 8 x 4096^2 bool, two rotating inputs; 1 B in + 1 B out per voxel
+    xbs = [(torch.rand((8, 1, 4096, 4096), generator=g) > 0.5).to(dev) for _ in range(2)]
+    nbv = xbs[0].numel()
+    for name, fn in (("binary_erosion_cross_8x4096x4096", lambda x: tm.binary_erosion(x)),
+                     ("binary_opening_cross_8x4096x4096_one_pass", lambda x: tm.binary_opening(x))):
+        tb = time_device(fn, xbs, steps, args.warmup, stream) / steps
+        out[name] = {"us_per_call": round(tb * 1e6, 1), "Gvoxel/s": round(nbv / tb / 1e9, 3),
+                     "frac_of_hbm": round(2.0 * nbv / tb / 1e9 / hbm_peak, 4)}
+    t2 = time_device(lambda x: tm.binary_dilation(tm.binary_erosion(x)), xbs, steps, args.warmup, stream) / steps
+    out["binary_opening_cross_8x4096x4096_one_pass"]["composition_us"] = round(t2 * 1e6, 1)
+    return out
+
+
+def secondary(args, dev, stream, hbm_peak):
+    """Grey/binary, chamfer, EDT shapes, ragged and Sinkhorn lines (rank 0 only)."""
+    out = grey_lines(args, dev, stream, hbm_peak)
+    out.update(binary_lines(args, dev, stream, hbm_peak))
 
     hbm = peaks()[0]
     out.update(cdt_lines(args, dev, stream))
@@ -982,7 +1000,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--case", choices=["all", "grey", "cdt", "sinkhorn", "ragged", "ragged3d", "edt-shapes", "pointcloud",
+    ap.add_argument("--case", choices=["all", "grey", "binary", "cdt", "sinkhorn", "ragged", "ragged3d", "edt-shapes", "pointcloud",
                                        "pointcloud-profile"],
                     default="all",
                     help="only the shared-cost Sinkhorn, ragged-batch or point-cloud lines (one JSON object); "
@@ -1004,6 +1022,8 @@ def main():
             print(json.dumps(pointcloud_profile_case(dev)))
         elif args.case == "ragged3d":
             print(json.dumps(ragged_volume_lines(dev, stream, max(args.steps, 10), args.warmup)))
+        elif args.case == "binary":
+            print(json.dumps(binary_lines(args, dev, stream, peaks()[0])))
         elif args.case == "cdt":
             print(json.dumps(cdt_lines(args, dev, stream)))
         elif args.case == "edt-shapes":

@@ -234,14 +234,28 @@ __global__ void __launch_bounds__(kBThreads) bitmorph_kernel(const uint8_t *__re
             __syncthreads();
             res = bit_op(I, ild, ijlo, hy2, r, w, t2, ops.or2);
         }
-        // ---- output: lane writes byte `lane` of each of its warp's words
+        // ---- output: a warp writes its 8 rows one at a time; lane l writes columns
+        // x0 + 4l .. x0 + 4l + 3, its nibble of the row's words spread to one byte
+        // per bit by a multiply -- one 4-byte store when the row segment is 4-byte
+        // aligned and inside the item, bytes otherwise
         uint8_t *dst = out + off;
         const int wr0 = warp * (32 / kBWords);  // first tile row of this warp
 #pragma unroll
-        for (int q = 0; q < 32; q++) {  // (row in warp, word) pairs, one per source lane
-            const uint32_t word = __shfl_sync(~0u, res, q);
-            const int y = y0 + wr0 + q / kBWords, x = x0 + 32 * (q % kBWords) + lane;
-            if (y < H && x < W) dst[(int64_t)y * W + x] = (uint8_t)((word >> lane) & 1u);
+        for (int rr = 0; rr < 32 / kBWords; rr++) {
+            const uint32_t word = __shfl_sync(~0u, res, rr * kBWords + (lane >> 3));
+            const int y = y0 + wr0 + rr;
+            if (y >= H) break;  // warp-uniform
+            const uint32_t nib = (word >> (4 * (lane & 7))) & 15u;
+            const uint32_t bytes = (nib * 0x00204081u) & 0x01010101u;
+            const int x = x0 + 4 * lane;
+            uint8_t *row = dst + (int64_t)y * W;
+            if ((reinterpret_cast<uintptr_t>(row + x0) & 3) == 0 && x + 3 < W) {
+                *reinterpret_cast<uint32_t *>(row + x) = bytes;
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    if (x + k < W) row[x + k] = (uint8_t)((bytes >> (8 * k)) & 1u);
+            }
         }
     }
 }

@@ -36,7 +36,9 @@ def _binary_morphology(input, structure, iterations, mask, output, border_value,
     structure = _normalize_structure(structure, nd)
     origin = _normalize_origin(origin, nd)
     _validate_origin(origin, structure)
-    x = input != 0
+    # foreground as bool (a bool input is used as is: comparing it with 0 is a slow
+    # promoted elementwise pass)
+    x = input.contiguous() if input.dtype == torch.bool else input != 0
     original = x
     if mask is not None and mask.shape != input.shape:
         raise ValueError(f"mask shape {mask.shape} must match input shape {input.shape}")
@@ -105,7 +107,8 @@ def binary_fill_holes(input, structure=None, output=None, origin=0) -> Tensor:
     validate_bcs_input(input)
     validate_output(input, output)
     outside = binary_propagation(torch.zeros_like(input, dtype=torch.bool), structure=structure,
-                                 mask=input == 0, output=None, border_value=True, origin=origin)
+                                 mask=torch.logical_not(input) if input.dtype == torch.bool else input == 0,
+                                 output=None, border_value=True, origin=origin)
     result = torch.logical_not(outside)
     if output is not None:
         output.copy_(result)
@@ -129,13 +132,13 @@ def binary_hit_or_miss(input, structure1=None, structure2=None, output=None, ori
     else:
         structure2 = _normalize_structure(structure2, nd, "structure2")
     _validate_origin(origin2, structure2, "origin2")
-    fg = input != 0
+    fg = input if input.dtype == torch.bool else input != 0
     if bool(structure1.any()):
         hit = binary_erosion(fg, structure=structure1, origin=origin1)
     else:
         hit = torch.ones_like(fg, dtype=torch.bool)
     if bool(structure2.any()):
-        result = torch.logical_and(hit, binary_erosion(fg == 0, structure=structure2, origin=origin2))
+        result = torch.logical_and(hit, binary_erosion(torch.logical_not(fg), structure=structure2, origin=origin2))
     else:
         result = hit
     if output is not None:
