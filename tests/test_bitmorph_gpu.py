@@ -101,3 +101,26 @@ def test_ragged_vs_oracle(cuda, kind):
             for v, g in zip(imgs, out.images()):
                 exp = _oracle(kind, v[None, None], st, origin, bv)[0, 0]
                 np.testing.assert_array_equal(g.cpu().numpy(), exp)
+
+
+@pytest.mark.parametrize("kind", ["erosion", "dilation", "opening", "closing"])
+@pytest.mark.parametrize("shape", [(2, 1, 9, 48), (1, 2, 200, 1040), (3, 1, 1, 4096), (1, 1, 130, 16)])
+def test_uniform_row_walkers(cuda, kind, shape):
+    """Rows of a multiple of 16 voxels take the row-streaming walkers (structures reaching
+    at most 2 rows and 32 columns; others the tile kernel): 32-word strips, row blocks
+    of 128, both border values, equal to the oracle."""
+    x = rng(sum(shape) + len(kind)).random(shape) < 0.6
+    fn = {"erosion": tm.binary_erosion, "dilation": tm.binary_dilation, "opening": tm.binary_opening,
+          "closing": tm.binary_closing}[kind]
+    nd = len(shape) - 2
+    structs = [(CROSS, (0, 0)), (np.ones((5, 3), bool), (1, 0)), (np.ones((1, 65), bool), (0, 0)),
+               (rng(4).random((5, 5)) < 0.5, (-1, 2))]
+    if nd == 1:
+        structs = [(np.array([1, 0, 1, 1, 1], bool), (1,)), (np.ones(65, bool), (0,))]
+    for st, origin in structs:
+        if not st.any():
+            continue
+        for bv in (False, True):
+            got = fn(torch.from_numpy(x).cuda(), structure=torch.from_numpy(st), border_value=bv,
+                     origin=list(origin))
+            np.testing.assert_array_equal(got.cpu().numpy(), _oracle(kind, x, st, origin, bv))

@@ -260,6 +260,224 @@ __global__ void __launch_bounds__(kBThreads) bitmorph_kernel(const uint8_t *__re
     }
 }
 
+// ---------------------------------------------------------------- walkers
+// Uniform batches whose rows start on 16-byte boundaries (W % 16 == 0, aligned
+// buffers) and whose structures reach at most HY rows and 32 columns: every
+// warp streams down a strip of 32 words (1024 columns) of one item.  Lane l
+// holds word s0 - HW + l of each row (two 16-byte loads, 4 bool bytes -> 4
+// bits by one multiply); the words left and right of it come from the
+// neighbouring lanes by shuffles, so an operator is, per output row, one
+// funnel shift and one AND / OR per tap on registers.  The rows an operator
+// reads stay in a register window; the fused opening / closing keeps a second
+// window of the first operator's rows (border_value outside the item).  Lanes
+// HW .. 31 - HW write their word as 32 bytes (two 16-byte stores).
+constexpr int kWalkBRows = 32;   // output rows per task
+constexpr int kWalkBChunk = 4;   // input rows whose loads are in flight together
+
+struct BitRows {  // an operator's taps grouped by row offset dy = k - hy
+    int n[5];
+    int8_t dx[5][66];
+};
+
+struct BitWalk {
+    BitRows op[2];
+    int or1, or2;
+    int border;
+    int64_t batch;
+    int H, W, nw;  // nw: words per row (W / 32 rounded up)
+    int strips, rblocks;
+};
+
+// bits of words wi of row y (item rows; outside the item: border words)
+__device__ __forceinline__ uint32_t walk_load(const uint8_t *item, int y, int wi, const BitWalk &a, uint32_t bvw) {
+    if ((unsigned)y >= (unsigned)a.H || wi < 0 || wi >= a.nw) return bvw;
+    const uint8_t *p = item + (int64_t)y * a.W + 32 * wi;
+    const int valid = min(32, a.W - 32 * wi);  // a multiple of 16
+    uint4 q0 = __ldg(reinterpret_cast<const uint4 *>(p));
+    uint4 q1 = valid > 16 ? __ldg(reinterpret_cast<const uint4 *>(p + 16)) : make_uint4(0, 0, 0, 0);
+    const uint32_t v[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+    uint32_t w = 0u;
+#pragma unroll
+    for (int i = 0; i < 8; i++) w |= ((v[i] * 0x01020408u) >> 24) << (4 * i);
+    if (valid < 32) w = (w & ((1u << valid) - 1u)) | (bvw & ~((1u << valid) - 1u));
+    return w;
+}
+
+template <bool OR, int HY>
+__device__ __forceinline__ uint32_t walk_op(const uint32_t (&wl)[2 * HY + 1], const uint32_t (&wc)[2 * HY + 1],
+                                            const uint32_t (&wr)[2 * HY + 1], const BitRows &t) {
+    uint32_t acc = OR ? 0u : ~0u;
+#pragma unroll
+    for (int k = 0; k < 2 * HY + 1; k++) {
+        for (int i = 0; i < t.n[k]; i++) {
+            const int dx = t.dx[k][i];
+            const uint32_t v = dx == 0 ? wc[k]
+                               : dx > 0 ? (dx == 32 ? wr[k] : __funnelshift_r(wc[k], wr[k], dx))
+                                        : (dx == -32 ? wl[k] : __funnelshift_r(wl[k], wc[k], 32 + dx));
+            acc = OR ? (acc | v) : (acc & v);
+        }
+    }
+    return acc;
+}
+
+template <int HY1, int HY2, bool FUSED>
+__global__ void __launch_bounds__(256) bitwalk_kernel(const uint8_t *__restrict__ in, uint8_t *__restrict__ out,
+                                                      const __grid_constant__ BitWalk a) {
+    constexpr int HW = FUSED ? 2 : 1;       // halo words per side
+    constexpr int KY1 = 2 * HY1 + 1, KY2 = 2 * HY2 + 1;
+    constexpr int HYT = HY1 + (FUSED ? HY2 : 0);  // input rows read above / below an output row
+    const int lane = threadIdx.x & 31;
+    const uint32_t bvw = a.border ? ~0u : 0u;
+    const int64_t per_item = (int64_t)a.strips * a.rblocks;
+    for (int64_t task = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); task < a.batch * per_item;
+         task += (int64_t)gridDim.x * (blockDim.x / 32)) {
+        const int64_t item = task / per_item;
+        const int rem = (int)(task - item * per_item);
+        const int sx = rem % a.strips, by = rem / a.strips;
+        const int wi = sx * (32 - 2 * HW) - HW + lane;  // this lane's word
+        const int ya = by * kWalkBRows, yb = min(ya + kWalkBRows, a.H);
+        const uint8_t *src = in + item * (int64_t)a.H * a.W;
+        uint8_t *dst = out + item * (int64_t)a.H * a.W;
+        uint32_t l1[KY1], c1[KY1], r1[KY1];  // input rows of the first operator (word, left, right)
+        uint32_t l2[KY2], c2[KY2], r2[KY2];  // first operator's rows (fused)
+        // rows y - HYT .. : the first row the window needs
+        const int y_first = ya - HYT;
+        const int nrows = (yb - ya) + 2 * HYT;  // input rows streamed
+#pragma unroll
+        for (int k = 0; k < KY1; k++) l1[k] = c1[k] = r1[k] = bvw;
+#pragma unroll
+        for (int k = 0; k < KY2; k++) l2[k] = c2[k] = r2[k] = bvw;
+        for (int t0 = 0; t0 < nrows; t0 += kWalkBChunk) {
+          uint32_t wch[kWalkBChunk];
+#pragma unroll
+          for (int u = 0; u < kWalkBChunk; u++) wch[u] = walk_load(src, y_first + t0 + u, wi, a, bvw);
+#pragma unroll
+          for (int u = 0; u < kWalkBChunk; u++) {
+            const int t = t0 + u;
+            if (t >= nrows) continue;  // (not break: the loop stays fully unrolled)
+            const int yin = y_first + t;
+            const uint32_t w = wch[u];
+            // shift the input window and append the new row with its neighbours
+#pragma unroll
+            for (int k = 0; k < KY1 - 1; k++) {
+                l1[k] = l1[k + 1];
+                c1[k] = c1[k + 1];
+                r1[k] = r1[k + 1];
+            }
+            c1[KY1 - 1] = w;
+            l1[KY1 - 1] = __shfl_up_sync(~0u, w, 1);
+            r1[KY1 - 1] = __shfl_down_sync(~0u, w, 1);
+            if (t < 2 * HY1) continue;  // window not full yet
+            const int y1 = yin - HY1;   // row of the first operator's result
+            uint32_t v = a.or1 ? walk_op<true, HY1>(l1, c1, r1, a.op[0]) : walk_op<false, HY1>(l1, c1, r1, a.op[0]);
+            if (!FUSED) {
+                if (lane >= HW && lane < 32 - HW && wi < a.nw) {
+                    // 32 bytes of row y1 (only whole 16-byte groups inside the item)
+                    uint8_t *p = dst + (int64_t)y1 * a.W + 32 * wi;
+                    uint32_t b[8];
+#pragma unroll
+                    for (int i = 0; i < 8; i++) b[i] = (((v >> (4 * i)) & 15u) * 0x00204081u) & 0x01010101u;
+                    *reinterpret_cast<uint4 *>(p) = make_uint4(b[0], b[1], b[2], b[3]);
+                    if (a.W - 32 * wi > 16) *reinterpret_cast<uint4 *>(p + 16) = make_uint4(b[4], b[5], b[6], b[7]);
+                }
+                continue;
+            }
+            // fused: the intermediate image outside the item is border_value
+            if ((unsigned)y1 >= (unsigned)a.H || wi < 0 || wi >= a.nw) v = bvw;
+            else if (a.W - 32 * wi < 32) {
+                const int valid = a.W - 32 * wi;
+                v = (v & ((1u << valid) - 1u)) | (bvw & ~((1u << valid) - 1u));
+            }
+#pragma unroll
+            for (int k = 0; k < KY2 - 1; k++) {
+                l2[k] = l2[k + 1];
+                c2[k] = c2[k + 1];
+                r2[k] = r2[k + 1];
+            }
+            c2[KY2 - 1] = v;
+            l2[KY2 - 1] = __shfl_up_sync(~0u, v, 1);
+            r2[KY2 - 1] = __shfl_down_sync(~0u, v, 1);
+            if (t < 2 * HY1 + 2 * HY2) continue;
+            const int y2 = y1 - HY2;  // output row
+            const uint32_t o =
+                a.or2 ? walk_op<true, HY2>(l2, c2, r2, a.op[1]) : walk_op<false, HY2>(l2, c2, r2, a.op[1]);
+            if (lane >= HW && lane < 32 - HW && wi < a.nw) {
+                uint8_t *p = dst + (int64_t)y2 * a.W + 32 * wi;
+                uint32_t b[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) b[i] = (((o >> (4 * i)) & 15u) * 0x00204081u) & 0x01010101u;
+                *reinterpret_cast<uint4 *>(p) = make_uint4(b[0], b[1], b[2], b[3]);
+                if (a.W - 32 * wi > 16) *reinterpret_cast<uint4 *>(p + 16) = make_uint4(b[4], b[5], b[6], b[7]);
+            }
+          }
+        }
+    }
+}
+
+// Tap lists of an operator grouped by row for the walkers; false when a tap is
+// beyond the walkers' reach (2 rows, 32 columns).
+bool walk_rows(const BitTaps &t, int hy, BitRows *r) {
+    std::memset(r, 0, sizeof(BitRows));
+    if (t.hy > hy || t.hx > 32) return false;
+    for (int i = 0; i < t.n; i++) {
+        const int k = t.dy[i] + hy;
+        r->dx[k][r->n[k]++] = t.dx[i];
+    }
+    return true;
+}
+
+template <int HY1, int HY2, bool FUSED>
+int launch_walk(const uint8_t *in, uint8_t *out, const BitWalk &a, cudaStream_t s) {
+    auto kernel = bitwalk_kernel<HY1, HY2, FUSED>;
+    static thread_local int cached_dev = -1, cached_ctas = 0;
+    int dev = 0;
+    TM_CHECK_CUDA(cudaGetDevice(&dev));
+    if (cached_dev != dev) {
+        int per_sm = 0;
+        TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0));
+        cached_ctas = (per_sm < 1 ? 1 : per_sm) * sm_count();
+        cached_dev = dev;
+    }
+    const int64_t tasks = a.batch * (int64_t)a.strips * a.rblocks;
+    const int64_t blocks = std::min<int64_t>(cached_ctas, ceil_div(tasks, 8));
+    kernel<<<(unsigned)blocks, 256, 0, s>>>(in, out, a);
+    TM_LAUNCH_CHECK("bitwalk_kernel");
+    return TM_OK;
+}
+
+// The walkers for a uniform batch, when they apply; *done = false otherwise.
+int try_walk(const BitOps &ops, const uint8_t *in, uint8_t *out, int64_t batch, int64_t H, int64_t W, cudaStream_t s,
+             bool *done) {
+    *done = false;
+    if (W % 16 != 0 || (reinterpret_cast<uintptr_t>(in) & 15) || (reinterpret_cast<uintptr_t>(out) & 15)) return TM_OK;
+    const bool fused = ops.nops == 2;
+    const int hy = ops.op[0].hy;
+    if (hy > 2 || (fused && ops.op[1].hy != hy)) return TM_OK;
+    BitWalk a;
+    std::memset(&a, 0, sizeof(a));
+    if (!walk_rows(ops.op[0], hy, &a.op[0])) return TM_OK;
+    if (fused && !walk_rows(ops.op[1], hy, &a.op[1])) return TM_OK;
+    a.or1 = ops.or1;
+    a.or2 = ops.or2;
+    a.border = ops.border;
+    a.batch = batch;
+    a.H = (int)H;
+    a.W = (int)W;
+    a.nw = (int)ceil_div(W, 32);
+    const int sw = 32 - 2 * (fused ? 2 : 1);
+    a.strips = (int)ceil_div(a.nw, sw);
+    a.rblocks = (int)ceil_div(H, kWalkBRows);
+    int st;
+    if (!fused)
+        st = hy == 0 ? launch_walk<0, 0, false>(in, out, a, s)
+             : hy == 1 ? launch_walk<1, 0, false>(in, out, a, s) : launch_walk<2, 0, false>(in, out, a, s);
+    else
+        st = hy == 0 ? launch_walk<0, 0, true>(in, out, a, s)
+             : hy == 1 ? launch_walk<1, 1, true>(in, out, a, s) : launch_walk<2, 2, true>(in, out, a, s);
+    if (st == TM_OK) *done = true;
+    return st;
+}
+
 size_t bitmorph_smem(const BitOps &ops) {
     const BitGeom g = bit_geom(ops);
     size_t words = (size_t)g.srows * g.sld;
@@ -342,6 +560,8 @@ int bitmorph_uniform(int kind, const uint8_t *in, uint8_t *out, int64_t batch, i
     const int oy = ndim == 2 ? (int)origin[0] : 0, ox = (int)origin[ndim - 1];
     BitOps ops;
     if (!build_bitops(kind, structure, kh, kw, oy, ox, border, &ops)) return TM_OK;
+    int st = try_walk(ops, in, out, batch, H, W, s, done);
+    if (st != TM_OK || *done) return st;
     BitUniform u;
     u.batch = batch;
     u.H = (int)H;
@@ -351,7 +571,7 @@ int bitmorph_uniform(int kind, const uint8_t *in, uint8_t *out, int64_t batch, i
     if (tiles_item >= ((int64_t)1 << 31)) return TM_OK;
     u.tiles_item = (int)tiles_item;
     const size_t smem = bitmorph_smem(ops);
-    int grid = 0, st;
+    int grid = 0;
     if ((st = bit_grid(smem, &grid)) != TM_OK) return st;
     const int64_t blocks = std::min<int64_t>((int64_t)grid, batch * tiles_item);
     if (blocks > 0)
