@@ -427,8 +427,9 @@ def binary_lines(args, dev, stream, hbm_peak):
     for name, fn in (("binary_erosion_cross_8x4096x4096", lambda x: tm.binary_erosion(x)),
                      ("binary_opening_cross_8x4096x4096_one_pass", lambda x: tm.binary_opening(x))):
         tb = time_device(fn, xbs, steps, args.warmup, stream) / steps
-        out[name] = {"us_per_call": round(tb * 1e6, 1), "Gvoxel/s": round(nbv / tb / 1e9, 3),
-                     "frac_of_hbm": round(2.0 * nbv / tb / 1e9 / hbm_peak, 4)}
+        tg = graph_time(fn, xbs, steps, args.warmup, stream)  # device time without the host front end
+        out[name] = {"us_per_call": round(tb * 1e6, 1), "us_per_call_graph": round(tg * 1e6, 1),
+                     "Gvoxel/s": round(nbv / tg / 1e9, 3), "frac_of_hbm": round(2.0 * nbv / tg / 1e9 / hbm_peak, 4)}
     t2 = time_device(lambda x: tm.binary_dilation(tm.binary_erosion(x)), xbs, steps, args.warmup, stream) / steps
     out["binary_opening_cross_8x4096x4096_one_pass"]["composition_us"] = round(t2 * 1e6, 1)
     return out

@@ -6,12 +6,20 @@ dilation step is one libtmcore launch through ``_C``.
 
 from __future__ import annotations
 
+import functools
+
 import torch
 from torch import Tensor
 
 from .. import _C
 from .._validation import validate_bcs_input, validate_output
 from .structure import _normalize_origin, _validate_origin, generate_binary_structure
+
+
+@functools.lru_cache(maxsize=None)
+def _default_structure(nd: int) -> Tensor:
+    """The default element (cross, connectivity 1), built once per rank; read only."""
+    return generate_binary_structure(nd, 1)
 
 
 def _normalize_structure(structure: Tensor, spatial_ndim: int, name: str = "structure") -> Tensor:
@@ -32,7 +40,7 @@ def _binary_morphology(input, structure, iterations, mask, output, border_value,
     nd = validate_bcs_input(input)
     validate_output(input, output)
     if structure is None:
-        structure = generate_binary_structure(nd, 1)
+        structure = _default_structure(nd)
     structure = _normalize_structure(structure, nd)
     origin = _normalize_origin(origin, nd)
     _validate_origin(origin, structure)
@@ -157,7 +165,7 @@ def _one_pass(kind, input, structure, iterations, mask, output, border_value, or
     if nd > 2:
         return None
     if structure is None:
-        structure = generate_binary_structure(nd, 1)
+        structure = _default_structure(nd)
     structure = _normalize_structure(structure, nd)
     origin = _normalize_origin(origin, nd)
     _validate_origin(origin, structure)
