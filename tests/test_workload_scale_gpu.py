@@ -15,7 +15,9 @@ on exactly them, not on reduced shapes:
 * the shared-cost Sinkhorn: 256 pairs x 8192 points on the tensor cores at
   eps 0.05 and 0.01 to an L1 residual of 1e-6, with the relative OT cost
   (<= 1e-4) and the L1 row / column marginals (<= 1e-6) of 8 pairs checked
-  against float64 Sinkhorn.
+  against float64 Sinkhorn;
+* the HBM-resident 8 x 4096^2 lines: binary erosion and one-pass opening
+  (default cross), one-pass grey opening and white top-hat 3 x 3.
 """
 
 import numpy as np
@@ -154,3 +156,28 @@ def test_tensor_core_sinkhorn_workload_error_bounds(cuda, eps):
     assert rel <= 1e-4, rel
     assert rows <= 1e-6, rows
     assert cols <= 1e-6, cols
+
+
+def test_hbm_resident_binary_and_grey_lines(cuda):
+    """The benchmark's HBM-resident 8 x 4096^2 lines: binary erosion and the one-pass
+    binary opening with the default cross (row walkers), and the one-pass grey opening and
+    white top-hat 3 x 3 (register walkers + ring tiles), against the oracle on two items
+    and against the two-call composition on all eight."""
+    g = torch.Generator(device="cpu").manual_seed(1)
+    x = torch.rand((8, 1, 4096, 4096), generator=g)
+    xb = (x > 0.5).cuda()
+    ero = tm.binary_erosion(xb)
+    opn = tm.binary_opening(xb)
+    assert torch.equal(opn, tm.binary_dilation(_C.binary_erosion_cuda(xb, torch.from_numpy(CROSS), [0, 0], False)))
+    for i in (0, 7):
+        xi = xb[i:i + 1].cpu().numpy()
+        e = oracle.binary(xi, CROSS)
+        np.testing.assert_array_equal(ero[i:i + 1].cpu().numpy(), e)
+        np.testing.assert_array_equal(opn[i:i + 1].cpu().numpy(), oracle.binary(e, CROSS, dilation=True))
+    xg = x.cuda()
+    gop = tm.grey_opening(xg, size=3)
+    assert torch.equal(gop, tm.grey_dilation(tm.grey_erosion(xg, size=3), size=3))
+    assert torch.equal(tm.white_tophat(xg, size=3), xg - gop)
+    z = np.zeros((3, 3), np.float32)
+    xi = x[3:4].numpy()
+    np.testing.assert_array_equal(gop[3:4].cpu().numpy(), oracle.grey(oracle.grey(xi, z), z, dilation=True))

@@ -211,10 +211,11 @@ __global__ void __launch_bounds__(kOThreads) open2d_kernel(const float *__restri
 // Outputs whose whole input footprint (and the intermediate values they use)
 // lie inside the item, for compile-time KH x KW windows: each warp owns a strip
 // of 32 - (KW - 1) output columns and walks kWalkRows rows down it.  Lane l
-// holds the intermediate column x0 + lo2x + l: per input row it takes the first
-// operator's row window from L1-cached loads (the loads of the next 8 input rows
-// in flight while the current 8 are used), the column window over the last KH
-// rows in registers; the
+// holds the intermediate column x0 + lo2x + l: per input row it loads one input
+// column (lanes < KW - 1 one more, 32 to the right) and takes the first
+// operator's row window from the neighbouring lanes by shuffles (the loads of the
+// next 8 input rows in flight while the current 8 are used), the column window
+// over the last KH rows in registers; the
 // second operator's row window for output column x0 + l reads lanes l .. l + KW - 1
 // by warp shuffles, its column window is again a register window.  No border
 // mapping anywhere: the rectangle excludes every output that would need it.
@@ -241,44 +242,66 @@ __global__ void __launch_bounds__(256) open2d_walk_kernel(const float *__restric
         const int yb = min(ya + kWalkRows, p.ry1);
         const float *src = in + item * (int64_t)p.H * p.W;
         float *dst = out + item * (int64_t)p.H * p.W;
-        // Every column an output of the rectangle uses reads input columns
-        // c + lo1x .. c + lo1x + KW - 1 inside the item; columns no output uses
-        // (right of the rectangle) are clamped into that range, so every load stays
-        // inside the item and the values that matter are unchanged.
-        const int ci = min(x0 + p.lo2x + lane, p.W - KW - p.lo1x);
+        // lane l loads input column x0 + lo2x + lo1x + l of each row (lanes < KW - 1
+        // also the column 32 further right); the first operator's row window of
+        // intermediate column x0 + lo2x + l is then lanes l .. l + KW - 1 of those
+        // values, taken by shuffles.  Every input column a rectangle output uses is
+        // inside the item; the others are clamped to its last column, so every load
+        // stays inside the item and the values that matter are unchanged.
+        const int c0 = x0 + p.lo2x + p.lo1x;
+        const int ca = min(c0 + lane, p.W - 1), cb = min(c0 + 32 + lane, p.W - 1);
+        const bool halo = lane < KW - 1;
         const int i0 = ya + p.lo2y;  // first intermediate row
         float h1[KH];  // the first operator's row results of the last KH input rows
         float v2[KH];  // the second operator's row results of the last KH intermediate rows
-        auto row1 = [&](int y) {  // first operator's row window at input row y
-            const float *r = src + (int64_t)y * p.W + ci + p.lo1x;
-            float acc = __ldg(r);
+        auto row_window = [&](float a, float b) {  // all lanes together (shuffles)
+            float acc = a;
 #pragma unroll
-            for (int j = 1; j < KW; j++) acc = Op1::combine(acc, __ldg(r + j));
+            for (int j = 1; j < KW; j++) {
+                const int sl = lane + j;
+                const float va = __shfl_sync(~0u, a, sl & 31);
+                const float vb = __shfl_sync(~0u, b, sl & 31);
+                acc = Op1::combine(acc, sl < 32 ? va : vb);
+            }
             return acc;
         };
 #pragma unroll
-        for (int k = 0; k < KH - 1; k++) h1[k] = row1(i0 + p.lo1y + k);
+        for (int k = 0; k < KH - 1; k++) {
+            const float *r = src + (int64_t)(i0 + p.lo1y + k) * p.W;
+            const float a = __ldg(r + ca), b = halo ? __ldg(r + cb) : 0.0f;
+            h1[k] = row_window(a, b);
+        }
         const int nint = (yb - ya) + KH - 1;            // intermediate rows to produce
         const int ylast = i0 + p.lo1y + nint + KH - 2;  // last input row read
         // the loads of the next chunk are issued before the current chunk is used
         // (two chunks in flight); rows past the end repeat the last row
-        float nxt[kWalkChunk];
+        float na[kWalkChunk], nb[kWalkChunk];
 #pragma unroll
-        for (int u = 0; u < kWalkChunk; u++) nxt[u] = row1(min(i0 + p.lo1y + u + KH - 1, ylast));
+        for (int u = 0; u < kWalkChunk; u++) {
+            const float *r = src + (int64_t)min(i0 + p.lo1y + u + KH - 1, ylast) * p.W;
+            na[u] = __ldg(r + ca);
+            nb[u] = halo ? __ldg(r + cb) : 0.0f;
+        }
         for (int t0 = 0; t0 < nint; t0 += kWalkChunk) {
-            float ra[kWalkChunk];
+            float ra[kWalkChunk], rb[kWalkChunk];
 #pragma unroll
-            for (int u = 0; u < kWalkChunk; u++) ra[u] = nxt[u];
+            for (int u = 0; u < kWalkChunk; u++) {
+                ra[u] = na[u];
+                rb[u] = nb[u];
+            }
             if (t0 + kWalkChunk < nint) {
 #pragma unroll
-                for (int u = 0; u < kWalkChunk; u++)
-                    nxt[u] = row1(min(i0 + p.lo1y + t0 + kWalkChunk + u + KH - 1, ylast));
+                for (int u = 0; u < kWalkChunk; u++) {
+                    const float *r = src + (int64_t)min(i0 + p.lo1y + t0 + kWalkChunk + u + KH - 1, ylast) * p.W;
+                    na[u] = __ldg(r + ca);
+                    nb[u] = halo ? __ldg(r + cb) : 0.0f;
+                }
             }
 #pragma unroll
             for (int u = 0; u < kWalkChunk; u++) {
                 const int t = t0 + u;
-                if (t >= nint) break;
-                h1[KH - 1] = ra[u];
+                if (t >= nint) continue;  // uniform; (not break: the loop stays unrolled)
+                h1[KH - 1] = row_window(ra[u], rb[u]);
                 float iv = h1[0];
 #pragma unroll
                 for (int k = 1; k < KH; k++) iv = Op1::combine(iv, h1[k]);
