@@ -1,0 +1,78 @@
+"""Float4 register walkers (centred 3 x 3 and 5 x 5 flat windows on float32 items whose
+rows are a multiple of 4 voxels): grey erosion / dilation and the one-pass opening,
+closing and top-hats against the oracle, with the per-output frame kernel around them.
+Widths around the 120-column strip step and the smallest items the walkers take,
+heights at the rectangle's limit, every border mode, a structure value, infinities."""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import torchmorph_gb300 as tm
+from torchmorph_gb300 import _C
+from tests.helpers import rng
+
+pytestmark = pytest.mark.gpu
+
+MODES = {"constant": 0, "reflect": 1, "nearest": 2, "mirror": 3, "wrap": 4}
+# W = 16 (one strip), 124 / 128 / 132 (one or two strips), 252 / 256, 1000; H at 2 * lag + 1
+SHAPES = [(2, 1, 5, 16), (1, 1, 9, 20), (1, 2, 40, 124), (2, 1, 11, 128), (1, 1, 64, 132), (3, 1, 17, 252),
+          (1, 1, 130, 256), (1, 1, 37, 1000), (1, 1, 4, 64), (1, 1, 70, 18)]
+
+
+def _values(r, shape):
+    x = r.random(shape).astype(np.float32)
+    x.flat[:: 97] = np.inf
+    x.flat[5:: 89] = -np.inf
+    return x
+
+
+@pytest.mark.parametrize("dilation", [False, True])
+@pytest.mark.parametrize("k", [3, 5])
+@pytest.mark.parametrize("mode", list(MODES))
+def test_single_operator_vs_oracle(cuda, dilation, k, mode):
+    r = rng(k * 10 + int(dilation) + len(mode))
+    for shape in SHAPES:
+        x = _values(r, shape)
+        for sval in (0.0, 0.25):
+            st = np.full((k, k), sval, np.float32)
+            fn = tm.grey_dilation if dilation else tm.grey_erosion
+            got = fn(torch.from_numpy(x).cuda(), structure=torch.from_numpy(st), mode=mode, cval=0.7)
+            exp = oracle.grey(x, st, mode=mode, cval=0.7, dilation=dilation)
+            np.testing.assert_array_equal(got.cpu().numpy(), exp, err_msg=str((shape, sval)))
+
+
+@pytest.mark.parametrize("kind", ["opening", "closing", "white_tophat", "black_tophat"])
+@pytest.mark.parametrize("k", [3, 5])
+@pytest.mark.parametrize("mode", ["reflect", "constant", "wrap", "nearest"])
+def test_one_pass_vs_oracle(cuda, kind, k, mode):
+    r = rng(k * 100 + len(kind) + len(mode))
+    for shape in SHAPES:
+        x = _values(r, shape) if mode != "wrap" else r.random(shape).astype(np.float32)
+        st = np.full((k, k), 0.125, np.float32)
+        got = _C.grey_composite(kind, torch.from_numpy(x).cuda(), torch.from_numpy(st),
+                                torch.empty(0, dtype=torch.bool), [0, 0], MODES[mode], 0.3)
+        assert got is not None
+        first_max = kind in ("closing", "black_tophat")
+        a = oracle.grey(x, st, mode=mode, cval=0.3, dilation=first_max)
+        op = oracle.grey(a, st, mode=mode, cval=0.3, dilation=not first_max)
+        exp = x - op if kind == "white_tophat" else (op - x if kind == "black_tophat" else op)
+        np.testing.assert_array_equal(got.cpu().numpy(), exp, err_msg=str(shape))
+
+
+def test_walker_declines_unaligned_and_offset_items(cuda):
+    """Rows that are not a multiple of 4 voxels, a storage offset that breaks 16-byte
+    alignment, and off-centre origins take the tile kernels: same results."""
+    r = rng(3)
+    x = r.random((1, 1, 50, 203)).astype(np.float32)
+    st = np.zeros((3, 3), np.float32)
+    got = tm.grey_erosion(torch.from_numpy(x).cuda(), size=3)
+    np.testing.assert_array_equal(got.cpu().numpy(), oracle.grey(x, st))
+    big = torch.from_numpy(r.random(1 + 50 * 200).astype(np.float32)).cuda()
+    view = big[1:].view(1, 1, 50, 200)
+    got = tm.grey_dilation(view, size=3)
+    np.testing.assert_array_equal(got.cpu().numpy(), oracle.grey(view.cpu().numpy(), st, dilation=True))
+    x = r.random((1, 1, 60, 256)).astype(np.float32)
+    got = tm.grey_erosion(torch.from_numpy(x).cuda(), size=3, origin=(1, -1))
+    np.testing.assert_array_equal(got.cpu().numpy(), oracle.grey(x, st, origin=(1, -1)))

@@ -26,6 +26,7 @@
 #include "morph_tile.cuh"
 #include "tm_common.cuh"
 #include "tm_tma.cuh"
+#include "vwalk.cuh"
 
 namespace tmc {
 namespace {
@@ -464,6 +465,28 @@ int run_morphology(const T *in, T *out, int64_t batch, int ndim, const int64_t *
         {
             const int RH = kTileH + p.kh - 1, RW = stage_pitch(p.kw);
             if ((size_t)RH * RW * sizeof(T) + (size_t)RH * kRowsPitch * sizeof(T) > 200 * 1024) goto stencil;
+            if constexpr (sizeof(T) == 4) {
+                // centred 3 x 3 / 5 x 5 windows on 16-byte aligned rows: register
+                // walkers for the interior, one thread per output for the frame
+                if (ndim == 2 && p.kh == p.kw && (p.kh == 3 || p.kh == 5) && p.lo_y == -(p.kh / 2) &&
+                    p.lo_x == -(p.kw / 2)) {
+                    bool done = false;
+                    vwalk::Params wp;
+                    st = p.kh == 3 ? vwalk::launch<MAX, 1, 0, 3>(in, out, p.H, p.W, batch, p.sval, stream, &wp, &done)
+                                   : vwalk::launch<MAX, 1, 0, 5>(in, out, p.H, p.W, batch, p.sval, stream, &wp, &done);
+                    if (st != TM_OK) return st;
+                    if (done) {
+                        const int64_t frame =
+                            batch * ((int64_t)p.H * p.W - (int64_t)(wp.ry1 - wp.ry0) * (p.W - 8));
+                        const int64_t blocks =
+                            std::max<int64_t>(1, std::min<int64_t>(ceil_div(frame, 256), (int64_t)sms * 16));
+                        vwalk::frame_kernel<MAX><<<(unsigned)blocks, 256, 0, stream>>>(in, out, p, wp.ry0, wp.ry1,
+                                                                                       4, p.W - 4);
+                        TM_LAUNCH_CHECK("vwalk::frame_kernel");
+                        return TM_OK;
+                    }
+                }
+            }
             if (p.kh == 3 && p.kw == 3) return launch_flat2d<T, MAX, 3, 3>(in, out, p, batch, sms, stream);
             if (p.kh == 5 && p.kw == 5) return launch_flat2d<T, MAX, 5, 5>(in, out, p, batch, sms, stream);
             if (p.kh == 1 && p.kw == 3) return launch_flat2d<T, MAX, 1, 3>(in, out, p, batch, sms, stream);

@@ -1,0 +1,273 @@
+// Register walkers for centred 3 x 3 and 5 x 5 flat windows over float32
+// items whose rows are 16-byte aligned (GB300, sm_103a): grey erosion and
+// dilation (one stage) and the one-pass opening, closing and top-hats (two
+// stages).  They take the outputs whose whole footprint, and every
+// intermediate value those outputs use, lies inside the item: rows
+// [STAGES * h, H - STAGES * h) and columns [4, W - 4), h = K / 2.  Outputs
+// outside that rectangle (a frame a few voxels wide) go to a per-output
+// kernel that applies the border mode.
+//
+// One warp walks down a strip of 128 input columns: lane l holds columns
+// x0 + 4l .. x0 + 4l + 3 of each row as one float4 load, its horizontal
+// neighbours (h on each side) come from lanes l - 1 and l + 1 by shuffles,
+// and the vertical window is a shift register of the last K - 1 row results
+// per stage.  Lanes 1 .. 30 write their four outputs with one float4 store;
+// lanes 0 and 31 only feed their neighbours (their outer columns' windows
+// reach outside the strip), so consecutive strips start 120 columns apart
+// and re-read 8 columns of each other (L2 hits).  A task is a block of
+// output rows of one strip; its input rows are loaded kChunk rows ahead.
+//
+// Semantics are the reference's operators (torchmorph/csrc/grey_kernel.cu:
+// 101-170): erosion min(x) - s, dilation max(x) + s for a flat element of
+// value s; min / max are fminf / fmaxf, exact and order-independent.  For
+// two stages the second operator reads the first one's image, every read
+// position of which lies inside the item here.
+#pragma once
+
+#include <algorithm>
+
+#include "morph_tile.cuh"
+
+namespace tmc {
+namespace vwalk {
+
+using morph::MorphOp;
+
+constexpr int kLanesOut = 30;               // lanes 1 .. 30 write outputs
+constexpr int kStrip = 4 * kLanesOut;       // output columns per strip
+constexpr int kChunk = 4;                   // input rows in flight per warp
+constexpr int kThreads = 256;
+constexpr int kTophatNone = 0, kTophatWhite = 1, kTophatBlack = 2;
+
+struct Params {
+    int H, W;
+    int64_t batch;
+    int ry0, ry1;   // output rows taken
+    int rows;       // output rows per task
+    int nrb;        // row blocks per item
+    int nstrips;    // strips per item
+    int64_t ntasks;
+    float sval;
+};
+
+// o[i] = Op over the columns i - h .. i + h of the lane's four columns,
+// neighbours from the adjacent lanes.
+template <class Op, int h>
+__device__ __forceinline__ void row_window(const float (&v)[4], float (&o)[4]) {
+    float a[4 + 2 * h];
+#pragma unroll
+    for (int i = 0; i < 4; i++) a[h + i] = v[i];
+#pragma unroll
+    for (int j = 1; j <= h; j++) a[h - j] = __shfl_up_sync(0xffffffffu, v[4 - j], 1);
+#pragma unroll
+    for (int j = 0; j < h; j++) a[h + 4 + j] = __shfl_down_sync(0xffffffffu, v[j], 1);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        float m = a[i];
+#pragma unroll
+        for (int j = 1; j <= 2 * h; j++) m = Op::combine(m, a[i + j]);
+        o[i] = m;
+    }
+}
+
+// Vertical window: combine the K - 1 held rows with the new one, then shift.
+template <class Op, int K>
+__device__ __forceinline__ void col_window(float (&ring)[K - 1][4], const float (&hnew)[4], float (&o)[4]) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        float m = hnew[i];
+#pragma unroll
+        for (int j = 0; j < K - 1; j++) m = Op::combine(m, ring[j][i]);
+        o[i] = m;
+    }
+#pragma unroll
+    for (int j = 0; j + 1 < K - 1; j++)
+#pragma unroll
+        for (int i = 0; i < 4; i++) ring[j][i] = ring[j + 1][i];
+#pragma unroll
+    for (int i = 0; i < 4; i++) ring[K - 2][i] = hnew[i];
+}
+
+template <bool MAX1, int STAGES, int TOPHAT, int K>
+__global__ void __launch_bounds__(kThreads) vwalk_kernel(const float *__restrict__ in, float *__restrict__ out,
+                                                         Params p) {
+    using Op1 = MorphOp<float, MAX1>;
+    using Op2 = MorphOp<float, !MAX1>;
+    constexpr int h = K / 2;
+    constexpr int kLag = STAGES * h;        // output row = input row - kLag
+    constexpr int kFill = 2 * kLag;         // input rows before the first output
+    constexpr int kXHold = TOPHAT != kTophatNone ? kLag : 1;
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
+    for (int64_t t = (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); t < p.ntasks; t += nwarps) {
+        const int strip = (int)(t % p.nstrips);
+        const int64_t rest = t / p.nstrips;
+        const int rb = (int)(rest % p.nrb);
+        const int64_t item = rest / p.nrb;
+        const int c = strip * kStrip + 4 * lane;             // first column of the lane
+        const bool loads = c < p.W;                          // W is a multiple of 4
+        const bool writes = lane >= 1 && lane <= kLanesOut && c + 8 <= p.W;
+        const int ya = p.ry0 + rb * p.rows;
+        const int yb = min(ya + p.rows, p.ry1);
+        const int rs = ya - kLag, re = yb - 1 + kLag;        // input rows, inside the item
+        const float4 *src = reinterpret_cast<const float4 *>(in + item * (int64_t)p.H * p.W) + (c >> 2);
+        float4 *dst = reinterpret_cast<float4 *>(out + item * (int64_t)p.H * p.W) + (c >> 2);
+        const int wq = p.W >> 2;
+
+        float ring1[K - 1][4], ring2[K - 1][4], xh[kXHold][4];
+        float4 cur[kChunk], nxt[kChunk];
+#pragma unroll
+        for (int k = 0; k < kChunk; k++)
+            cur[k] = (loads && rs + k <= re) ? __ldg(src + (int64_t)(rs + k) * wq) : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int r0 = rs; r0 <= re; r0 += kChunk) {
+            if (r0 + kChunk <= re) {
+#pragma unroll
+                for (int k = 0; k < kChunk; k++) {
+                    const int r = r0 + kChunk + k;
+                    nxt[k] = (loads && r <= re) ? __ldg(src + (int64_t)r * wq) : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kChunk; k++) {
+                const int r = r0 + k;
+                if (r > re) continue;
+                const float v[4] = {cur[k].x, cur[k].y, cur[k].z, cur[k].w};
+                float hr[4], e[4];
+                row_window<Op1, h>(v, hr);
+                col_window<Op1, K>(ring1, hr, e);
+#pragma unroll
+                for (int i = 0; i < 4; i++) e[i] = Op1::apply(e[i], p.sval);
+                float o[4];
+                if constexpr (STAGES == 1) {
+#pragma unroll
+                    for (int i = 0; i < 4; i++) o[i] = e[i];
+                } else {
+                    float h2[4];
+                    row_window<Op2, h>(e, h2);
+                    col_window<Op2, K>(ring2, h2, o);
+#pragma unroll
+                    for (int i = 0; i < 4; i++) o[i] = Op2::apply(o[i], p.sval);
+                }
+                if constexpr (TOPHAT != kTophatNone) {
+                    // xh holds input rows r - kLag .. r - 1
+#pragma unroll
+                    for (int i = 0; i < 4; i++) o[i] = TOPHAT == kTophatWhite ? xh[0][i] - o[i] : o[i] - xh[0][i];
+#pragma unroll
+                    for (int j = 0; j + 1 < kXHold; j++)
+#pragma unroll
+                        for (int i = 0; i < 4; i++) xh[j][i] = xh[j + 1][i];
+#pragma unroll
+                    for (int i = 0; i < 4; i++) xh[kXHold - 1][i] = v[i];
+                }
+                if (r - rs >= kFill && writes)
+                    __stcs(dst + (int64_t)(r - kLag) * wq, make_float4(o[0], o[1], o[2], o[3]));
+            }
+#pragma unroll
+            for (int k = 0; k < kChunk; k++) cur[k] = nxt[k];
+        }
+    }
+}
+
+// Outputs of a one-stage flat window outside the walkers' rectangle
+// [ry0, ry1) x [rx0, rx1), one thread each, with the border mode.
+template <bool MAX>
+__global__ void __launch_bounds__(256) frame_kernel(const float *__restrict__ in, float *__restrict__ out,
+                                                    morph::Flat2DParams p, int ry0, int ry1, int rx0, int rx1) {
+    using Op = MorphOp<float, MAX>;
+    const int64_t ring = (int64_t)p.H * p.W - (int64_t)(ry1 - ry0) * (rx1 - rx0);
+    const int side = rx0 + (p.W - rx1);
+    const int64_t top = (int64_t)ry0 * p.W, mid = (int64_t)(ry1 - ry0) * side;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < p.batch * ring;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t item = idx / ring;
+        int64_t k = idx - item * ring;
+        int y, x;
+        if (k < top) {
+            y = (int)(k / p.W);
+            x = (int)(k % p.W);
+        } else if ((k -= top) < mid) {
+            y = ry0 + (int)(k / side);
+            x = (int)(k % side);
+            if (x >= rx0) x += rx1 - rx0;
+        } else {
+            k -= mid;
+            y = ry1 + (int)(k / p.W);
+            x = (int)(k % p.W);
+        }
+        const float *src = in + item * (int64_t)p.H * p.W;
+        float acc = Op::identity();
+        for (int i = 0; i < p.kh; i++) {
+            const int my = morph::map_coord(y + p.lo_y + i, p.H, p.mode);
+            for (int j = 0; j < p.kw; j++) {
+                const int mx = morph::map_coord(x + p.lo_x + j, p.W, p.mode);
+                acc = Op::combine(acc, (my < 0 || mx < 0) ? p.cval : src[(int64_t)my * p.W + mx]);
+            }
+        }
+        out[item * (int64_t)p.H * p.W + (int64_t)y * p.W + x] = Op::apply(acc, p.sval);
+    }
+}
+
+// Plans the walk: false when the item does not fit (rows not 16-byte
+// aligned, too narrow or too short for the rectangle).  resident_warps is
+// the number of walker warps the device holds at once; the row block is
+// chosen so the tasks fill whole waves of them.
+inline bool plan(int H, int W, int64_t batch, int K, int stages, const void *in, const void *out,
+                 int64_t resident_warps, Params &p) {
+    const int lag = stages * (K / 2);
+    if (W % 4 != 0 || W < 16 || H < 2 * lag + 1) return false;
+    if ((reinterpret_cast<uintptr_t>(in) & 15) || (reinterpret_cast<uintptr_t>(out) & 15)) return false;
+    p.H = H;
+    p.W = W;
+    p.batch = batch;
+    p.ry0 = lag;
+    p.ry1 = H - lag;
+    p.nstrips = (W - 8 + kStrip - 1) / kStrip;
+    const int rows = p.ry1 - p.ry0;
+    // cost of a candidate row block: waves of tasks x rows each task reads
+    double best = 0.0;
+    p.rows = 0;
+    for (int R = 8; R <= 64; R += 4) {
+        const int nrb = (rows + R - 1) / R;
+        const int64_t tasks = batch * nrb * (int64_t)p.nstrips;
+        const double waves = std::ceil((double)tasks / (double)std::max<int64_t>(resident_warps, 1));
+        const double cost = waves * (R + 2 * lag);
+        if (p.rows == 0 || cost < best) {
+            best = cost;
+            p.rows = R;
+        }
+    }
+    p.nrb = (rows + p.rows - 1) / p.rows;
+    p.ntasks = batch * p.nrb * (int64_t)p.nstrips;
+    return true;
+}
+
+// Launches the walker over the rectangle (and nothing else); false when the
+// item does not fit the walker.
+template <bool MAX1, int STAGES, int TOPHAT, int K>
+int launch(const float *in, float *out, int H, int W, int64_t batch, float sval, cudaStream_t s, Params *planned,
+           bool *done) {
+    *done = false;
+    static thread_local int cached_dev = -1, cached_per_sm = 1;
+    int dev = 0;
+    TM_CHECK_CUDA(cudaGetDevice(&dev));
+    if (cached_dev != dev) {
+        int per_sm = 0;
+        TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vwalk_kernel<MAX1, STAGES, TOPHAT, K>,
+                                                                    kThreads, 0));
+        cached_per_sm = std::max(per_sm, 1);
+        cached_dev = dev;
+    }
+    const int64_t resident_blocks = (int64_t)sm_count() * cached_per_sm;
+    Params p;
+    if (!plan(H, W, batch, K, STAGES, in, out, resident_blocks * (kThreads / 32), p)) return TM_OK;
+    p.sval = sval;
+    const int64_t blocks = std::min<int64_t>(ceil_div(p.ntasks, kThreads / 32), resident_blocks);
+    if (p.ntasks > 0) vwalk_kernel<MAX1, STAGES, TOPHAT, K><<<(unsigned)blocks, kThreads, 0, s>>>(in, out, p);
+    TM_LAUNCH_CHECK("vwalk_kernel");
+    *planned = p;
+    *done = true;
+    return TM_OK;
+}
+
+}  // namespace vwalk
+}  // namespace tmc
