@@ -76,3 +76,22 @@ def test_walker_declines_unaligned_and_offset_items(cuda):
     x = r.random((1, 1, 60, 256)).astype(np.float32)
     got = tm.grey_erosion(torch.from_numpy(x).cuda(), size=3, origin=(1, -1))
     np.testing.assert_array_equal(got.cpu().numpy(), oracle.grey(x, st, origin=(1, -1)))
+
+
+@pytest.mark.parametrize("kind", ["gradient", "laplace"])
+@pytest.mark.parametrize("k", [3, 5])
+@pytest.mark.parametrize("mode", ["reflect", "constant", "mirror"])
+def test_gradient_and_laplace_vs_oracle(cuda, kind, k, mode):
+    """Both extrema in one walk: dilation - erosion and (dilation + erosion) - 2 x,
+    rounded like the reference's elementwise ops on the two operator images."""
+    r = rng(k + len(kind) + len(mode))
+    fn = tm.morphological_gradient if kind == "gradient" else tm.morphological_laplace
+    for shape in SHAPES:
+        x = r.random(shape).astype(np.float32) * 8 - 4
+        for sval in (0.0, 0.375):
+            st = np.full((k, k), sval, np.float32)
+            got = fn(torch.from_numpy(x).cuda(), structure=torch.from_numpy(st), mode=mode, cval=0.5)
+            d = oracle.grey(x, st, mode=mode, cval=0.5, dilation=True)
+            e = oracle.grey(x, st, mode=mode, cval=0.5)
+            exp = d - e if kind == "gradient" else (d + e) - np.float32(2) * x
+            np.testing.assert_array_equal(got.cpu().numpy(), exp, err_msg=str((shape, sval)))

@@ -25,6 +25,7 @@
 
 #include "morph_tile.cuh"
 #include "tm_common.cuh"
+#include "vwalk.cuh"
 
 namespace tmc {
 namespace {
@@ -753,6 +754,48 @@ int run_composite(int op, const float *in, float *out, int64_t batch, int ndim, 
     st = build_grad_taps(false, batch, ndim, shape, structure, footprint, sshape, origin, mode, cval, &pe, &te);
     if (st != TM_OK) return st;
     if (pd.ntaps > kT2MaxTaps) return fail(TM_ERR_UNSUPPORTED, "the one-pass composites take up to %d taps", kT2MaxTaps);
+    {
+        // centred flat 3 x 3 / 5 x 5 box on 16-byte aligned rows: float4 register
+        // walkers for the interior, one thread per output for the frame
+        const int k = (int)sshape[0];
+        bool flat = sshape[1] == k && (k == 3 || k == 5) && origin[0] == 0 && origin[1] == 0 && pd.ntaps == k * k;
+        for (int t = 1; t < pd.ntaps && flat; t++) flat = std::memcmp(&td.val[t], &td.val[0], sizeof(float)) == 0;
+        if (flat) {
+            vwalk::Params wp;
+            bool done = false;
+            const int H = (int)shape[0], W = (int)shape[1];
+            const float sv = td.val[0];
+            if (op == 0)
+                st = k == 3 ? vwalk::launch<true, 1, 0, 3, vwalk::kGradient>(in, out, H, W, batch, sv, s, &wp, &done)
+                            : vwalk::launch<true, 1, 0, 5, vwalk::kGradient>(in, out, H, W, batch, sv, s, &wp, &done);
+            else
+                st = k == 3 ? vwalk::launch<true, 1, 0, 3, vwalk::kLaplace>(in, out, H, W, batch, sv, s, &wp, &done)
+                            : vwalk::launch<true, 1, 0, 5, vwalk::kLaplace>(in, out, H, W, batch, sv, s, &wp, &done);
+            if (st != TM_OK) return st;
+            if (done) {
+                morph::Flat2DParams fp;
+                fp.H = H;
+                fp.W = W;
+                fp.kh = fp.kw = k;
+                fp.lo_y = fp.lo_x = -(k / 2);
+                fp.mode = mode;
+                fp.batch = batch;
+                fp.cval = cval;
+                fp.sval = sv;
+                const int64_t frame = batch * ((int64_t)H * W - (int64_t)(wp.ry1 - wp.ry0) * (W - 8));
+                const unsigned blocks =
+                    (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(frame, 256), (int64_t)sm_count() * 16));
+                if (op == 0)
+                    vwalk::frame_kernel<true, vwalk::kGradient><<<blocks, 256, 0, s>>>(in, out, fp, wp.ry0, wp.ry1, 4,
+                                                                                      W - 4);
+                else
+                    vwalk::frame_kernel<true, vwalk::kLaplace><<<blocks, 256, 0, s>>>(in, out, fp, wp.ry0, wp.ry1, 4,
+                                                                                     W - 4);
+                TM_LAUNCH_CHECK("vwalk::frame_kernel");
+                return TM_OK;
+            }
+        }
+    }
     int mny = 0, mxy = 0, mnx = 0, mxx = 0;  // union of both tap regions (and the voxel itself)
     for (int t = 0; t < pd.ntaps; t++)
         for (const GradTaps *tt : {&td, &te}) {

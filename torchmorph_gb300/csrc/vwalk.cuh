@@ -38,6 +38,7 @@ constexpr int kStrip = 4 * kLanesOut;       // output columns per strip
 constexpr int kChunk = 4;                   // input rows in flight per warp
 constexpr int kThreads = 256;
 constexpr int kTophatNone = 0, kTophatWhite = 1, kTophatBlack = 2;
+constexpr int kGradient = 1, kLaplace = 2;
 
 struct Params {
     int H, W;
@@ -70,6 +71,29 @@ __device__ __forceinline__ void row_window(const float (&v)[4], float (&o)[4]) {
     }
 }
 
+// Both extrema over the columns i - h .. i + h (one set of shuffles).
+template <int h>
+__device__ __forceinline__ void row_window_both(const float (&v)[4], float (&mx)[4], float (&mn)[4]) {
+    float a[4 + 2 * h];
+#pragma unroll
+    for (int i = 0; i < 4; i++) a[h + i] = v[i];
+#pragma unroll
+    for (int j = 1; j <= h; j++) a[h - j] = __shfl_up_sync(0xffffffffu, v[4 - j], 1);
+#pragma unroll
+    for (int j = 0; j < h; j++) a[h + 4 + j] = __shfl_down_sync(0xffffffffu, v[j], 1);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        float hi = a[i], lo = a[i];
+#pragma unroll
+        for (int j = 1; j <= 2 * h; j++) {
+            hi = fmaxf(hi, a[i + j]);
+            lo = fminf(lo, a[i + j]);
+        }
+        mx[i] = hi;
+        mn[i] = lo;
+    }
+}
+
 // Vertical window: combine the K - 1 held rows with the new one, then shift.
 template <class Op, int K>
 __device__ __forceinline__ void col_window(float (&ring)[K - 1][4], const float (&hnew)[4], float (&o)[4]) {
@@ -88,7 +112,9 @@ __device__ __forceinline__ void col_window(float (&ring)[K - 1][4], const float 
     for (int i = 0; i < 4; i++) ring[K - 2][i] = hnew[i];
 }
 
-template <bool MAX1, int STAGES, int TOPHAT, int K>
+// COMBINE: 0 the operators alone; kGradient dilation - erosion, kLaplace
+// (dilation + erosion) - 2 x, both of one stage over the same window.
+template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE = 0>
 __global__ void __launch_bounds__(kThreads) vwalk_kernel(const float *__restrict__ in, float *__restrict__ out,
                                                          Params p) {
     using Op1 = MorphOp<float, MAX1>;
@@ -96,7 +122,8 @@ __global__ void __launch_bounds__(kThreads) vwalk_kernel(const float *__restrict
     constexpr int h = K / 2;
     constexpr int kLag = STAGES * h;        // output row = input row - kLag
     constexpr int kFill = 2 * kLag;         // input rows before the first output
-    constexpr int kXHold = TOPHAT != kTophatNone ? kLag : 1;
+    constexpr bool kHoldX = TOPHAT != kTophatNone || COMBINE == kLaplace;
+    constexpr int kXHold = kHoldX ? kLag : 1;
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
     for (int64_t t = (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); t < p.ntasks; t += nwarps) {
@@ -132,26 +159,43 @@ __global__ void __launch_bounds__(kThreads) vwalk_kernel(const float *__restrict
                 const int r = r0 + k;
                 if (r > re) continue;
                 const float v[4] = {cur[k].x, cur[k].y, cur[k].z, cur[k].w};
-                float hr[4], e[4];
-                row_window<Op1, h>(v, hr);
-                col_window<Op1, K>(ring1, hr, e);
+                float hr[4], e[4], o[4];
+                if constexpr (COMBINE != 0) {
+                    // ring1 holds the maxima, ring2 the minima; rounded like the
+                    // reference's elementwise ops on the two operator images
+                    float hl[4], d[4];
+                    row_window_both<h>(v, hr, hl);
+                    col_window<MorphOp<float, true>, K>(ring1, hr, d);
+                    col_window<MorphOp<float, false>, K>(ring2, hl, e);
 #pragma unroll
-                for (int i = 0; i < 4; i++) e[i] = Op1::apply(e[i], p.sval);
-                float o[4];
-                if constexpr (STAGES == 1) {
-#pragma unroll
-                    for (int i = 0; i < 4; i++) o[i] = e[i];
+                    for (int i = 0; i < 4; i++) {
+                        const float dv = __fadd_rn(d[i], p.sval), ev = __fsub_rn(e[i], p.sval);
+                        o[i] = COMBINE == kGradient ? __fsub_rn(dv, ev)
+                                                    : __fsub_rn(__fadd_rn(dv, ev), __fmul_rn(2.f, xh[0][i]));
+                    }
                 } else {
-                    float h2[4];
-                    row_window<Op2, h>(e, h2);
-                    col_window<Op2, K>(ring2, h2, o);
+                    row_window<Op1, h>(v, hr);
+                    col_window<Op1, K>(ring1, hr, e);
 #pragma unroll
-                    for (int i = 0; i < 4; i++) o[i] = Op2::apply(o[i], p.sval);
+                    for (int i = 0; i < 4; i++) e[i] = Op1::apply(e[i], p.sval);
+                    if constexpr (STAGES == 1) {
+#pragma unroll
+                        for (int i = 0; i < 4; i++) o[i] = e[i];
+                    } else {
+                        float h2[4];
+                        row_window<Op2, h>(e, h2);
+                        col_window<Op2, K>(ring2, h2, o);
+#pragma unroll
+                        for (int i = 0; i < 4; i++) o[i] = Op2::apply(o[i], p.sval);
+                    }
                 }
-                if constexpr (TOPHAT != kTophatNone) {
+                if constexpr (kHoldX) {
                     // xh holds input rows r - kLag .. r - 1
+                    if constexpr (TOPHAT != kTophatNone) {
 #pragma unroll
-                    for (int i = 0; i < 4; i++) o[i] = TOPHAT == kTophatWhite ? xh[0][i] - o[i] : o[i] - xh[0][i];
+                        for (int i = 0; i < 4; i++)
+                            o[i] = TOPHAT == kTophatWhite ? xh[0][i] - o[i] : o[i] - xh[0][i];
+                    }
 #pragma unroll
                     for (int j = 0; j + 1 < kXHold; j++)
 #pragma unroll
@@ -169,8 +213,9 @@ __global__ void __launch_bounds__(kThreads) vwalk_kernel(const float *__restrict
 }
 
 // Outputs of a one-stage flat window outside the walkers' rectangle
-// [ry0, ry1) x [rx0, rx1), one thread each, with the border mode.
-template <bool MAX>
+// [ry0, ry1) x [rx0, rx1), one thread each, with the border mode (COMBINE as
+// in the walker: both extrema, combined like the reference's elementwise ops).
+template <bool MAX, int COMBINE = 0>
 __global__ void __launch_bounds__(256) frame_kernel(const float *__restrict__ in, float *__restrict__ out,
                                                     morph::Flat2DParams p, int ry0, int ry1, int rx0, int rx1) {
     using Op = MorphOp<float, MAX>;
@@ -195,15 +240,24 @@ __global__ void __launch_bounds__(256) frame_kernel(const float *__restrict__ in
             x = (int)(k % p.W);
         }
         const float *src = in + item * (int64_t)p.H * p.W;
-        float acc = Op::identity();
+        float acc = Op::identity(), lo = INFINITY;
         for (int i = 0; i < p.kh; i++) {
             const int my = morph::map_coord(y + p.lo_y + i, p.H, p.mode);
             for (int j = 0; j < p.kw; j++) {
                 const int mx = morph::map_coord(x + p.lo_x + j, p.W, p.mode);
-                acc = Op::combine(acc, (my < 0 || mx < 0) ? p.cval : src[(int64_t)my * p.W + mx]);
+                const float v = (my < 0 || mx < 0) ? p.cval : src[(int64_t)my * p.W + mx];
+                acc = Op::combine(acc, v);
+                if (COMBINE != 0) lo = fminf(lo, v);
             }
         }
-        out[item * (int64_t)p.H * p.W + (int64_t)y * p.W + x] = Op::apply(acc, p.sval);
+        float o = Op::apply(acc, p.sval);
+        if (COMBINE != 0) {
+            const float ev = __fsub_rn(lo, p.sval);
+            o = COMBINE == kGradient
+                    ? __fsub_rn(o, ev)
+                    : __fsub_rn(__fadd_rn(o, ev), __fmul_rn(2.f, src[(int64_t)y * p.W + x]));
+        }
+        out[item * (int64_t)p.H * p.W + (int64_t)y * p.W + x] = o;
     }
 }
 
@@ -243,7 +297,7 @@ inline bool plan(int H, int W, int64_t batch, int K, int stages, const void *in,
 
 // Launches the walker over the rectangle (and nothing else); false when the
 // item does not fit the walker.
-template <bool MAX1, int STAGES, int TOPHAT, int K>
+template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE = 0>
 int launch(const float *in, float *out, int H, int W, int64_t batch, float sval, cudaStream_t s, Params *planned,
            bool *done) {
     *done = false;
@@ -252,7 +306,7 @@ int launch(const float *in, float *out, int H, int W, int64_t batch, float sval,
     TM_CHECK_CUDA(cudaGetDevice(&dev));
     if (cached_dev != dev) {
         int per_sm = 0;
-        TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vwalk_kernel<MAX1, STAGES, TOPHAT, K>,
+        TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vwalk_kernel<MAX1, STAGES, TOPHAT, K, COMBINE>,
                                                                     kThreads, 0));
         cached_per_sm = std::max(per_sm, 1);
         cached_dev = dev;
@@ -262,7 +316,8 @@ int launch(const float *in, float *out, int H, int W, int64_t batch, float sval,
     if (!plan(H, W, batch, K, STAGES, in, out, resident_blocks * (kThreads / 32), p)) return TM_OK;
     p.sval = sval;
     const int64_t blocks = std::min<int64_t>(ceil_div(p.ntasks, kThreads / 32), resident_blocks);
-    if (p.ntasks > 0) vwalk_kernel<MAX1, STAGES, TOPHAT, K><<<(unsigned)blocks, kThreads, 0, s>>>(in, out, p);
+    if (p.ntasks > 0)
+        vwalk_kernel<MAX1, STAGES, TOPHAT, K, COMBINE><<<(unsigned)blocks, kThreads, 0, s>>>(in, out, p);
     TM_LAUNCH_CHECK("vwalk_kernel");
     *planned = p;
     *done = true;
