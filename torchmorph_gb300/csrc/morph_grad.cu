@@ -773,26 +773,24 @@ int run_composite(int op, const float *in, float *out, int64_t batch, int ndim, 
                             : vwalk::launch<true, 1, 0, 5, vwalk::kLaplace>(in, out, H, W, batch, sv, s, &wp, &done);
             if (st != TM_OK) return st;
             if (done) {
-                morph::Flat2DParams fp;
-                fp.H = H;
-                fp.W = W;
-                fp.kh = fp.kw = k;
-                fp.lo_y = fp.lo_x = -(k / 2);
-                fp.mode = mode;
-                fp.batch = batch;
-                fp.cval = cval;
-                fp.sval = sv;
-                const int64_t frame = batch * ((int64_t)H * W - (int64_t)(wp.ry1 - wp.ry0) * (W - 8));
-                const unsigned blocks =
-                    (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(frame, 256), (int64_t)sm_count() * 16));
+                vwalk::FrameParams f;
+                f.H = H;
+                f.W = W;
+                f.batch = batch;
+                f.lo1y = f.lo1x = -(k / 2);
+                f.lo2y = f.lo2x = 0;
+                f.mode = mode;
+                f.cval = cval;
+                f.sval = sv;
+                f.ry0 = wp.ry0;
+                f.ry1 = wp.ry1;
+                f.rx0 = 4;
+                f.rx1 = W - 4;
                 if (op == 0)
-                    vwalk::frame_kernel<true, vwalk::kGradient><<<blocks, 256, 0, s>>>(in, out, fp, wp.ry0, wp.ry1, 4,
-                                                                                      W - 4);
-                else
-                    vwalk::frame_kernel<true, vwalk::kLaplace><<<blocks, 256, 0, s>>>(in, out, fp, wp.ry0, wp.ry1, 4,
-                                                                                     W - 4);
-                TM_LAUNCH_CHECK("vwalk::frame_kernel");
-                return TM_OK;
+                    return k == 3 ? vwalk::launch_frame<true, 1, 0, 3, vwalk::kGradient>(in, out, f, s)
+                                  : vwalk::launch_frame<true, 1, 0, 5, vwalk::kGradient>(in, out, f, s);
+                return k == 3 ? vwalk::launch_frame<true, 1, 0, 3, vwalk::kLaplace>(in, out, f, s)
+                              : vwalk::launch_frame<true, 1, 0, 5, vwalk::kLaplace>(in, out, f, s);
             }
         }
     }

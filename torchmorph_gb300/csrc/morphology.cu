@@ -476,14 +476,22 @@ int run_morphology(const T *in, T *out, int64_t batch, int ndim, const int64_t *
                                    : vwalk::launch<MAX, 1, 0, 5>(in, out, p.H, p.W, batch, p.sval, stream, &wp, &done);
                     if (st != TM_OK) return st;
                     if (done) {
-                        const int64_t frame =
-                            batch * ((int64_t)p.H * p.W - (int64_t)(wp.ry1 - wp.ry0) * (p.W - 8));
-                        const int64_t blocks =
-                            std::max<int64_t>(1, std::min<int64_t>(ceil_div(frame, 256), (int64_t)sms * 16));
-                        vwalk::frame_kernel<MAX><<<(unsigned)blocks, 256, 0, stream>>>(in, out, p, wp.ry0, wp.ry1,
-                                                                                       4, p.W - 4);
-                        TM_LAUNCH_CHECK("vwalk::frame_kernel");
-                        return TM_OK;
+                        vwalk::FrameParams f;
+                        f.H = p.H;
+                        f.W = p.W;
+                        f.batch = batch;
+                        f.lo1y = p.lo_y;
+                        f.lo1x = p.lo_x;
+                        f.lo2y = f.lo2x = 0;
+                        f.mode = p.mode;
+                        f.cval = p.cval;
+                        f.sval = p.sval;
+                        f.ry0 = wp.ry0;
+                        f.ry1 = wp.ry1;
+                        f.rx0 = 4;
+                        f.rx1 = p.W - 4;
+                        return p.kh == 3 ? vwalk::launch_frame<MAX, 1, 0, 3>(in, out, f, stream)
+                                         : vwalk::launch_frame<MAX, 1, 0, 5>(in, out, f, stream);
                     }
                 }
             }

@@ -334,58 +334,6 @@ __global__ void __launch_bounds__(256) open2d_walk_kernel(const float *__restric
     }
 }
 
-// Outputs outside the walkers' rectangle, one thread each, straight from the
-// definition: the second operator over the intermediate image's window, each
-// intermediate value the first operator's window of the input (first_at, with
-// the input's border mapping); intermediate positions outside the item take
-// cval or the value at the mapped position.  Used when those outputs are a
-// small part of the item (a thin frame along its border).
-template <bool MAX1, int TOPHAT>
-__global__ void __launch_bounds__(256) open2d_ring_kernel(const float *__restrict__ in, float *__restrict__ out,
-                                                          Open2DParams p) {
-    using Op2 = MorphOp<float, !MAX1>;
-    const int64_t inner = (int64_t)(p.ry1 - p.ry0) * (p.rx1 - p.rx0);
-    const int64_t ring = (int64_t)p.H * p.W - inner;
-    const int side = p.rx0 + (p.W - p.rx1);
-    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < p.batch * ring;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t item = idx / ring;
-        int64_t k = idx - item * ring;
-        int y, x;
-        const int64_t top = (int64_t)p.ry0 * p.W, mid = (int64_t)(p.ry1 - p.ry0) * side;
-        if (k < top) {
-            y = (int)(k / p.W);
-            x = (int)(k % p.W);
-        } else if ((k -= top) < mid) {
-            y = p.ry0 + (int)(k / side);
-            x = (int)(k % side);
-            if (x >= p.rx0) x += p.rx1 - p.rx0;
-        } else {
-            k -= mid;
-            y = p.ry1 + (int)(k / p.W);
-            x = (int)(k % p.W);
-        }
-        const float *src = in + item * (int64_t)p.H * p.W;
-        float acc = Op2::identity();
-        for (int i = 0; i < p.kh; i++) {
-            const int iy = y + p.lo2y + i;
-            const int my = (unsigned)iy < (unsigned)p.H ? iy : map_coord(iy, p.H, p.mode);
-            for (int j = 0; j < p.kw; j++) {
-                const int ix = x + p.lo2x + j;
-                const int mx = (unsigned)ix < (unsigned)p.W ? ix : map_coord(ix, p.W, p.mode);
-                const float v = (my < 0 || mx < 0) ? p.cval : first_at<MAX1>(src, p, my, mx);
-                acc = Op2::combine(acc, v);
-            }
-        }
-        float o = Op2::apply(acc, p.sval);
-        if (TOPHAT != kTophatNone) {
-            const float xv = src[(int64_t)y * p.W + x];
-            o = TOPHAT == kTophatWhite ? xv - o : o - xv;
-        }
-        out[item * (int64_t)p.H * p.W + (int64_t)y * p.W + x] = o;
-    }
-}
-
 // The rectangle of outputs the walkers can take (see open2d_walk_kernel).
 void walk_rect(Open2DParams &p) {
     // output y reads intermediate rows y + lo2y .. y + lo2y + kh - 1 (all inside the item)
@@ -482,11 +430,23 @@ int run_open2d(const float *in, float *out, int64_t batch, int ndim, const int64
     if (p.ry1 > p.ry0) {
         const int64_t frame = (int64_t)p.H * p.W - (int64_t)(p.ry1 - p.ry0) * (p.rx1 - p.rx0);
         if (frame * 16 <= (int64_t)p.H * p.W) {
-            const int64_t total = batch * frame;
-            const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(total, 256), (int64_t)sm_count() * 16));
-            if (total > 0) open2d_ring_kernel<MAX1, TOPHAT><<<(unsigned)blocks, 256, 0, s>>>(in, out, p);
-            TM_LAUNCH_CHECK("open2d_ring_kernel");
-            return TM_OK;
+            vwalk::FrameParams f;
+            f.H = p.H;
+            f.W = p.W;
+            f.batch = batch;
+            f.lo1y = p.lo1y;
+            f.lo1x = p.lo1x;
+            f.lo2y = p.lo2y;
+            f.lo2x = p.lo2x;
+            f.mode = p.mode;
+            f.cval = p.cval;
+            f.sval = p.sval;
+            f.ry0 = p.ry0;
+            f.ry1 = p.ry1;
+            f.rx0 = p.rx0;
+            f.rx1 = p.rx1;
+            return p.kh == 3 ? vwalk::launch_frame<MAX1, 2, TOPHAT, 3>(in, out, f, s)
+                             : vwalk::launch_frame<MAX1, 2, TOPHAT, 5>(in, out, f, s);
         }
     }
     // tiles entirely inside the walkers' rectangle are skipped by the tile kernel

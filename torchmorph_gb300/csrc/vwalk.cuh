@@ -212,53 +212,193 @@ __global__ void __launch_bounds__(kThreads) vwalk_kernel(const float *__restrict
     }
 }
 
-// Outputs of a one-stage flat window outside the walkers' rectangle
-// [ry0, ry1) x [rx0, rx1), one thread each, with the border mode (COMBINE as
-// in the walker: both extrema, combined like the reference's elementwise ops).
-template <bool MAX, int COMBINE = 0>
-__global__ void __launch_bounds__(256) frame_kernel(const float *__restrict__ in, float *__restrict__ out,
-                                                    morph::Flat2DParams p, int ry0, int ry1, int rx0, int rx1) {
-    using Op = MorphOp<float, MAX>;
-    const int64_t ring = (int64_t)p.H * p.W - (int64_t)(ry1 - ry0) * (rx1 - rx0);
-    const int side = rx0 + (p.W - rx1);
-    const int64_t top = (int64_t)ry0 * p.W, mid = (int64_t)(ry1 - ry0) * side;
-    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < p.batch * ring;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t item = idx / ring;
-        int64_t k = idx - item * ring;
-        int y, x;
-        if (k < top) {
-            y = (int)(k / p.W);
-            x = (int)(k % p.W);
-        } else if ((k -= top) < mid) {
-            y = ry0 + (int)(k / side);
-            x = (int)(k % side);
-            if (x >= rx0) x += rx1 - rx0;
-        } else {
-            k -= mid;
-            y = ry1 + (int)(k / p.W);
-            x = (int)(k % p.W);
+// Outputs outside the walkers' rectangle [ry0, ry1) x [rx0, rx1) (a frame a
+// few voxels wide), one thread each, straight from the definition with the
+// border mode at both levels: the first operator over the input (rows
+// y + lo1y .., columns x + lo1x ..), and for two stages the second operator
+// over the intermediate image (rows y + lo2y .., positions outside the item
+// taking cval or the intermediate value at the mapped position).  Window
+// sizes are compile-time, so a window's loads are independent; where the
+// rows (side bands) or the columns (top and bottom bands) of the whole
+// footprint lie inside the item, the first operator runs separably over the
+// 2K - 1 footprint rows (columns) shared by the intermediate positions.
+struct FrameParams {
+    int H, W;
+    int64_t batch;
+    int lo1y, lo1x, lo2y, lo2x;
+    int mode;
+    float cval, sval;
+    int ry0, ry1, rx0, rx1;
+};
+
+__device__ __forceinline__ float frame_ld(const float *src, const FrameParams &f, int r, int c) {
+    return (r < 0 || c < 0) ? f.cval : __ldg(src + (int64_t)r * f.W + c);
+}
+
+template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE>
+__device__ __forceinline__ float frame_value(const float *src, const FrameParams &f, int y, int x) {
+    using Op1 = MorphOp<float, MAX1>;
+    using Op2 = MorphOp<float, !MAX1>;
+    using morph::map_coord;
+    if constexpr (STAGES == 1) {
+        int R[K], C[K];
+#pragma unroll
+        for (int a = 0; a < K; a++) {
+            R[a] = map_coord(y + f.lo1y + a, f.H, f.mode);
+            C[a] = map_coord(x + f.lo1x + a, f.W, f.mode);
         }
-        const float *src = in + item * (int64_t)p.H * p.W;
-        float acc = Op::identity(), lo = INFINITY;
-        for (int i = 0; i < p.kh; i++) {
-            const int my = morph::map_coord(y + p.lo_y + i, p.H, p.mode);
-            for (int j = 0; j < p.kw; j++) {
-                const int mx = morph::map_coord(x + p.lo_x + j, p.W, p.mode);
-                const float v = (my < 0 || mx < 0) ? p.cval : src[(int64_t)my * p.W + mx];
-                acc = Op::combine(acc, v);
+        float acc = Op1::identity(), lo = INFINITY;
+#pragma unroll
+        for (int a = 0; a < K; a++)
+#pragma unroll
+            for (int b = 0; b < K; b++) {
+                const float v = frame_ld(src, f, R[a], C[b]);
+                acc = Op1::combine(acc, v);
                 if (COMBINE != 0) lo = fminf(lo, v);
             }
-        }
-        float o = Op::apply(acc, p.sval);
+        float o = Op1::apply(acc, f.sval);
         if (COMBINE != 0) {
-            const float ev = __fsub_rn(lo, p.sval);
-            o = COMBINE == kGradient
-                    ? __fsub_rn(o, ev)
-                    : __fsub_rn(__fadd_rn(o, ev), __fmul_rn(2.f, src[(int64_t)y * p.W + x]));
+            const float ev = __fsub_rn(lo, f.sval);
+            o = COMBINE == kGradient ? __fsub_rn(o, ev)
+                                     : __fsub_rn(__fadd_rn(o, ev), __fmul_rn(2.f, src[(int64_t)y * f.W + x]));
         }
-        out[item * (int64_t)p.H * p.W + (int64_t)y * p.W + x] = o;
+        return o;
+    } else {
+        float acc2 = Op2::identity();
+        const int by = y + f.lo2y + f.lo1y, bx = x + f.lo2x + f.lo1x;  // first footprint row / column
+        if (by >= 0 && by + 2 * K - 2 < f.H) {
+            // every row at both levels inside the item: per footprint row, the
+            // first operator along each intermediate column's mapped window
+            int C2[K], CC[K][K];
+#pragma unroll
+            for (int j = 0; j < K; j++) {
+                C2[j] = map_coord(x + f.lo2x + j, f.W, f.mode);
+#pragma unroll
+                for (int b = 0; b < K; b++) CC[j][b] = C2[j] < 0 ? 0 : map_coord(C2[j] + f.lo1x + b, f.W, f.mode);
+            }
+            float rm[2 * K - 1][K];
+#pragma unroll
+            for (int r = 0; r < 2 * K - 1; r++)
+#pragma unroll
+                for (int j = 0; j < K; j++) {
+                    float m = Op1::identity();
+#pragma unroll
+                    for (int b = 0; b < K; b++) m = Op1::combine(m, frame_ld(src, f, by + r, CC[j][b]));
+                    rm[r][j] = m;
+                }
+#pragma unroll
+            for (int i = 0; i < K; i++)
+#pragma unroll
+                for (int j = 0; j < K; j++) {
+                    float m = rm[i][j];
+#pragma unroll
+                    for (int a = 1; a < K; a++) m = Op1::combine(m, rm[i + a][j]);
+                    acc2 = Op2::combine(acc2, C2[j] < 0 ? f.cval : Op1::apply(m, f.sval));
+                }
+        } else if (bx >= 0 && bx + 2 * K - 2 < f.W) {
+            // every column inside the item: the same with rows and columns swapped
+            int R2[K], RR[K][K];
+#pragma unroll
+            for (int i = 0; i < K; i++) {
+                R2[i] = map_coord(y + f.lo2y + i, f.H, f.mode);
+#pragma unroll
+                for (int a = 0; a < K; a++) RR[i][a] = R2[i] < 0 ? 0 : map_coord(R2[i] + f.lo1y + a, f.H, f.mode);
+            }
+            float cm[2 * K - 1][K];
+#pragma unroll
+            for (int c = 0; c < 2 * K - 1; c++)
+#pragma unroll
+                for (int i = 0; i < K; i++) {
+                    float m = Op1::identity();
+#pragma unroll
+                    for (int a = 0; a < K; a++) m = Op1::combine(m, frame_ld(src, f, RR[i][a], bx + c));
+                    cm[c][i] = m;
+                }
+#pragma unroll
+            for (int i = 0; i < K; i++)
+#pragma unroll
+                for (int j = 0; j < K; j++) {
+                    float m = cm[j][i];
+#pragma unroll
+                    for (int b = 1; b < K; b++) m = Op1::combine(m, cm[j + b][i]);
+                    acc2 = Op2::combine(acc2, R2[i] < 0 ? f.cval : Op1::apply(m, f.sval));
+                }
+        } else {
+            // corners: both axes mapped
+#pragma unroll 1
+            for (int i = 0; i < K; i++) {
+                const int my = map_coord(y + f.lo2y + i, f.H, f.mode);
+                int RR[K];
+#pragma unroll
+                for (int a = 0; a < K; a++) RR[a] = my < 0 ? 0 : map_coord(my + f.lo1y + a, f.H, f.mode);
+#pragma unroll 1
+                for (int j = 0; j < K; j++) {
+                    const int mx = map_coord(x + f.lo2x + j, f.W, f.mode);
+                    float e = f.cval;
+                    if (my >= 0 && mx >= 0) {
+                        float m = Op1::identity();
+#pragma unroll
+                        for (int b = 0; b < K; b++) {
+                            const int cc = map_coord(mx + f.lo1x + b, f.W, f.mode);
+#pragma unroll
+                            for (int a = 0; a < K; a++) m = Op1::combine(m, frame_ld(src, f, RR[a], cc));
+                        }
+                        e = Op1::apply(m, f.sval);
+                    }
+                    acc2 = Op2::combine(acc2, e);
+                }
+            }
+        }
+        float o = Op2::apply(acc2, f.sval);
+        if (TOPHAT != kTophatNone) {
+            const float xv = src[(int64_t)y * f.W + x];
+            o = TOPHAT == kTophatWhite ? xv - o : o - xv;
+        }
+        return o;
     }
+}
+
+template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE>
+__global__ void __launch_bounds__(256) frame_kernel(const float *__restrict__ in, float *__restrict__ out,
+                                                    FrameParams f) {
+    const int ring = f.H * f.W - (f.ry1 - f.ry0) * (f.rx1 - f.rx0);
+    const int side = f.rx0 + (f.W - f.rx1);
+    const int top = f.ry0 * f.W, mid = (f.ry1 - f.ry0) * side;
+    for (int64_t item = blockIdx.y; item < f.batch; item += gridDim.y) {
+        const float *src = in + item * (int64_t)f.H * f.W;
+        float *dst = out + item * (int64_t)f.H * f.W;
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ring; k += gridDim.x * blockDim.x) {
+            int y, x, q = k;
+            if (q < top) {
+                y = q / f.W;
+                x = q - y * f.W;
+            } else if ((q -= top) < mid) {
+                const int r = q / side;
+                y = f.ry0 + r;
+                x = q - r * side;
+                if (x >= f.rx0) x += f.rx1 - f.rx0;
+            } else {
+                q -= mid;
+                const int r = q / f.W;
+                y = f.ry1 + r;
+                x = q - r * f.W;
+            }
+            dst[(int64_t)y * f.W + x] = frame_value<MAX1, STAGES, TOPHAT, K, COMBINE>(src, f, y, x);
+        }
+    }
+}
+
+// Launches the frame kernel for the outputs outside the rectangle.
+template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE = 0>
+int launch_frame(const float *in, float *out, const FrameParams &f, cudaStream_t s) {
+    const int64_t ring = (int64_t)f.H * f.W - (int64_t)(f.ry1 - f.ry0) * (f.rx1 - f.rx0);
+    if (ring <= 0 || f.batch <= 0) return TM_OK;
+    const unsigned gy = (unsigned)std::min<int64_t>(f.batch, 65535);
+    const int64_t want = std::max<int64_t>(1, (int64_t)sm_count() * 16 / gy);
+    const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(ring, 256), want));
+    frame_kernel<MAX1, STAGES, TOPHAT, K, COMBINE><<<dim3(gx, gy), 256, 0, s>>>(in, out, f);
+    TM_LAUNCH_CHECK("vwalk::frame_kernel");
+    return TM_OK;
 }
 
 // Plans the walk: false when the item does not fit (rows not 16-byte
