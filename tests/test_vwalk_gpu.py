@@ -1,8 +1,10 @@
 """Float4 register walkers (centred 3 x 3 and 5 x 5 flat windows on float32 items whose
-rows are a multiple of 4 voxels): grey erosion / dilation and the one-pass opening,
-closing and top-hats against the oracle, with the per-output frame kernel around them.
-Widths around the 120-column strip step and the smallest items the walkers take,
-heights at the rectangle's limit, every border mode, a structure value, infinities."""
+rows are a multiple of 4 voxels): grey erosion / dilation, gradient, laplace and the
+one-pass opening, closing and top-hats against the oracle, with the edge lanes' border
+mapping and the frame kernel for the outputs the walkers leave.  Widths around the
+120-column strip step, heights from one row (mapped rows) to the two-stage limit, every
+border mode (wrap leaves the side columns to the frame kernel), a structure value,
+infinities."""
 
 import numpy as np
 import pytest
@@ -18,7 +20,8 @@ pytestmark = pytest.mark.gpu
 MODES = {"constant": 0, "reflect": 1, "nearest": 2, "mirror": 3, "wrap": 4}
 # W = 16 (one strip), 124 / 128 / 132 (one or two strips), 252 / 256, 1000; H at 2 * lag + 1
 SHAPES = [(2, 1, 5, 16), (1, 1, 9, 20), (1, 2, 40, 124), (2, 1, 11, 128), (1, 1, 64, 132), (3, 1, 17, 252),
-          (1, 1, 130, 256), (1, 1, 37, 1000), (1, 1, 4, 64), (1, 1, 70, 18)]
+          (1, 1, 130, 256), (1, 1, 37, 1000), (1, 1, 4, 64), (1, 1, 70, 18), (1, 1, 1, 16), (2, 1, 2, 32),
+          (1, 1, 3, 248)]
 
 
 def _values(r, shape):
@@ -45,7 +48,7 @@ def test_single_operator_vs_oracle(cuda, dilation, k, mode):
 
 @pytest.mark.parametrize("kind", ["opening", "closing", "white_tophat", "black_tophat"])
 @pytest.mark.parametrize("k", [3, 5])
-@pytest.mark.parametrize("mode", ["reflect", "constant", "wrap", "nearest"])
+@pytest.mark.parametrize("mode", list(MODES))
 def test_one_pass_vs_oracle(cuda, kind, k, mode):
     r = rng(k * 100 + len(kind) + len(mode))
     for shape in SHAPES:
@@ -80,7 +83,7 @@ def test_walker_declines_unaligned_and_offset_items(cuda):
 
 @pytest.mark.parametrize("kind", ["gradient", "laplace"])
 @pytest.mark.parametrize("k", [3, 5])
-@pytest.mark.parametrize("mode", ["reflect", "constant", "mirror"])
+@pytest.mark.parametrize("mode", list(MODES))
 def test_gradient_and_laplace_vs_oracle(cuda, kind, k, mode):
     """Both extrema in one walk: dilation - erosion and (dilation + erosion) - 2 x,
     rounded like the reference's elementwise ops on the two operator images."""

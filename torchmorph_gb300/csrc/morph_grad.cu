@@ -761,37 +761,16 @@ int run_composite(int op, const float *in, float *out, int64_t batch, int ndim, 
         bool flat = sshape[1] == k && (k == 3 || k == 5) && origin[0] == 0 && origin[1] == 0 && pd.ntaps == k * k;
         for (int t = 1; t < pd.ntaps && flat; t++) flat = std::memcmp(&td.val[t], &td.val[0], sizeof(float)) == 0;
         if (flat) {
-            vwalk::Params wp;
             bool done = false;
             const int H = (int)shape[0], W = (int)shape[1];
             const float sv = td.val[0];
             if (op == 0)
-                st = k == 3 ? vwalk::launch<true, 1, 0, 3, vwalk::kGradient>(in, out, H, W, batch, sv, s, &wp, &done)
-                            : vwalk::launch<true, 1, 0, 5, vwalk::kGradient>(in, out, H, W, batch, sv, s, &wp, &done);
+                st = k == 3 ? vwalk::run<true, 1, 0, 3, vwalk::kGradient>(in, out, H, W, batch, mode, cval, sv, s, &done)
+                            : vwalk::run<true, 1, 0, 5, vwalk::kGradient>(in, out, H, W, batch, mode, cval, sv, s, &done);
             else
-                st = k == 3 ? vwalk::launch<true, 1, 0, 3, vwalk::kLaplace>(in, out, H, W, batch, sv, s, &wp, &done)
-                            : vwalk::launch<true, 1, 0, 5, vwalk::kLaplace>(in, out, H, W, batch, sv, s, &wp, &done);
-            if (st != TM_OK) return st;
-            if (done) {
-                vwalk::FrameParams f;
-                f.H = H;
-                f.W = W;
-                f.batch = batch;
-                f.lo1y = f.lo1x = -(k / 2);
-                f.lo2y = f.lo2x = 0;
-                f.mode = mode;
-                f.cval = cval;
-                f.sval = sv;
-                f.ry0 = wp.ry0;
-                f.ry1 = wp.ry1;
-                f.rx0 = 4;
-                f.rx1 = W - 4;
-                if (op == 0)
-                    return k == 3 ? vwalk::launch_frame<true, 1, 0, 3, vwalk::kGradient>(in, out, f, s)
-                                  : vwalk::launch_frame<true, 1, 0, 5, vwalk::kGradient>(in, out, f, s);
-                return k == 3 ? vwalk::launch_frame<true, 1, 0, 3, vwalk::kLaplace>(in, out, f, s)
-                              : vwalk::launch_frame<true, 1, 0, 5, vwalk::kLaplace>(in, out, f, s);
-            }
+                st = k == 3 ? vwalk::run<true, 1, 0, 3, vwalk::kLaplace>(in, out, H, W, batch, mode, cval, sv, s, &done)
+                            : vwalk::run<true, 1, 0, 5, vwalk::kLaplace>(in, out, H, W, batch, mode, cval, sv, s, &done);
+            if (st != TM_OK || done) return st;
         }
     }
     int mny = 0, mxy = 0, mnx = 0, mxx = 0;  // union of both tap regions (and the voxel itself)

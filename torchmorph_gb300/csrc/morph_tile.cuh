@@ -54,7 +54,7 @@ struct MorphOp<uint8_t, true> {  // binary dilation (OR)
 
 // Border mapping (torchmorph/csrc/grey_kernel.cu:63-97).  Returns -1 when
 // the constant value must be used.
-__device__ __forceinline__ int map_coord(int c, int n, int mode) {
+__host__ __device__ __forceinline__ int map_coord(int c, int n, int mode) {
     if ((unsigned)c < (unsigned)n) return c;
     switch (mode) {
     case TM_MODE_NEAREST:

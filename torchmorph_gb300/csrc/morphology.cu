@@ -471,28 +471,10 @@ int run_morphology(const T *in, T *out, int64_t batch, int ndim, const int64_t *
                 if (ndim == 2 && p.kh == p.kw && (p.kh == 3 || p.kh == 5) && p.lo_y == -(p.kh / 2) &&
                     p.lo_x == -(p.kw / 2)) {
                     bool done = false;
-                    vwalk::Params wp;
-                    st = p.kh == 3 ? vwalk::launch<MAX, 1, 0, 3>(in, out, p.H, p.W, batch, p.sval, stream, &wp, &done)
-                                   : vwalk::launch<MAX, 1, 0, 5>(in, out, p.H, p.W, batch, p.sval, stream, &wp, &done);
-                    if (st != TM_OK) return st;
-                    if (done) {
-                        vwalk::FrameParams f;
-                        f.H = p.H;
-                        f.W = p.W;
-                        f.batch = batch;
-                        f.lo1y = p.lo_y;
-                        f.lo1x = p.lo_x;
-                        f.lo2y = f.lo2x = 0;
-                        f.mode = p.mode;
-                        f.cval = p.cval;
-                        f.sval = p.sval;
-                        f.ry0 = wp.ry0;
-                        f.ry1 = wp.ry1;
-                        f.rx0 = 4;
-                        f.rx1 = p.W - 4;
-                        return p.kh == 3 ? vwalk::launch_frame<MAX, 1, 0, 3>(in, out, f, stream)
-                                         : vwalk::launch_frame<MAX, 1, 0, 5>(in, out, f, stream);
-                    }
+                    st = p.kh == 3
+                             ? vwalk::run<MAX, 1, 0, 3>(in, out, p.H, p.W, batch, mode, p.cval, p.sval, stream, &done)
+                             : vwalk::run<MAX, 1, 0, 5>(in, out, p.H, p.W, batch, mode, p.cval, p.sval, stream, &done);
+                    if (st != TM_OK || done) return st;
                 }
             }
             if (p.kh == 3 && p.kw == 3) return launch_flat2d<T, MAX, 3, 3>(in, out, p, batch, sms, stream);

@@ -402,22 +402,15 @@ int run_open2d(const float *in, float *out, int64_t batch, int ndim, const int64
     p.batch = batch;
     p.ry0 = p.ry1 = p.rx0 = p.rx1 = 0;
     const bool walk = ndim == 2 && ((p.kh == 3 && p.kw == 3) || (p.kh == 5 && p.kw == 5));
-    bool vdone = false;
     if (walk && cy == p.kh / 2 && cx == p.kw / 2) {
-        // centred windows on 16-byte aligned rows: float4 register walkers
-        vwalk::Params wp;
-        st = p.kh == 3 ? vwalk::launch<MAX1, 2, TOPHAT, 3>(in, out, p.H, p.W, batch, p.sval, s, &wp, &vdone)
-                       : vwalk::launch<MAX1, 2, TOPHAT, 5>(in, out, p.H, p.W, batch, p.sval, s, &wp, &vdone);
-        if (st != TM_OK) return st;
-        if (vdone) {
-            p.ry0 = wp.ry0;
-            p.ry1 = wp.ry1;
-            p.rx0 = 4;
-            p.rx1 = p.W - 4;
-        }
+        // centred windows on 16-byte aligned rows: float4 register walkers and a frame
+        bool done = false;
+        st = p.kh == 3 ? vwalk::run<MAX1, 2, TOPHAT, 3>(in, out, p.H, p.W, batch, mode, cval, p.sval, s, &done)
+                       : vwalk::run<MAX1, 2, TOPHAT, 5>(in, out, p.H, p.W, batch, mode, cval, p.sval, s, &done);
+        if (st != TM_OK || done) return st;
     }
-    if (walk && !vdone) walk_rect(p);
-    if (!vdone && p.ry1 > p.ry0) {
+    if (walk) walk_rect(p);
+    if (p.ry1 > p.ry0) {
         const int sw = 32 - (p.kw - 1);
         const int64_t tasks = batch * (int64_t)((p.rx1 - p.rx0 + sw - 1) / sw) *
                               ((p.ry1 - p.ry0 + kWalkRows - 1) / kWalkRows);

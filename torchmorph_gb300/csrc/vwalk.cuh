@@ -1,11 +1,13 @@
 // Register walkers for centred 3 x 3 and 5 x 5 flat windows over float32
 // items whose rows are 16-byte aligned (GB300, sm_103a): grey erosion and
-// dilation (one stage) and the one-pass opening, closing and top-hats (two
-// stages).  They take the outputs whose whole footprint, and every
-// intermediate value those outputs use, lies inside the item: rows
-// [STAGES * h, H - STAGES * h) and columns [4, W - 4), h = K / 2.  Outputs
-// outside that rectangle (a frame a few voxels wide) go to a per-output
-// kernel that applies the border mode.
+// dilation, the morphological gradient and laplace (one stage) and the
+// one-pass opening, closing and top-hats (two stages).  The walkers take
+// the outputs whose whole footprint, and every intermediate value those
+// outputs use, lies inside the item: rows [STAGES * h, H - STAGES * h) and
+// columns [4, W - 4), h = K / 2.  The outputs outside that rectangle (a
+// frame a few voxels wide) go to the frame kernel, which applies the border
+// mode; it is launched first and lets the walker launch at once
+// (programmatic dependent launch), so the two overlap.
 //
 // One warp walks down a strip of 128 input columns: lane l holds columns
 // x0 + 4l .. x0 + 4l + 3 of each row as one float4 load, its horizontal
@@ -51,17 +53,21 @@ struct Params {
     float sval;
 };
 
-// o[i] = Op over the columns i - h .. i + h of the lane's four columns,
-// neighbours from the adjacent lanes.
-template <class Op, int h>
-__device__ __forceinline__ void row_window(const float (&v)[4], float (&o)[4]) {
-    float a[4 + 2 * h];
+// a[h + i] = v[i]; a[0 .. h - 1] and a[h + 4 ..] the columns left and right
+// of the lane's four, from the adjacent lanes.
+template <int h>
+__device__ __forceinline__ void extend(const float (&v)[4], float (&a)[4 + 2 * h]) {
 #pragma unroll
     for (int i = 0; i < 4; i++) a[h + i] = v[i];
 #pragma unroll
     for (int j = 1; j <= h; j++) a[h - j] = __shfl_up_sync(0xffffffffu, v[4 - j], 1);
 #pragma unroll
     for (int j = 0; j < h; j++) a[h + 4 + j] = __shfl_down_sync(0xffffffffu, v[j], 1);
+}
+
+// o[i] = Op over the columns i - h .. i + h.
+template <class Op, int h>
+__device__ __forceinline__ void row_window(const float (&a)[4 + 2 * h], float (&o)[4]) {
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         float m = a[i];
@@ -71,16 +77,9 @@ __device__ __forceinline__ void row_window(const float (&v)[4], float (&o)[4]) {
     }
 }
 
-// Both extrema over the columns i - h .. i + h (one set of shuffles).
+// Both extrema over the columns i - h .. i + h.
 template <int h>
-__device__ __forceinline__ void row_window_both(const float (&v)[4], float (&mx)[4], float (&mn)[4]) {
-    float a[4 + 2 * h];
-#pragma unroll
-    for (int i = 0; i < 4; i++) a[h + i] = v[i];
-#pragma unroll
-    for (int j = 1; j <= h; j++) a[h - j] = __shfl_up_sync(0xffffffffu, v[4 - j], 1);
-#pragma unroll
-    for (int j = 0; j < h; j++) a[h + 4 + j] = __shfl_down_sync(0xffffffffu, v[j], 1);
+__device__ __forceinline__ void row_window_both(const float (&a)[4 + 2 * h], float (&mx)[4], float (&mn)[4]) {
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         float hi = a[i], lo = a[i];
@@ -112,11 +111,19 @@ __device__ __forceinline__ void col_window(float (&ring)[K - 1][4], const float 
     for (int i = 0; i < 4; i++) ring[K - 2][i] = hnew[i];
 }
 
-// COMBINE: 0 the operators alone; kGradient dilation - erosion, kLaplace
-// (dilation + erosion) - 2 x, both of one stage over the same window.
-template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE = 0>
-__global__ void __launch_bounds__(kThreads) vwalk_kernel(const float *__restrict__ in, float *__restrict__ out,
-                                                         Params p) {
+// Resident blocks per SM the register budget is set for: 3 x 3 walks get
+// 80 registers (three blocks: the loads in flight of 24 warps matter more
+// than a few spilled values) unless they also hold input rows (top-hats,
+// laplace: 128), 5 x 5 one-stage walks 128, two stages of 5 x 5 more (one
+// block).
+constexpr int kMinBlocks(int stages, int k, int tophat, int combine) {
+    return k == 3 ? (tophat != 0 || combine == 2 ? 2 : 3) : (stages == 1 ? 2 : 1);
+}
+
+// One task: output rows [ya, yb) of the strip at the lane's columns.
+template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE>
+__device__ __forceinline__ void walk_task(const float4 *src, float4 *dst, int ya, int yb, bool loads, bool writes,
+                                          const Params &p) {
     using Op1 = MorphOp<float, MAX1>;
     using Op2 = MorphOp<float, !MAX1>;
     constexpr int h = K / 2;
@@ -124,6 +131,84 @@ __global__ void __launch_bounds__(kThreads) vwalk_kernel(const float *__restrict
     constexpr int kFill = 2 * kLag;         // input rows before the first output
     constexpr bool kHoldX = TOPHAT != kTophatNone || COMBINE == kLaplace;
     constexpr int kXHold = kHoldX ? kLag : 1;
+    const int rs = ya - kLag, re = yb - 1 + kLag;  // input rows
+    const int wq = p.W >> 2;
+    float ring1[K - 1][4], ring2[K - 1][4], xh[kXHold][4];
+    float4 cur[kChunk], nxt[kChunk];
+#pragma unroll
+    for (int k = 0; k < kChunk; k++)
+        cur[k] = (loads && rs + k <= re) ? __ldg(src + (int64_t)(rs + k) * wq) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int r0 = rs; r0 <= re; r0 += kChunk) {
+        if (r0 + kChunk <= re) {
+#pragma unroll
+            for (int k = 0; k < kChunk; k++) {
+                const int r = r0 + kChunk + k;
+                nxt[k] = (loads && r <= re) ? __ldg(src + (int64_t)r * wq) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kChunk; k++) {
+            const int r = r0 + k;
+            if (r > re) continue;
+            const float v[4] = {cur[k].x, cur[k].y, cur[k].z, cur[k].w};
+            float a[4 + 2 * h];
+            extend<h>(v, a);
+            float hr[4], e[4], o[4];
+            if constexpr (COMBINE != 0) {
+                // ring1 holds the maxima, ring2 the minima; rounded like the
+                // reference's elementwise ops on the two operator images
+                float hl[4], d[4];
+                row_window_both<h>(a, hr, hl);
+                col_window<MorphOp<float, true>, K>(ring1, hr, d);
+                col_window<MorphOp<float, false>, K>(ring2, hl, e);
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const float dv = __fadd_rn(d[i], p.sval), ev = __fsub_rn(e[i], p.sval);
+                    o[i] = COMBINE == kGradient ? __fsub_rn(dv, ev)
+                                                : __fsub_rn(__fadd_rn(dv, ev), __fmul_rn(2.f, xh[0][i]));
+                }
+            } else {
+                row_window<Op1, h>(a, hr);
+                col_window<Op1, K>(ring1, hr, e);
+#pragma unroll
+                for (int i = 0; i < 4; i++) e[i] = Op1::apply(e[i], p.sval);
+                if constexpr (STAGES == 1) {
+#pragma unroll
+                    for (int i = 0; i < 4; i++) o[i] = e[i];
+                } else {
+                    float a2[4 + 2 * h], h2[4];
+                    extend<h>(e, a2);
+                    row_window<Op2, h>(a2, h2);
+                    col_window<Op2, K>(ring2, h2, o);
+#pragma unroll
+                    for (int i = 0; i < 4; i++) o[i] = Op2::apply(o[i], p.sval);
+                }
+            }
+            if constexpr (kHoldX) {
+                // xh holds input rows r - kLag .. r - 1
+                if constexpr (TOPHAT != kTophatNone) {
+#pragma unroll
+                    for (int i = 0; i < 4; i++) o[i] = TOPHAT == kTophatWhite ? xh[0][i] - o[i] : o[i] - xh[0][i];
+                }
+#pragma unroll
+                for (int j = 0; j + 1 < kXHold; j++)
+#pragma unroll
+                    for (int i = 0; i < 4; i++) xh[j][i] = xh[j + 1][i];
+#pragma unroll
+                for (int i = 0; i < 4; i++) xh[kXHold - 1][i] = v[i];
+            }
+            if (r - rs >= kFill && writes) __stcs(dst + (int64_t)(r - kLag) * wq, make_float4(o[0], o[1], o[2], o[3]));
+        }
+#pragma unroll
+        for (int k = 0; k < kChunk; k++) cur[k] = nxt[k];
+    }
+}
+
+// COMBINE: 0 the operators alone; kGradient dilation - erosion, kLaplace
+// (dilation + erosion) - 2 x, both of one stage over the same window.
+template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE = 0>
+__global__ void __launch_bounds__(kThreads, kMinBlocks(STAGES, K, TOPHAT, COMBINE))
+    vwalk_kernel(const float *__restrict__ in, float *__restrict__ out, Params p) {
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
     for (int64_t t = (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); t < p.ntasks; t += nwarps) {
@@ -136,80 +221,14 @@ __global__ void __launch_bounds__(kThreads) vwalk_kernel(const float *__restrict
         const bool writes = lane >= 1 && lane <= kLanesOut && c + 8 <= p.W;
         const int ya = p.ry0 + rb * p.rows;
         const int yb = min(ya + p.rows, p.ry1);
-        const int rs = ya - kLag, re = yb - 1 + kLag;        // input rows, inside the item
         const float4 *src = reinterpret_cast<const float4 *>(in + item * (int64_t)p.H * p.W) + (c >> 2);
         float4 *dst = reinterpret_cast<float4 *>(out + item * (int64_t)p.H * p.W) + (c >> 2);
-        const int wq = p.W >> 2;
-
-        float ring1[K - 1][4], ring2[K - 1][4], xh[kXHold][4];
-        float4 cur[kChunk], nxt[kChunk];
-#pragma unroll
-        for (int k = 0; k < kChunk; k++)
-            cur[k] = (loads && rs + k <= re) ? __ldg(src + (int64_t)(rs + k) * wq) : make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int r0 = rs; r0 <= re; r0 += kChunk) {
-            if (r0 + kChunk <= re) {
-#pragma unroll
-                for (int k = 0; k < kChunk; k++) {
-                    const int r = r0 + kChunk + k;
-                    nxt[k] = (loads && r <= re) ? __ldg(src + (int64_t)r * wq) : make_float4(0.f, 0.f, 0.f, 0.f);
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < kChunk; k++) {
-                const int r = r0 + k;
-                if (r > re) continue;
-                const float v[4] = {cur[k].x, cur[k].y, cur[k].z, cur[k].w};
-                float hr[4], e[4], o[4];
-                if constexpr (COMBINE != 0) {
-                    // ring1 holds the maxima, ring2 the minima; rounded like the
-                    // reference's elementwise ops on the two operator images
-                    float hl[4], d[4];
-                    row_window_both<h>(v, hr, hl);
-                    col_window<MorphOp<float, true>, K>(ring1, hr, d);
-                    col_window<MorphOp<float, false>, K>(ring2, hl, e);
-#pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        const float dv = __fadd_rn(d[i], p.sval), ev = __fsub_rn(e[i], p.sval);
-                        o[i] = COMBINE == kGradient ? __fsub_rn(dv, ev)
-                                                    : __fsub_rn(__fadd_rn(dv, ev), __fmul_rn(2.f, xh[0][i]));
-                    }
-                } else {
-                    row_window<Op1, h>(v, hr);
-                    col_window<Op1, K>(ring1, hr, e);
-#pragma unroll
-                    for (int i = 0; i < 4; i++) e[i] = Op1::apply(e[i], p.sval);
-                    if constexpr (STAGES == 1) {
-#pragma unroll
-                        for (int i = 0; i < 4; i++) o[i] = e[i];
-                    } else {
-                        float h2[4];
-                        row_window<Op2, h>(e, h2);
-                        col_window<Op2, K>(ring2, h2, o);
-#pragma unroll
-                        for (int i = 0; i < 4; i++) o[i] = Op2::apply(o[i], p.sval);
-                    }
-                }
-                if constexpr (kHoldX) {
-                    // xh holds input rows r - kLag .. r - 1
-                    if constexpr (TOPHAT != kTophatNone) {
-#pragma unroll
-                        for (int i = 0; i < 4; i++)
-                            o[i] = TOPHAT == kTophatWhite ? xh[0][i] - o[i] : o[i] - xh[0][i];
-                    }
-#pragma unroll
-                    for (int j = 0; j + 1 < kXHold; j++)
-#pragma unroll
-                        for (int i = 0; i < 4; i++) xh[j][i] = xh[j + 1][i];
-#pragma unroll
-                    for (int i = 0; i < 4; i++) xh[kXHold - 1][i] = v[i];
-                }
-                if (r - rs >= kFill && writes)
-                    __stcs(dst + (int64_t)(r - kLag) * wq, make_float4(o[0], o[1], o[2], o[3]));
-            }
-#pragma unroll
-            for (int k = 0; k < kChunk; k++) cur[k] = nxt[k];
-        }
+        walk_task<MAX1, STAGES, TOPHAT, K, COMBINE>(src, dst, ya, yb, loads, writes, p);
     }
+    // launched right behind the frame kernel (programmatic dependent launch):
+    // finish only once the frame kernel has, so the next work of the stream
+    // sees every output
+    pdl_wait();
 }
 
 // Outputs outside the walkers' rectangle [ry0, ry1) x [rx0, rx1) (a frame a
@@ -361,6 +380,7 @@ __device__ __forceinline__ float frame_value(const float *src, const FrameParams
 template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE>
 __global__ void __launch_bounds__(256) frame_kernel(const float *__restrict__ in, float *__restrict__ out,
                                                     FrameParams f) {
+    pdl_trigger();  // the walker (launched behind this kernel) may start now
     const int ring = f.H * f.W - (f.ry1 - f.ry0) * (f.rx1 - f.rx0);
     const int side = f.rx0 + (f.W - f.rx1);
     const int top = f.ry0 * f.W, mid = (f.ry1 - f.ry0) * side;
@@ -402,9 +422,9 @@ int launch_frame(const float *in, float *out, const FrameParams &f, cudaStream_t
 }
 
 // Plans the walk: false when the item does not fit (rows not 16-byte
-// aligned, too narrow or too short for the rectangle).  resident_warps is
-// the number of walker warps the device holds at once; the row block is
-// chosen so the tasks fill whole waves of them.
+// aligned, too narrow or too short).  resident_warps is the number of walker
+// warps the device holds at once; the row block is chosen so the tasks fill
+// whole waves of them.
 inline bool plan(int H, int W, int64_t batch, int K, int stages, const void *in, const void *out,
                  int64_t resident_warps, Params &p) {
     const int lag = stages * (K / 2);
@@ -435,19 +455,20 @@ inline bool plan(int H, int W, int64_t batch, int K, int stages, const void *in,
     return true;
 }
 
-// Launches the walker over the rectangle (and nothing else); false when the
-// item does not fit the walker.
+// Centred K x K flat window (value sval) of float32 items: the frame kernel,
+// then the walkers launched behind it.  Sets *done = false and launches
+// nothing when the items do not fit the walkers.
 template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE = 0>
-int launch(const float *in, float *out, int H, int W, int64_t batch, float sval, cudaStream_t s, Params *planned,
-           bool *done) {
+int run(const float *in, float *out, int H, int W, int64_t batch, int mode, float cval, float sval, cudaStream_t s,
+        bool *done) {
     *done = false;
     static thread_local int cached_dev = -1, cached_per_sm = 1;
     int dev = 0;
     TM_CHECK_CUDA(cudaGetDevice(&dev));
     if (cached_dev != dev) {
         int per_sm = 0;
-        TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vwalk_kernel<MAX1, STAGES, TOPHAT, K, COMBINE>,
-                                                                    kThreads, 0));
+        TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, vwalk_kernel<MAX1, STAGES, TOPHAT, K, COMBINE>, kThreads, 0));
         cached_per_sm = std::max(per_sm, 1);
         cached_dev = dev;
     }
@@ -455,12 +476,25 @@ int launch(const float *in, float *out, int H, int W, int64_t batch, float sval,
     Params p;
     if (!plan(H, W, batch, K, STAGES, in, out, resident_blocks * (kThreads / 32), p)) return TM_OK;
     p.sval = sval;
+    *done = true;
+    FrameParams f;
+    f.H = H;
+    f.W = W;
+    f.batch = batch;
+    f.lo1y = f.lo1x = f.lo2y = f.lo2x = -(K / 2);
+    f.mode = mode;
+    f.cval = cval;
+    f.sval = sval;
+    f.ry0 = p.ry0;
+    f.ry1 = p.ry1;
+    f.rx0 = 4;
+    f.rx1 = W - 4;
+    int st = launch_frame<MAX1, STAGES, TOPHAT, K, COMBINE>(in, out, f, s);
+    if (st != TM_OK) return st;
     const int64_t blocks = std::min<int64_t>(ceil_div(p.ntasks, kThreads / 32), resident_blocks);
     if (p.ntasks > 0)
-        vwalk_kernel<MAX1, STAGES, TOPHAT, K, COMBINE><<<(unsigned)blocks, kThreads, 0, s>>>(in, out, p);
-    TM_LAUNCH_CHECK("vwalk_kernel");
-    *planned = p;
-    *done = true;
+        TM_CHECK_CUDA(launch_pdl(vwalk_kernel<MAX1, STAGES, TOPHAT, K, COMBINE>, dim3((unsigned)blocks),
+                                 dim3(kThreads), 0, s, in, out, p));
     return TM_OK;
 }
 
