@@ -185,6 +185,8 @@ __global__ void __launch_bounds__(kCols *kSegs) edt_c0_smem_kernel(const In *__r
                                                                    int16_t *__restrict__ c1, CompactParams p,
                                                                    const int *__restrict__ todo) {
     pdl_wait();  // launched after the shell search: its flags are complete
+    // the plane passes may be scheduled now: the flags they read are final
+    pdl_trigger();
     const int64_t cblocks = (p.numel_item / p.L0 + kCols - 1) / kCols;
     const int64_t nblk = p.batch * cblocks;
     for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
@@ -1049,11 +1051,18 @@ __global__ void __launch_bounds__(kC12Threads, 3) edt_c12_kernel(const int16_t *
                                                               int32_t *__restrict__ indices,
                                                               int32_t *__restrict__ sqdist, CompactParams p,
                                                               const int *__restrict__ todo) {
-    pdl_wait();  // launched after pass 0: its features are complete
+    // Launched behind pass 0, which lets this grid be scheduled once the shell
+    // search has completed: the flags are final here (read through L2), and a
+    // block waits for pass 0's features only when it has a plane to compute.
     const int64_t nblk = p.batch * (int64_t)p.L0;
+    bool waited = false;
     for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
         const int64_t item = blk / p.L0;
-        if (todo && !todo[item]) continue;  // item finished by the shell pass
+        if (todo && !__ldcg(todo + item)) continue;  // item finished by the shell pass
+        if (!waited) {
+            pdl_wait();  // pass 0's features are complete
+            waited = true;
+        }
         const int z = (int)(blk - item * p.L0);
         edt_c12_plane<true>(item * p.numel_item + (int64_t)z * p.L1 * p.L2, z, p.L1, p.L2, p.numel, c1, dist, indices,
                             sqdist);

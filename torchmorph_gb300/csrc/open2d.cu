@@ -438,8 +438,8 @@ int run_open2d(const float *in, float *out, int64_t batch, int ndim, const int64
             f.ry1 = p.ry1;
             f.rx0 = p.rx0;
             f.rx1 = p.rx1;
-            return p.kh == 3 ? vwalk::launch_frame<MAX1, 2, TOPHAT, 3>(in, out, f, s)
-                             : vwalk::launch_frame<MAX1, 2, TOPHAT, 5>(in, out, f, s);
+            return p.kh == 3 ? vwalk::launch_frame<MAX1, 2, TOPHAT, 3>(in, out, f, s, false)
+                             : vwalk::launch_frame<MAX1, 2, TOPHAT, 5>(in, out, f, s, false);
         }
     }
     // tiles entirely inside the walkers' rectangle are skipped by the tile kernel

@@ -6,8 +6,8 @@
 // outputs use, lies inside the item: rows [STAGES * h, H - STAGES * h) and
 // columns [4, W - 4), h = K / 2.  The outputs outside that rectangle (a
 // frame a few voxels wide) go to the frame kernel, which applies the border
-// mode; it is launched first and lets the walker launch at once
-// (programmatic dependent launch), so the two overlap.
+// mode; it is launched behind the walkers with programmatic dependent launch,
+// so its blocks fill the SMs as the walkers' CTAs retire.
 //
 // One warp walks down a strip of 128 input columns: lane l holds columns
 // x0 + 4l .. x0 + 4l + 3 of each row as one float4 load, its horizontal
@@ -209,6 +209,7 @@ __device__ __forceinline__ void walk_task(const float4 *src, float4 *dst, int ya
 template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE = 0>
 __global__ void __launch_bounds__(kThreads, kMinBlocks(STAGES, K, TOPHAT, COMBINE))
     vwalk_kernel(const float *__restrict__ in, float *__restrict__ out, Params p) {
+    pdl_trigger();  // the frame kernel may fill the SMs as this grid's CTAs retire
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
     for (int64_t t = (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); t < p.ntasks; t += nwarps) {
@@ -225,10 +226,6 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks(STAGES, K, TOPHAT, COMBIN
         float4 *dst = reinterpret_cast<float4 *>(out + item * (int64_t)p.H * p.W) + (c >> 2);
         walk_task<MAX1, STAGES, TOPHAT, K, COMBINE>(src, dst, ya, yb, loads, writes, p);
     }
-    // launched right behind the frame kernel (programmatic dependent launch):
-    // finish only once the frame kernel has, so the next work of the stream
-    // sees every output
-    pdl_wait();
 }
 
 // Outputs outside the walkers' rectangle [ry0, ry1) x [rx0, rx1) (a frame a
@@ -380,7 +377,6 @@ __device__ __forceinline__ float frame_value(const float *src, const FrameParams
 template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE>
 __global__ void __launch_bounds__(256) frame_kernel(const float *__restrict__ in, float *__restrict__ out,
                                                     FrameParams f) {
-    pdl_trigger();  // the walker (launched behind this kernel) may start now
     const int ring = f.H * f.W - (f.ry1 - f.ry0) * (f.rx1 - f.rx0);
     const int side = f.rx0 + (f.W - f.rx1);
     const int top = f.ry0 * f.W, mid = (f.ry1 - f.ry0) * side;
@@ -406,18 +402,29 @@ __global__ void __launch_bounds__(256) frame_kernel(const float *__restrict__ in
             dst[(int64_t)y * f.W + x] = frame_value<MAX1, STAGES, TOPHAT, K, COMBINE>(src, f, y, x);
         }
     }
+    // launched behind the walkers (programmatic dependent launch): finish only
+    // once they have, so the next work of the stream sees every output
+    pdl_wait();
 }
 
-// Launches the frame kernel for the outputs outside the rectangle.
+// Launches the frame kernel for the outputs outside the rectangle.  Right
+// behind a walker launch it may start early (programmatic dependent launch:
+// the frame reads only the input and writes only its own outputs); behind
+// anything else it is an ordinary launch.
 template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE = 0>
-int launch_frame(const float *in, float *out, const FrameParams &f, cudaStream_t s) {
+int launch_frame(const float *in, float *out, const FrameParams &f, cudaStream_t s, bool behind_walker) {
     const int64_t ring = (int64_t)f.H * f.W - (int64_t)(f.ry1 - f.ry0) * (f.rx1 - f.rx0);
     if (ring <= 0 || f.batch <= 0) return TM_OK;
     const unsigned gy = (unsigned)std::min<int64_t>(f.batch, 65535);
     const int64_t want = std::max<int64_t>(1, (int64_t)sm_count() * 16 / gy);
     const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(ring, 256), want));
-    frame_kernel<MAX1, STAGES, TOPHAT, K, COMBINE><<<dim3(gx, gy), 256, 0, s>>>(in, out, f);
-    TM_LAUNCH_CHECK("vwalk::frame_kernel");
+    if (behind_walker) {
+        TM_CHECK_CUDA(
+            launch_pdl(frame_kernel<MAX1, STAGES, TOPHAT, K, COMBINE>, dim3(gx, gy), dim3(256), 0, s, in, out, f));
+    } else {
+        frame_kernel<MAX1, STAGES, TOPHAT, K, COMBINE><<<dim3(gx, gy), 256, 0, s>>>(in, out, f);
+        TM_LAUNCH_CHECK("vwalk::frame_kernel");
+    }
     return TM_OK;
 }
 
@@ -455,8 +462,8 @@ inline bool plan(int H, int W, int64_t batch, int K, int stages, const void *in,
     return true;
 }
 
-// Centred K x K flat window (value sval) of float32 items: the frame kernel,
-// then the walkers launched behind it.  Sets *done = false and launches
+// Centred K x K flat window (value sval) of float32 items: the walkers, then
+// the frame kernel launched behind them.  Sets *done = false and launches
 // nothing when the items do not fit the walkers.
 template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE = 0>
 int run(const float *in, float *out, int H, int W, int64_t batch, int mode, float cval, float sval, cudaStream_t s,
@@ -489,13 +496,10 @@ int run(const float *in, float *out, int H, int W, int64_t batch, int mode, floa
     f.ry1 = p.ry1;
     f.rx0 = 4;
     f.rx1 = W - 4;
-    int st = launch_frame<MAX1, STAGES, TOPHAT, K, COMBINE>(in, out, f, s);
-    if (st != TM_OK) return st;
     const int64_t blocks = std::min<int64_t>(ceil_div(p.ntasks, kThreads / 32), resident_blocks);
-    if (p.ntasks > 0)
-        TM_CHECK_CUDA(launch_pdl(vwalk_kernel<MAX1, STAGES, TOPHAT, K, COMBINE>, dim3((unsigned)blocks),
-                                 dim3(kThreads), 0, s, in, out, p));
-    return TM_OK;
+    if (p.ntasks > 0) vwalk_kernel<MAX1, STAGES, TOPHAT, K, COMBINE><<<(unsigned)blocks, kThreads, 0, s>>>(in, out, p);
+    TM_LAUNCH_CHECK("vwalk_kernel");
+    return launch_frame<MAX1, STAGES, TOPHAT, K, COMBINE>(in, out, f, s, p.ntasks > 0);
 }
 
 }  // namespace vwalk
