@@ -113,11 +113,10 @@ __device__ __forceinline__ void col_window(float (&ring)[K - 1][4], const float 
 
 // Resident blocks per SM the register budget is set for: 3 x 3 walks get
 // 80 registers (three blocks: the loads in flight of 24 warps matter more
-// than a few spilled values) unless they also hold input rows (top-hats,
-// laplace: 128), 5 x 5 one-stage walks 128, two stages of 5 x 5 more (one
-// block).
+// than a few spilled values) unless they hold input rows (laplace: 128),
+// 5 x 5 one-stage walks 128, two stages of 5 x 5 more (one block).
 constexpr int kMinBlocks(int stages, int k, int tophat, int combine) {
-    return k == 3 ? (tophat != 0 || combine == 2 ? 2 : 3) : (stages == 1 ? 2 : 1);
+    return k == 3 ? (combine == 2 ? 2 : 3) : (stages == 1 ? 2 : 1);
 }
 
 // One task: output rows [ya, yb) of the strip at the lane's columns.
@@ -129,7 +128,9 @@ __device__ __forceinline__ void walk_task(const float4 *src, float4 *dst, int ya
     constexpr int h = K / 2;
     constexpr int kLag = STAGES * h;        // output row = input row - kLag
     constexpr int kFill = 2 * kLag;         // input rows before the first output
-    constexpr bool kHoldX = TOPHAT != kTophatNone || COMBINE == kLaplace;
+    // the laplace holds its input rows in registers; the top-hats reload the
+    // input row of the output (kLag rows back: an L1 hit) to stay in 80 registers
+    constexpr bool kHoldX = COMBINE == kLaplace;
     constexpr int kXHold = kHoldX ? kLag : 1;
     const int rs = ya - kLag, re = yb - 1 + kLag;  // input rows
     const int wq = p.W >> 2;
@@ -184,12 +185,16 @@ __device__ __forceinline__ void walk_task(const float4 *src, float4 *dst, int ya
                     for (int i = 0; i < 4; i++) o[i] = Op2::apply(o[i], p.sval);
                 }
             }
+            if constexpr (TOPHAT != kTophatNone) {
+                if (r - rs >= kFill && writes) {
+                    const float4 xv = __ldg(src + (int64_t)(r - kLag) * wq);
+                    const float xa[4] = {xv.x, xv.y, xv.z, xv.w};
+#pragma unroll
+                    for (int i = 0; i < 4; i++) o[i] = TOPHAT == kTophatWhite ? xa[i] - o[i] : o[i] - xa[i];
+                }
+            }
             if constexpr (kHoldX) {
                 // xh holds input rows r - kLag .. r - 1
-                if constexpr (TOPHAT != kTophatNone) {
-#pragma unroll
-                    for (int i = 0; i < 4; i++) o[i] = TOPHAT == kTophatWhite ? xh[0][i] - o[i] : o[i] - xh[0][i];
-                }
 #pragma unroll
                 for (int j = 0; j + 1 < kXHold; j++)
 #pragma unroll
