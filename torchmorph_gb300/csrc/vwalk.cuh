@@ -6,8 +6,9 @@
 // outputs use, lies inside the item: rows [STAGES * h, H - STAGES * h) and
 // columns [4, W - 4), h = K / 2.  The outputs outside that rectangle (a
 // frame a few voxels wide) go to the frame kernel, which applies the border
-// mode; it is launched behind the walkers with programmatic dependent launch,
-// so its blocks fill the SMs as the walkers' CTAs retire.
+// mode; it is launched behind the walkers with programmatic dependent launch
+// in small blocks that fit beside the walkers' CTAs, so it runs while they
+// stream.
 //
 // One warp walks down a strip of 128 input columns: lane l holds columns
 // x0 + 4l .. x0 + 4l + 3 of each row as one float4 load, its horizontal
@@ -421,6 +422,19 @@ int launch_frame(const float *in, float *out, const FrameParams &f, cudaStream_t
     const int64_t ring = (int64_t)f.H * f.W - (int64_t)(f.ry1 - f.ry0) * (f.rx1 - f.rx0);
     if (ring <= 0 || f.batch <= 0) return TM_OK;
     const unsigned gy = (unsigned)std::min<int64_t>(f.batch, 65535);
+    if (behind_walker && STAGES == 1) {
+        // one stage (9 or 25 loads per output): blocks of 64 threads fit beside
+        // the walker's CTAs (in the registers a 3 x 3 walk leaves: 65536 -
+        // 3 x 256 x 80 = 4096), so the frame is computed while the walker
+        // streams: about one block per SM, at most 32 outputs per thread
+        const int64_t want = std::max<int64_t>(sm_count(), ceil_div(ring * f.batch, 64 * 32));
+        const unsigned gx = (unsigned)std::max<int64_t>(1, ceil_div(want, gy));
+        TM_CHECK_CUDA(
+            launch_pdl(frame_kernel<MAX1, STAGES, TOPHAT, K, COMBINE>, dim3(gx, gy), dim3(64), 0, s, in, out, f));
+        return TM_OK;
+    }
+    // two stages (45 or more loads per output): a full wave of one output per
+    // thread, behind the walker's last CTAs
     const int64_t want = std::max<int64_t>(1, (int64_t)sm_count() * 16 / gy);
     const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(ring, 256), want));
     if (behind_walker) {
