@@ -565,6 +565,7 @@ def ragged_lines(dev, stream, steps, warmup):
     backward = {"grey_dilation_3x3_backward_8x2048x2048": {
         "forward_with_arg_us": round(t_fwd * 1e6, 1), "backward_us": round(t_bwd * 1e6, 1),
         "forward_with_arg_GBps": round(9.0 * nb / t_fwd / 1e9, 1),
+        "forward_with_arg_frac_of_hbm": round(9.0 * nb / t_fwd / 1e9 / hbm, 4),
         "backward_GBps": round(9.0 * nb / t_bwd / 1e9, 1),
         "backward_frac_of_hbm": round(9.0 * nb / t_bwd / 1e9 / hbm, 4),
         "bytes_per_pixel": "forward 4 in + 4 out + 1 arg; backward 4 grad_out + 1 arg + 4 grad_in"}}

@@ -98,3 +98,52 @@ def test_gradient_and_laplace_vs_oracle(cuda, kind, k, mode):
             e = oracle.grey(x, st, mode=mode, cval=0.5)
             exp = d - e if kind == "gradient" else (d + e) - np.float32(2) * x
             np.testing.assert_array_equal(got.cpu().numpy(), exp, err_msg=str((shape, sval)))
+
+
+def _gather_f32(g, arg, k, dilation):
+    """float32 gather in tap order for pixels no border mapping reaches (rows and
+    columns in [h + 1, n - 1 - h)): the walker's sums, bit for bit."""
+    h = k // 2
+    B, C, H, W = g.shape
+    acc = np.zeros_like(g)
+    for t in range(k * k):
+        i, j = divmod(t, k)
+        dy, dx = (h - i, h - j) if dilation else (i - h, j - h)
+        # output o = p - (dy, dx)
+        gs = np.zeros_like(g)
+        as_ = np.full(arg.shape, 255, np.uint8)
+        ys, ye = max(0, dy), H + min(0, dy)
+        xs, xe = max(0, dx), W + min(0, dx)
+        gs[..., ys:ye, xs:xe] = g[..., ys - dy:ye - dy, xs - dx:xe - dx]
+        as_[..., ys:ye, xs:xe] = arg[..., ys - dy:ye - dy, xs - dx:xe - dx]
+        acc = np.where(as_ == t, acc + gs, acc).astype(np.float32)
+    return acc[..., h + 1:H - 1 - h, h + 1:W - 1 - h]
+
+
+@pytest.mark.parametrize("dilation", [False, True])
+@pytest.mark.parametrize("k", [3, 5])
+@pytest.mark.parametrize("mode", list(MODES))
+def test_arg_forward_and_backward_walkers(cuda, dilation, k, mode):
+    """Forward with argument (first tap attaining the extremum, raster order) and the
+    gather backward: values and arguments bit-exact vs the oracle, gradients vs the
+    float64 oracle and, away from the border, bit-exact vs a float32 gather in tap order.
+    Quantised values make ties common."""
+    r = rng(k * 7 + int(dilation) + len(mode))
+    for shape in SHAPES:
+        x = (np.floor(r.random(shape) * 6) / 4).astype(np.float32)
+        st = np.full((k, k), 0.125, np.float32)
+        fn = _C.grey_dilation_arg if dilation else _C.grey_erosion_arg
+        out, arg = fn(torch.from_numpy(x).cuda(), torch.from_numpy(st), torch.empty(0, dtype=torch.bool), [0, 0],
+                      MODES[mode], 0.3)
+        exp_out, exp_arg = oracle.grey_arg(x, st, None, (0, 0), mode, 0.3, dilation)
+        np.testing.assert_array_equal(out.cpu().numpy(), exp_out, err_msg=str(shape))
+        np.testing.assert_array_equal(arg.cpu().numpy(), exp_arg, err_msg=str(shape))
+        g = r.standard_normal(shape).astype(np.float32)
+        gin = _C.grey_morphology_backward(torch.from_numpy(g).cuda(), arg, [k, k],
+                                          torch.empty(0, dtype=torch.bool), [0, 0], MODES[mode], dilation)
+        gin = gin.cpu().numpy()
+        exp = oracle.grey_backward(g, exp_arg, (k, k), None, (0, 0), mode, dilation)
+        np.testing.assert_allclose(gin, exp, rtol=2e-5, atol=1e-5, err_msg=str(shape))
+        h = k // 2
+        np.testing.assert_array_equal(gin[..., h + 1:shape[2] - 1 - h, h + 1:shape[3] - 1 - h],
+                                      _gather_f32(g, exp_arg, k, dilation), err_msg=str(shape))

@@ -256,6 +256,146 @@ __global__ void __launch_bounds__(kGradThreads) morph_grad_kernel(const float *_
     }
 }
 
+// Frames of the float4 walkers (centred K x K flat boxes of 2-D items): the
+// outputs (forward) or input pixels (backward) outside the walkers'
+// rectangle, one thread each, with the per-voxel code above (same taps, same
+// order).  Launched behind the walker (programmatic dependent launch); each
+// finishes only once the walker has, so the stream's next work sees every
+// output.
+template <bool MAX>
+__global__ void __launch_bounds__(256) arg_frame_kernel(const float *__restrict__ in, float *__restrict__ out,
+                                                        uint8_t *__restrict__ arg, GradParams p,
+                                                        const __grid_constant__ GradTaps taps, vwalk::FrameRect fr) {
+    using Op = MorphOp<float, MAX>;
+    const int n = fr.count();
+    for (int64_t item = blockIdx.y; item < p.batch; item += gridDim.y) {
+        const float *src = in + item * p.numel_item;
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+            int y, x;
+            fr.at(k, y, x);
+            float best = Op::identity();
+            int a = kNoTap;
+            for (int t = 0; t < p.ntaps; t++) {
+                const int my = map_coord(y + taps.off[t][0], p.shape[0], p.mode);
+                const int mx = map_coord(x + taps.off[t][1], p.shape[1], p.mode);
+                const float v =
+                    Op::apply((my < 0 || mx < 0) ? p.cval : src[(int64_t)my * p.shape[1] + mx], taps.val[t]);
+                if (MAX ? v > best : v < best) {
+                    best = v;
+                    a = t;
+                }
+            }
+            const int64_t o = item * p.numel_item + (int64_t)y * p.shape[1] + x;
+            out[o] = best;
+            arg[o] = (uint8_t)a;
+        }
+    }
+    pdl_wait();
+}
+
+__global__ void __launch_bounds__(256) grad_frame_kernel(const float *__restrict__ gout,
+                                                         const uint8_t *__restrict__ arg, float *__restrict__ gin,
+                                                         GradParams p, const __grid_constant__ GradTaps taps,
+                                                         vwalk::FrameRect fr) {
+    const int n = fr.count();
+    for (int64_t item = blockIdx.y; item < p.batch; item += gridDim.y) {
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+            int y, x;
+            fr.at(k, y, x);
+            gin[item * p.numel_item + (int64_t)y * p.shape[1] + x] =
+                grad_pixel2d(gout + item * p.numel_item, arg + item * p.numel_item, y, x, p, taps);
+        }
+    }
+    pdl_wait();
+}
+
+// The walkers' box: a full centred K x K footprint (K 3 or 5) of a 2-D item
+// with one structure value (the backward needs no values); 0 otherwise.
+int walk_box(const GradParams &p, const GradTaps &taps, const int64_t *sshape, const int64_t *origin,
+             bool need_flat) {
+    if (p.ndim != 2 || sshape[0] != sshape[1] || origin[0] != 0 || origin[1] != 0) return 0;
+    const int k = (int)sshape[0];
+    if ((k != 3 && k != 5) || p.ntaps != k * k) return 0;
+    if (need_flat)
+        for (int t = 1; t < p.ntaps; t++)
+            if (std::memcmp(&taps.val[t], &taps.val[0], sizeof(float)) != 0) return 0;
+    return k;
+}
+
+dim3 frame_grid(const vwalk::FrameRect &fr, int64_t batch) {
+    const unsigned gy = (unsigned)std::min<int64_t>(batch, 65535);
+    const int64_t want = std::max<int64_t>(1, (int64_t)sm_count() * 16 / gy);
+    return dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(fr.count(), 256), want)), gy);
+}
+
+// Forward with argument through the walkers; *done = false when they do not apply.
+template <bool MAX>
+int run_arg_walk(const float *in, float *out, uint8_t *arg, const GradParams &p, const GradTaps &taps, int k,
+                 cudaStream_t s, bool *done) {
+    *done = false;
+    const int H = p.shape[0], W = p.shape[1];
+    if (reinterpret_cast<uintptr_t>(arg) & 3) return TM_OK;
+    static thread_local int cached_dev[2] = {-1, -1}, cached_blocks[2] = {0, 0};
+    int dev = 0;
+    TM_CHECK_CUDA(cudaGetDevice(&dev));
+    const int ki = k == 3 ? 0 : 1;
+    auto kern = k == 3 ? vwalk::vwalk_arg_kernel<MAX, 3> : vwalk::vwalk_arg_kernel<MAX, 5>;
+    if (cached_dev[ki] != dev) {
+        int per_sm = 0;
+        TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, vwalk::kThreads, 0));
+        cached_blocks[ki] = std::max(per_sm, 1) * sm_count();
+        cached_dev[ki] = dev;
+    }
+    vwalk::Params wp;
+    if (!vwalk::plan(H, W, p.batch, k, 1, in, out, (int64_t)cached_blocks[ki] * (vwalk::kThreads / 32), wp))
+        return TM_OK;
+    wp.sval = taps.val[0];
+    *done = true;
+    const int64_t blocks = std::min<int64_t>(ceil_div(wp.ntasks, vwalk::kThreads / 32), cached_blocks[ki]);
+    if (wp.ntasks > 0)
+        kern<<<(unsigned)blocks, vwalk::kThreads, 0, s>>>(in, out, reinterpret_cast<uint32_t *>(arg), wp);
+    TM_LAUNCH_CHECK("vwalk_arg_kernel");
+    const vwalk::FrameRect fr{H, W, wp.ry0, wp.ry1, 4, W - 4};
+    TM_CHECK_CUDA(launch_pdl(arg_frame_kernel<MAX>, frame_grid(fr, p.batch), dim3(256), 0, s, in, out, arg, p, taps,
+                             fr));
+    return TM_OK;
+}
+
+// Backward through the walkers; *done = false when they do not apply.
+int run_grad_walk(bool dilation, const float *gout, const uint8_t *arg, float *gin, const GradParams &p,
+                  const GradTaps &taps, int k, cudaStream_t s, bool *done) {
+    *done = false;
+    const int H = p.shape[0], W = p.shape[1];
+    if ((reinterpret_cast<uintptr_t>(arg) & 3) || (reinterpret_cast<uintptr_t>(gin) & 15)) return TM_OK;
+    using KernT = void (*)(const float *, const uint32_t *, float *, vwalk::Params);
+    const KernT kern = dilation ? (k == 3 ? vwalk::vwalk_grad_kernel<true, 3> : vwalk::vwalk_grad_kernel<true, 5>)
+                                : (k == 3 ? vwalk::vwalk_grad_kernel<false, 3> : vwalk::vwalk_grad_kernel<false, 5>);
+    static thread_local int cached_dev[4] = {-1, -1, -1, -1}, cached_blocks[4] = {0, 0, 0, 0};
+    const int ki = (dilation ? 2 : 0) + (k == 3 ? 0 : 1);
+    int dev = 0;
+    TM_CHECK_CUDA(cudaGetDevice(&dev));
+    if (cached_dev[ki] != dev) {
+        int per_sm = 0;
+        TM_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, vwalk::kThreads, 0));
+        cached_blocks[ki] = std::max(per_sm, 1) * sm_count();
+        cached_dev[ki] = dev;
+    }
+    vwalk::Params wp;
+    // input rows [h + 1, H - 1 - h): no border mapping routes a gradient there
+    if (!vwalk::plan(H, W, p.batch, k, 1, gout, gin, (int64_t)cached_blocks[ki] * (vwalk::kThreads / 32), wp, 1))
+        return TM_OK;
+    wp.sval = 0.f;
+    *done = true;
+    const int64_t blocks = std::min<int64_t>(ceil_div(wp.ntasks, vwalk::kThreads / 32), cached_blocks[ki]);
+    if (wp.ntasks > 0)
+        kern<<<(unsigned)blocks, vwalk::kThreads, 0, s>>>(gout, reinterpret_cast<const uint32_t *>(arg), gin, wp);
+    TM_LAUNCH_CHECK("vwalk_grad_kernel");
+    const vwalk::FrameRect fr{H, W, wp.ry0, wp.ry1, 4, W - 4};
+    TM_CHECK_CUDA(
+        launch_pdl(grad_frame_kernel, frame_grid(fr, p.batch), dim3(256), 0, s, gout, arg, gin, p, taps, fr));
+    return TM_OK;
+}
+
 // ------------------------------------------------------------- 2-D tiles
 // 2-D items: 128 x 32 tiles, 256 threads, one column and 16 rows per
 // thread.  The forward stages the input region the tile's taps read
@@ -700,6 +840,11 @@ int run_arg(const float *in, float *out, uint8_t *arg, int64_t batch, int ndim, 
     GradTaps taps;
     int st = build_grad_taps(MAX, batch, ndim, shape, structure, footprint, sshape, origin, mode, cval, &p, &taps);
     if (st != TM_OK) return st;
+    if (const int k = walk_box(p, taps, sshape, origin, true)) {
+        bool done = false;
+        st = run_arg_walk<MAX>(in, out, arg, p, taps, k, s, &done);
+        if (st != TM_OK || done) return st;
+    }
     Taps2D tp;
     if (make_taps2d(p, taps, false, &tp)) {
         const int P = pitch2d(tp.ext_x);
@@ -725,6 +870,11 @@ int run_grad(bool dilation, const float *gout, const uint8_t *arg, float *gin, i
     GradTaps taps;
     int st = build_grad_taps(dilation, batch, ndim, shape, nullptr, footprint, sshape, origin, mode, 0.f, &p, &taps);
     if (st != TM_OK) return st;
+    if (const int k = walk_box(p, taps, sshape, origin, false)) {
+        bool done = false;
+        st = run_grad_walk(dilation, gout, arg, gin, p, taps, k, s, &done);
+        if (st != TM_OK || done) return st;
+    }
     Taps2D tp;
     if (make_taps2d(p, taps, true, &tp)) {
         const int P = pitch2d(tp.ext_x);

@@ -42,6 +42,7 @@ constexpr int kChunk = 4;                   // input rows in flight per warp
 constexpr int kThreads = 256;
 constexpr int kTophatNone = 0, kTophatWhite = 1, kTophatBlack = 2;
 constexpr int kGradient = 1, kLaplace = 2;
+constexpr uint32_t kNoArg = 255u;  // no tap (every tap gave the identity)
 
 struct Params {
     int H, W;
@@ -234,6 +235,222 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks(STAGES, K, TOPHAT, COMBIN
     }
 }
 
+// ------------------------------------------ forward with argument, backward
+// The opt-in backward of grey erosion / dilation for the same centred K x K
+// flat boxes.  Tap t = K i + j of the footprint reads row y + dy_i and column
+// x + dx_j, dy_i = MAX ? h - i : i - h (dx likewise: dilation reads x - delta).
+//
+// Forward: the operator's value and the FIRST tap (raster order, strict
+// comparison) attaining it -- per input row the first column tap attaining
+// the row's extremum, then over the K rows the first row attaining the
+// overall one; the pair is the first tap overall.  Backward (gather): input
+// pixel p receives grad_out[o] from each output o = p - off_t whose recorded
+// tap is t, summed in tap order, for pixels no border mapping routes a
+// gradient to (rows [h + 1, H - 1 - h), columns [4, W - 4)); arguments are
+// read four to a 32-bit word (bytes).
+template <bool MAX, int K>
+__global__ void __launch_bounds__(kThreads, K == 3 ? 3 : 2)
+    vwalk_arg_kernel(const float *__restrict__ in, float *__restrict__ out, uint32_t *__restrict__ arg, Params p) {
+    using Op = MorphOp<float, MAX>;
+    constexpr int h = K / 2;
+    pdl_trigger();
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
+    for (int64_t t = (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); t < p.ntasks; t += nwarps) {
+        const int strip = (int)(t % p.nstrips);
+        const int64_t rest = t / p.nstrips;
+        const int rb = (int)(rest % p.nrb);
+        const int64_t item = rest / p.nrb;
+        const int c = strip * kStrip + 4 * lane;
+        const bool loads = c < p.W;
+        const bool writes = lane >= 1 && lane <= kLanesOut && c + 8 <= p.W;
+        const int ya = p.ry0 + rb * p.rows;
+        const int yb = min(ya + p.rows, p.ry1);
+        const int rs = ya - h, re = yb - 1 + h;
+        const int wq = p.W >> 2;
+        const float4 *src = reinterpret_cast<const float4 *>(in + item * (int64_t)p.H * p.W) + (c >> 2);
+        float4 *dst = reinterpret_cast<float4 *>(out + item * (int64_t)p.H * p.W) + (c >> 2);
+        uint32_t *adst = arg + ((item * (int64_t)p.H * p.W + c) >> 2);
+        float ring[K - 1][4];
+        uint32_t ringa[K - 1];
+        float4 cur[kChunk], nxt[kChunk];
+#pragma unroll
+        for (int k = 0; k < kChunk; k++)
+            cur[k] = (loads && rs + k <= re) ? __ldg(src + (int64_t)(rs + k) * wq) : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int r0 = rs; r0 <= re; r0 += kChunk) {
+            if (r0 + kChunk <= re) {
+#pragma unroll
+                for (int k = 0; k < kChunk; k++) {
+                    const int r = r0 + kChunk + k;
+                    nxt[k] = (loads && r <= re) ? __ldg(src + (int64_t)r * wq) : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kChunk; k++) {
+                const int r = r0 + k;
+                if (r > re) continue;
+                const float v[4] = {cur[k].x, cur[k].y, cur[k].z, cur[k].w};
+                float a[4 + 2 * h];
+                extend<h>(v, a);
+                // row pass: first column tap attaining the row's extremum
+                float rb4[4];
+                uint32_t ra = 0u;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    float b = Op::identity();
+                    uint32_t bj = kNoArg;
+#pragma unroll
+                    for (int j = 0; j < K; j++) {
+                        const int dx = MAX ? h - j : j - h;
+                        const float val = Op::apply(a[q + h + dx], p.sval);
+                        if (MAX ? val > b : val < b) {
+                            b = val;
+                            bj = (uint32_t)j;
+                        }
+                    }
+                    rb4[q] = b;
+                    ra |= bj << (8 * q);
+                }
+                if (r - rs >= 2 * h && writes) {
+                    // rows r - 2h .. r: ring[0 .. K-2], then this row (window index w)
+                    float o[4];
+                    uint32_t oa = 0u;
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        float B = Op::identity();
+                        uint32_t A = kNoArg;
+#pragma unroll
+                        for (int i = 0; i < K; i++) {
+                            const int w = MAX ? 2 * h - i : i;  // row y + dy_i, y = r - h
+                            const float rv = w == K - 1 ? rb4[q] : ring[w][q];
+                            const uint32_t rj = ((w == K - 1 ? ra : ringa[w]) >> (8 * q)) & 255u;
+                            if (MAX ? rv > B : rv < B) {
+                                B = rv;
+                                A = (uint32_t)(K * i) + rj;
+                            }
+                        }
+                        o[q] = B;
+                        oa |= A << (8 * q);
+                    }
+                    __stcs(dst + (int64_t)(r - h) * wq, make_float4(o[0], o[1], o[2], o[3]));
+                    __stcs(adst + (int64_t)(r - h) * wq, oa);
+                }
+#pragma unroll
+                for (int j = 0; j + 1 < K - 1; j++) {
+#pragma unroll
+                    for (int q = 0; q < 4; q++) ring[j][q] = ring[j + 1][q];
+                    ringa[j] = ringa[j + 1];
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++) ring[K - 2][q] = rb4[q];
+                ringa[K - 2] = ra;
+            }
+#pragma unroll
+            for (int k = 0; k < kChunk; k++) cur[k] = nxt[k];
+        }
+    }
+}
+
+template <bool MAX, int K>
+__global__ void __launch_bounds__(kThreads, K == 3 ? 2 : 1)
+    vwalk_grad_kernel(const float *__restrict__ gout, const uint32_t *__restrict__ arg, float *__restrict__ gin,
+                      Params p) {
+    constexpr int h = K / 2;
+    pdl_trigger();
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
+    for (int64_t t = (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); t < p.ntasks; t += nwarps) {
+        const int strip = (int)(t % p.nstrips);
+        const int64_t rest = t / p.nstrips;
+        const int rb = (int)(rest % p.nrb);
+        const int64_t item = rest / p.nrb;
+        const int c = strip * kStrip + 4 * lane;
+        const bool loads = c < p.W;
+        const bool writes = lane >= 1 && lane <= kLanesOut && c + 8 <= p.W;
+        const int ya = p.ry0 + rb * p.rows;  // input rows written
+        const int yb = min(ya + p.rows, p.ry1);
+        const int rs = ya - h, re = yb - 1 + h;  // output rows read
+        const int wq = p.W >> 2;
+        const int64_t base4 = (item * (int64_t)p.H * p.W + c) >> 2;
+        const float4 *gsrc = reinterpret_cast<const float4 *>(gout) + base4;
+        const uint32_t *asrc = arg + base4;
+        float4 *dst = reinterpret_cast<float4 *>(gin) + base4;
+        // window rows r - 2h .. r: gradients with h columns each side, and the
+        // argument words of the lane and its two neighbours
+        float rg[K - 1][4 + 2 * h];
+        uint32_t raw[K - 1][3];
+        float4 cg[kChunk], ng[kChunk];
+        uint32_t ca[kChunk], na[kChunk];
+#pragma unroll
+        for (int k = 0; k < kChunk; k++) {
+            const bool ok = loads && rs + k <= re;
+            cg[k] = ok ? __ldg(gsrc + (int64_t)(rs + k) * wq) : make_float4(0.f, 0.f, 0.f, 0.f);
+            ca[k] = ok ? __ldg(asrc + (int64_t)(rs + k) * wq) : 0xffffffffu;
+        }
+        for (int r0 = rs; r0 <= re; r0 += kChunk) {
+            if (r0 + kChunk <= re) {
+#pragma unroll
+                for (int k = 0; k < kChunk; k++) {
+                    const int r = r0 + kChunk + k;
+                    const bool ok = loads && r <= re;
+                    ng[k] = ok ? __ldg(gsrc + (int64_t)r * wq) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    na[k] = ok ? __ldg(asrc + (int64_t)r * wq) : 0xffffffffu;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kChunk; k++) {
+                const int r = r0 + k;
+                if (r > re) continue;
+                const float v[4] = {cg[k].x, cg[k].y, cg[k].z, cg[k].w};
+                float ge[4 + 2 * h];
+                extend<h>(v, ge);
+                const uint32_t aw[3] = {__shfl_up_sync(0xffffffffu, ca[k], 1), ca[k],
+                                        __shfl_down_sync(0xffffffffu, ca[k], 1)};
+                if (r - rs >= 2 * h && writes) {
+                    // input row r - h: tap (i, j) came from output row
+                    // r - h - dy_i (window index w) and column x - dx_j
+                    float acc[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        float s = 0.f;
+#pragma unroll
+                        for (int i = 0; i < K; i++) {
+                            const int w = MAX ? i : 2 * h - i;
+#pragma unroll
+                            for (int j = 0; j < K; j++) {
+                                const int kx = q - (MAX ? h - j : j - h);  // column offset from c, in [-h, 3 + h]
+                                const int word = kx < 0 ? 0 : (kx < 4 ? 1 : 2);
+                                const int byte = kx - 4 * (word - 1);
+                                const uint32_t wv = w == K - 1 ? aw[word] : raw[w][word];
+                                const float gv = w == K - 1 ? ge[kx + h] : rg[w][kx + h];
+                                if (((wv >> (8 * byte)) & 255u) == (uint32_t)(K * i + j)) s += gv;
+                            }
+                        }
+                        acc[q] = s;
+                    }
+                    __stcs(dst + (int64_t)(r - h) * wq, make_float4(acc[0], acc[1], acc[2], acc[3]));
+                }
+#pragma unroll
+                for (int j = 0; j + 1 < K - 1; j++) {
+#pragma unroll
+                    for (int q = 0; q < 4 + 2 * h; q++) rg[j][q] = rg[j + 1][q];
+#pragma unroll
+                    for (int q = 0; q < 3; q++) raw[j][q] = raw[j + 1][q];
+                }
+#pragma unroll
+                for (int q = 0; q < 4 + 2 * h; q++) rg[K - 2][q] = ge[q];
+#pragma unroll
+                for (int q = 0; q < 3; q++) raw[K - 2][q] = aw[q];
+            }
+#pragma unroll
+            for (int k = 0; k < kChunk; k++) {
+                cg[k] = ng[k];
+                ca[k] = na[k];
+            }
+        }
+    }
+}
+
 // Outputs outside the walkers' rectangle [ry0, ry1) x [rx0, rx1) (a frame a
 // few voxels wide), one thread each, straight from the definition with the
 // border mode at both levels: the first operator over the input (rows
@@ -380,31 +597,42 @@ __device__ __forceinline__ float frame_value(const float *src, const FrameParams
     }
 }
 
+// Position (y, x) of the k-th of the H x W positions outside the rectangle
+// [ry0, ry1) x [rx0, rx1): the rows above, the side columns of the rows in
+// between, the rows below.
+struct FrameRect {
+    int H, W, ry0, ry1, rx0, rx1;
+    __host__ __device__ int count() const { return H * W - (ry1 - ry0) * (rx1 - rx0); }
+    __device__ __forceinline__ void at(int k, int &y, int &x) const {
+        const int side = rx0 + (W - rx1), top = ry0 * W, mid = (ry1 - ry0) * side;
+        if (k < top) {
+            y = k / W;
+            x = k - y * W;
+        } else if ((k -= top) < mid) {
+            const int r = k / side;
+            y = ry0 + r;
+            x = k - r * side;
+            if (x >= rx0) x += rx1 - rx0;
+        } else {
+            k -= mid;
+            const int r = k / W;
+            y = ry1 + r;
+            x = k - r * W;
+        }
+    }
+};
+
 template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE>
 __global__ void __launch_bounds__(256) frame_kernel(const float *__restrict__ in, float *__restrict__ out,
                                                     FrameParams f) {
-    const int ring = f.H * f.W - (f.ry1 - f.ry0) * (f.rx1 - f.rx0);
-    const int side = f.rx0 + (f.W - f.rx1);
-    const int top = f.ry0 * f.W, mid = (f.ry1 - f.ry0) * side;
+    const FrameRect fr{f.H, f.W, f.ry0, f.ry1, f.rx0, f.rx1};
+    const int ring = fr.count();
     for (int64_t item = blockIdx.y; item < f.batch; item += gridDim.y) {
         const float *src = in + item * (int64_t)f.H * f.W;
         float *dst = out + item * (int64_t)f.H * f.W;
         for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ring; k += gridDim.x * blockDim.x) {
-            int y, x, q = k;
-            if (q < top) {
-                y = q / f.W;
-                x = q - y * f.W;
-            } else if ((q -= top) < mid) {
-                const int r = q / side;
-                y = f.ry0 + r;
-                x = q - r * side;
-                if (x >= f.rx0) x += f.rx1 - f.rx0;
-            } else {
-                q -= mid;
-                const int r = q / f.W;
-                y = f.ry1 + r;
-                x = q - r * f.W;
-            }
+            int y, x;
+            fr.at(k, y, x);
             dst[(int64_t)y * f.W + x] = frame_value<MAX1, STAGES, TOPHAT, K, COMBINE>(src, f, y, x);
         }
     }
@@ -451,16 +679,17 @@ int launch_frame(const float *in, float *out, const FrameParams &f, cudaStream_t
 // aligned, too narrow or too short).  resident_warps is the number of walker
 // warps the device holds at once; the row block is chosen so the tasks fill
 // whole waves of them.
+// margin: rows kept out of the walk beyond the lag on each side.
 inline bool plan(int H, int W, int64_t batch, int K, int stages, const void *in, const void *out,
-                 int64_t resident_warps, Params &p) {
+                 int64_t resident_warps, Params &p, int margin = 0) {
     const int lag = stages * (K / 2);
-    if (W % 4 != 0 || W < 16 || H < 2 * lag + 1) return false;
+    if (W % 4 != 0 || W < 16 || H < 2 * (lag + margin) + 1) return false;
     if ((reinterpret_cast<uintptr_t>(in) & 15) || (reinterpret_cast<uintptr_t>(out) & 15)) return false;
     p.H = H;
     p.W = W;
     p.batch = batch;
-    p.ry0 = lag;
-    p.ry1 = H - lag;
+    p.ry0 = lag + margin;
+    p.ry1 = H - lag - margin;
     p.nstrips = (W - 8 + kStrip - 1) / kStrip;
     const int rows = p.ry1 - p.ry0;
     // cost of a candidate row block: waves of tasks x rows each task reads
