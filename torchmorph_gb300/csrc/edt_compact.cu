@@ -1664,13 +1664,14 @@ __global__ void __launch_bounds__(kShellCtThreads) edt_shell_ct_kernel(const uin
                     i1[q] = y0 + r + (int)((c >> 4) & 15u) - 8;
                     i2[q] = x + q + (int)((c >> 8) & 15u) - 8;
                 }
+                // streaming stores: the outputs are not read again by this call
                 const int64_t gi = rowbase + (int64_t)r * W + x;
-                if (dist) *reinterpret_cast<float4 *>(dist + gi) = make_float4(dv[0], dv[1], dv[2], dv[3]);
-                if (sqdist) *reinterpret_cast<int4 *>(sqdist + gi) = make_int4(sq[0], sq[1], sq[2], sq[3]);
+                if (dist) __stcs(reinterpret_cast<float4 *>(dist + gi), make_float4(dv[0], dv[1], dv[2], dv[3]));
+                if (sqdist) __stcs(reinterpret_cast<int4 *>(sqdist + gi), make_int4(sq[0], sq[1], sq[2], sq[3]));
                 if (indices) {
-                    *reinterpret_cast<int4 *>(indices + gi) = make_int4(i0[0], i0[1], i0[2], i0[3]);
-                    *reinterpret_cast<int4 *>(indices + numel + gi) = make_int4(i1[0], i1[1], i1[2], i1[3]);
-                    *reinterpret_cast<int4 *>(indices + 2 * numel + gi) = make_int4(i2[0], i2[1], i2[2], i2[3]);
+                    __stcs(reinterpret_cast<int4 *>(indices + gi), make_int4(i0[0], i0[1], i0[2], i0[3]));
+                    __stcs(reinterpret_cast<int4 *>(indices + numel + gi), make_int4(i1[0], i1[1], i1[2], i1[3]));
+                    __stcs(reinterpret_cast<int4 *>(indices + 2 * numel + gi), make_int4(i2[0], i2[1], i2[2], i2[3]));
                 }
             }
         }
