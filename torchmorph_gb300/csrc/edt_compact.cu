@@ -1900,7 +1900,7 @@ __global__ void __launch_bounds__(kShellThreads) cdt_shell_kernel(const uint32_t
             d.y = divisor == 1.f ? (float)((v4 >> 8) & 255u) : (float)((v4 >> 8) & 255u) / divisor;
             d.z = divisor == 1.f ? (float)((v4 >> 16) & 255u) : (float)((v4 >> 16) & 255u) / divisor;
             d.w = divisor == 1.f ? (float)(v4 >> 24) : (float)(v4 >> 24) / divisor;
-            *reinterpret_cast<float4 *>(dist + rowbase + (int64_t)r * W + x) = d;
+            __stcs(reinterpret_cast<float4 *>(dist + rowbase + (int64_t)r * W + x), d);
         }
     }
     if (nfar == 0) return;
@@ -2098,7 +2098,7 @@ __global__ void __launch_bounds__(kShellCtThreads) cdt_shell_warp_kernel(const u
                 d.y = divisor == 1.f ? (float)((acc >> 8) & 255u) : (float)((acc >> 8) & 255u) / divisor;
                 d.z = divisor == 1.f ? (float)((acc >> 16) & 255u) : (float)((acc >> 16) & 255u) / divisor;
                 d.w = divisor == 1.f ? (float)(acc >> 24) : (float)(acc >> 24) / divisor;
-                *reinterpret_cast<float4 *>(dist + rowbase + (int64_t)r * W + x) = d;
+                __stcs(reinterpret_cast<float4 *>(dist + rowbase + (int64_t)r * W + x), d);
             }
         }
         if (nfar) {
