@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(kBThreads) bitmorph_kernel(const uint8_t *__re
             const int x = x0 + 4 * lane;
             uint8_t *row = dst + (int64_t)y * W;
             if ((reinterpret_cast<uintptr_t>(row + x0) & 3) == 0 && x + 3 < W) {
-                *reinterpret_cast<uint32_t *>(row + x) = bytes;
+                __stcs(reinterpret_cast<unsigned int *>(row + x), bytes);
             } else {
 #pragma unroll
                 for (int k = 0; k < 4; k++)
@@ -377,8 +377,8 @@ __global__ void __launch_bounds__(256) bitwalk_kernel(const uint8_t *__restrict_
                     uint32_t b[8];
 #pragma unroll
                     for (int i = 0; i < 8; i++) b[i] = (((v >> (4 * i)) & 15u) * 0x00204081u) & 0x01010101u;
-                    *reinterpret_cast<uint4 *>(p) = make_uint4(b[0], b[1], b[2], b[3]);
-                    if (a.W - 32 * wi > 16) *reinterpret_cast<uint4 *>(p + 16) = make_uint4(b[4], b[5], b[6], b[7]);
+                    __stcs(reinterpret_cast<uint4 *>(p), make_uint4(b[0], b[1], b[2], b[3]));
+                    if (a.W - 32 * wi > 16) __stcs(reinterpret_cast<uint4 *>(p + 16), make_uint4(b[4], b[5], b[6], b[7]));
                 }
                 continue;
             }
@@ -406,8 +406,8 @@ __global__ void __launch_bounds__(256) bitwalk_kernel(const uint8_t *__restrict_
                 uint32_t b[8];
 #pragma unroll
                 for (int i = 0; i < 8; i++) b[i] = (((o >> (4 * i)) & 15u) * 0x00204081u) & 0x01010101u;
-                *reinterpret_cast<uint4 *>(p) = make_uint4(b[0], b[1], b[2], b[3]);
-                if (a.W - 32 * wi > 16) *reinterpret_cast<uint4 *>(p + 16) = make_uint4(b[4], b[5], b[6], b[7]);
+                __stcs(reinterpret_cast<uint4 *>(p), make_uint4(b[0], b[1], b[2], b[3]));
+                if (a.W - 32 * wi > 16) __stcs(reinterpret_cast<uint4 *>(p + 16), make_uint4(b[4], b[5], b[6], b[7]));
             }
           }
         }

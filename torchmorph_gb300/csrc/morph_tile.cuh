@@ -183,7 +183,7 @@ __device__ __forceinline__ void flat_tile_compute(const T *tile, int ld, T *rows
 #pragma unroll
             for (int j = 0; j < kRun; j++) {
                 int gy = y0 + r + j;
-                if (gy < p.H) dst[(int64_t)gy * p.W + gx] = MorphOp<T, MAX>::apply(res[j], p.sval);
+                if (gy < p.H) __stcs(dst + (int64_t)gy * p.W + gx, MorphOp<T, MAX>::apply(res[j], p.sval));
             }
         }
     }
@@ -225,7 +225,7 @@ __device__ __forceinline__ void flat_tile_walk(const T *tile, int ld, const Flat
         T v = h[0];
 #pragma unroll
         for (int k = 1; k < KH; k++) v = Op::combine(v, h[k]);
-        if (r < rows_left) o[(int64_t)r * p.W] = Op::apply(v, p.sval);
+        if (r < rows_left) __stcs(o + (int64_t)r * p.W, Op::apply(v, p.sval));  // outputs: streaming stores
 #pragma unroll
         for (int k = 0; k < KH - 1; k++) h[k] = h[k + 1];
     }
