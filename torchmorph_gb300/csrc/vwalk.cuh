@@ -117,8 +117,8 @@ __device__ __forceinline__ void col_window(float (&ring)[K - 1][4], const float 
 // 80 registers (three blocks: the loads in flight of 24 warps matter more
 // than a few spilled values) unless they hold input rows (laplace: 128),
 // 5 x 5 one-stage walks 128, two stages of 5 x 5 more (one block).
-constexpr int kMinBlocks(int stages, int k, int tophat, int combine) {
-    return k == 3 ? (combine == 2 ? 2 : 3) : (stages == 1 ? 2 : 1);
+constexpr int kMinBlocks(int stages, int k, int combine) {
+    return k == 3 ? (combine == kLaplace ? 2 : 3) : (stages == 1 ? 2 : 1);
 }
 
 // One task: output rows [ya, yb) of the strip at the lane's columns.
@@ -214,9 +214,9 @@ __device__ __forceinline__ void walk_task(const float4 *src, float4 *dst, int ya
 // COMBINE: 0 the operators alone; kGradient dilation - erosion, kLaplace
 // (dilation + erosion) - 2 x, both of one stage over the same window.
 template <bool MAX1, int STAGES, int TOPHAT, int K, int COMBINE = 0>
-__global__ void __launch_bounds__(kThreads, kMinBlocks(STAGES, K, TOPHAT, COMBINE))
+__global__ void __launch_bounds__(kThreads, kMinBlocks(STAGES, K, COMBINE))
     vwalk_kernel(const float *__restrict__ in, float *__restrict__ out, Params p) {
-    pdl_trigger();  // the frame kernel may fill the SMs as this grid's CTAs retire
+    pdl_trigger();  // the frame kernel launched behind this grid may start now
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
     for (int64_t t = (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); t < p.ntasks; t += nwarps) {
